@@ -1,0 +1,257 @@
+"""numpy front-end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/_build/liboracle.so`` (the C restatement in hala_oracle.c) and, when it was built
+in a container that holds the reference sources, ``oracle/_ref/libhalaref.so`` (the reference's
+own CPU templates, see oracle/ref/).  Only tests/, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline leg import this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libhalaref.so")
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
+
+
+def build():
+    """Compile the C restatement (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = C.CDLL(LIB_PATH)
+    i, c, vp = C.c_int, C.c_char, C.c_void_p
+    lib.or_diag_index.argtypes = [i, _i32p, _i32p, _i32p]
+    lib.or_diag_index.restype = i
+    lib.or_split_pattern.argtypes = [i, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]
+    lib.or_levels.argtypes = [i, _i32p, _i32p, _i32p, c, _i32p]
+    lib.or_levels.restype = i
+    lib.or_ilu_factor_pivot_d.argtypes = [i, _i32p, _i32p, _i32p, _f64p]
+    lib.or_spmv_bf16f32.argtypes = [c, i, i, C.c_float, _i32p, _i32p, _u16p, _f32p, C.c_float, _f32p]
+    for s, fp, ft in (("d", _f64p, C.c_double), ("f", _f32p, C.c_float)):
+        getattr(lib, f"or_spmv_{s}").argtypes = [c, i, i, ft, _i32p, _i32p, fp, fp, ft, fp]
+        getattr(lib, f"or_split_values_{s}").argtypes = [c, c, i, _i32p, fp, _i32p, _i32p, fp, fp]
+        getattr(lib, f"or_ilu_factor_{s}").argtypes = [i, _i32p, _i32p, _i32p, fp]
+        getattr(lib, f"or_ilu_factor_{s}").restype = i
+        getattr(lib, f"or_ilu_apply_{s}").argtypes = [i, _i32p, _i32p, _i32p, fp, fp]
+        getattr(lib, f"or_ilu_apply_t_{s}").argtypes = [i, _i32p, _i32p, _i32p, fp, fp]
+        getattr(lib, f"or_trsv_{s}").argtypes = [c, c, c, i, ft, _i32p, _i32p, fp, fp, fp]
+        getattr(lib, f"or_dot_{s}").argtypes = [i, fp, fp]
+        getattr(lib, f"or_dot_{s}").restype = ft
+        getattr(lib, f"or_nrm2_{s}").argtypes = [i, fp]
+        getattr(lib, f"or_nrm2_{s}").restype = ft
+        getattr(lib, f"or_cg_{s}").argtypes = [i, _i32p, _i32p, fp, vp, vp, fp, fp, ft, i, C.POINTER(ft)]
+        getattr(lib, f"or_cg_{s}").restype = i
+        getattr(lib, f"or_gmres_{s}").argtypes = [i, _i32p, _i32p, fp, vp, vp, i, fp, fp, ft, i]
+        getattr(lib, f"or_gmres_{s}").restype = i
+    lib.or_ir_pcg.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, _f64p, _f64p,
+                              C.c_double, C.c_double, i, i, C.POINTER(i)]
+    lib.or_ir_pcg.restype = i
+    return lib
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = _load()
+    return _lib
+
+
+def _sfx(dtype):
+    return "d" if np.dtype(dtype) == np.float64 else "f"
+
+
+def _b(ch):
+    return ch.encode() if isinstance(ch, str) else ch
+
+
+def diag_index(pntr, indx):
+    n = len(pntr) - 1
+    d = np.zeros(n, np.int32)
+    st = lib().or_diag_index(n, pntr, indx, d)
+    if st != 0:
+        raise ValueError(f"row {-st - 1} has no diagonal entry")
+    return d
+
+
+def split_pattern(pntr, indx, diag):
+    n = len(pntr) - 1
+    nnz = int(pntr[-1])
+    up = np.zeros(n + 1, np.int32); lp = np.zeros(n + 1, np.int32)
+    ui = np.zeros(nnz + n, np.int32); li = np.zeros(nnz + n, np.int32)
+    lib().or_split_pattern(n, pntr, indx, diag, up, ui, lp, li)
+    return up, ui[: up[-1]].copy(), lp, li[: lp[-1]].copy()
+
+
+def split_values(uplo, diagc, pntr, vals, up, lp):
+    n = len(pntr) - 1
+    uv = np.zeros(int(up[-1]), vals.dtype); lv = np.zeros(int(lp[-1]), vals.dtype)
+    getattr(lib(), f"or_split_values_{_sfx(vals.dtype)}")(_b(uplo), _b(diagc), n, pntr, vals, up, lp, uv, lv)
+    return uv, lv
+
+
+def levels(pntr, indx, diag, uplo):
+    n = len(pntr) - 1
+    lev = np.zeros(n, np.int32)
+    nl = lib().or_levels(n, pntr, indx, diag, _b(uplo), lev)
+    return lev, nl
+
+
+def spmv(trans, m, ncols, alpha, pntr, indx, vals, x, beta, y=None):
+    out_len = m if trans in ("N", "n") else ncols
+    y = np.zeros(out_len, vals.dtype) if y is None else np.array(y, vals.dtype)
+    getattr(lib(), f"or_spmv_{_sfx(vals.dtype)}")(_b(trans), m, ncols, alpha, pntr, indx, vals,
+                                                  np.ascontiguousarray(x, vals.dtype), beta, y)
+    return y
+
+
+def spmv_bf16f32(trans, m, ncols, alpha, pntr, indx, vals_bf16, x, beta, y=None):
+    out_len = m if trans in ("N", "n") else ncols
+    y = np.zeros(out_len, np.float32) if y is None else np.array(y, np.float32)
+    lib().or_spmv_bf16f32(_b(trans), m, ncols, alpha, pntr, indx, vals_bf16,
+                          np.ascontiguousarray(x, np.float32), beta, y)
+    return y
+
+
+def f32_to_bf16(a):
+    """Round-to-nearest-even float32 -> bfloat16 bit pattern (uint16), vectorised."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    nan = (u & 0x7FFFFFFF) > 0x7F800000
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    r[nan] = ((u[nan] >> 16) | 0x40).astype(np.uint16)
+    return r
+
+
+def bf16_to_f32(b):
+    return (np.asarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def ilu_factor(pntr, indx, vals, diag=None):
+    """Row-wise restatement of factorize_ilu (bit-identical to the reference loop)."""
+    diag = diag_index(pntr, indx) if diag is None else diag
+    n = len(pntr) - 1
+    f = np.array(vals, copy=True)
+    st = getattr(lib(), f"or_ilu_factor_{_sfx(vals.dtype)}")(n, pntr, indx, diag, f)
+    return f, diag, st
+
+
+def ilu_factor_pivot(pntr, indx, vals, diag):
+    """The reference's own O(n^2) loop, restated (small n only)."""
+    f = np.array(vals, np.float64, copy=True)
+    lib().or_ilu_factor_pivot_d(len(pntr) - 1, pntr, indx, diag, f)
+    return f
+
+
+def ilu_apply(pntr, indx, diag, ilu, x, trans="N"):
+    n = len(pntr) - 1
+    y = np.array(x, ilu.dtype, copy=True)
+    fn = "or_ilu_apply_" if trans in ("N", "n") else "or_ilu_apply_t_"
+    getattr(lib(), fn + _sfx(ilu.dtype))(n, pntr, indx, diag, ilu, y)
+    return y
+
+
+def trsv(uplo, diagc, trans, alpha, pntr, indx, vals, b):
+    n = len(pntr) - 1
+    x = np.zeros(n, vals.dtype)
+    getattr(lib(), f"or_trsv_{_sfx(vals.dtype)}")(_b(uplo), _b(diagc), _b(trans), n, alpha, pntr,
+                                                  indx, vals, np.ascontiguousarray(b, vals.dtype), x)
+    return x
+
+
+def dot(x, y):
+    return getattr(lib(), f"or_dot_{_sfx(x.dtype)}")(len(x), x, np.ascontiguousarray(y, x.dtype))
+
+
+def nrm2(x):
+    return getattr(lib(), f"or_nrm2_{_sfx(x.dtype)}")(len(x), x)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def cg(pntr, indx, vals, b, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):
+    """solve_cg / solve_cg_ilu restated.  Returns (x, iterations, final ||r||)."""
+    n = len(pntr) - 1
+    x = np.zeros(n, vals.dtype) if x0 is None else np.array(x0, vals.dtype, copy=True)
+    ft = C.c_double if vals.dtype == np.float64 else C.c_float
+    res = ft(0)
+    it = getattr(lib(), f"or_cg_{_sfx(vals.dtype)}")(n, pntr, indx, vals, _ptr(diag), _ptr(ilu),
+                                                     np.ascontiguousarray(b, vals.dtype), x, tol,
+                                                     max_iter, C.byref(res))
+    return x, it, res.value
+
+
+def gmres(pntr, indx, vals, b, restart, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):
+    """solve_gmres / solve_gmres_ilu restated.  Returns (x, total applications)."""
+    n = len(pntr) - 1
+    x = np.zeros(n, vals.dtype) if x0 is None else np.array(x0, vals.dtype, copy=True)
+    it = getattr(lib(), f"or_gmres_{_sfx(vals.dtype)}")(n, pntr, indx, vals, _ptr(diag), _ptr(ilu),
+                                                        restart, np.ascontiguousarray(b, vals.dtype),
+                                                        x, tol, max_iter)
+    return x, it
+
+
+def ir_pcg(pntr, indx, vals, vals32, diag, ilu32, piv, b, tol, inner_rtol=1e-4, max_inner=100000,
+           max_outer=50, x0=None):
+    n = len(pntr) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    outer = C.c_int(0)
+    tot = lib().or_ir_pcg(n, pntr, indx, vals, vals32, diag, ilu32, piv, b, x, tol, inner_rtol,
+                          max_inner, max_outer, C.byref(outer))
+    return x, tot, outer.value
+
+
+# ---------------------------------------------------------------- reference (oracle/_ref) ---
+
+_ref = None
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    """The reference's own CPU templates (oracle/_ref/libhalaref.so), or None when not built."""
+    global _ref
+    if _ref is None and ref_available():
+        r = C.CDLL(REF_PATH)
+        i, c, vp = C.c_int, C.c_char, C.c_void_p
+        r.ref_sparse_gemv_d.argtypes = [c, i, i, C.c_double, _i32p, _i32p, _f64p, _f64p, C.c_double, _f64p]
+        r.ref_sparse_gemv_f.argtypes = [c, i, i, C.c_float, _i32p, _i32p, _f32p, _f32p, C.c_float, _f32p]
+        r.ref_get_diagonal_index.argtypes = [i, _i32p, _i32p, _i32p]
+        r.ref_split_pattern.argtypes = [i, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p,
+                                        C.POINTER(i), C.POINTER(i)]
+        r.ref_split_values_d.argtypes = [c, c, i, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p]
+        r.ref_factorize_ilu_d.argtypes = [i, _i32p, _i32p, _f64p, _f64p]
+        r.ref_factorize_ilu_f.argtypes = [i, _i32p, _i32p, _f32p, _f32p]
+        r.ref_apply_ilu_d.argtypes = [i, _i32p, _i32p, _i32p, _f64p, _f64p]
+        r.ref_apply_ilu_f.argtypes = [i, _i32p, _i32p, _i32p, _f32p, _f32p]
+        r.ref_trsv_d.argtypes = [c, c, c, i, C.c_double, _i32p, _i32p, _f64p, _f64p, _f64p]
+        r.ref_solve_cg_d.argtypes = [i, _i32p, _i32p, _f64p, vp, vp, _f64p, _f64p, C.c_double, i]
+        r.ref_solve_cg_d.restype = i
+        r.ref_solve_cg_f.argtypes = [i, _i32p, _i32p, _f32p, vp, vp, _f32p, _f32p, C.c_float, i]
+        r.ref_solve_cg_f.restype = i
+        r.ref_solve_gmres_d.argtypes = [i, _i32p, _i32p, _f64p, vp, vp, i, _f64p, _f64p, C.c_double, i]
+        r.ref_solve_gmres_d.restype = i
+        r.ref_solve_gmres_f.argtypes = [i, _i32p, _i32p, _f32p, vp, vp, i, _f32p, _f32p, C.c_float, i]
+        r.ref_solve_gmres_f.restype = i
+        r.ref_solve_batch_cg_ilu_d.argtypes = [i, _i32p, _i32p, _f64p, i, _f64p, _f64p, C.c_double, i]
+        r.ref_solve_batch_cg_ilu_d.restype = i
+        _ref = r
+    return _ref
