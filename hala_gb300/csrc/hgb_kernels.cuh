@@ -1,0 +1,120 @@
+// Kernel-level building blocks shared between libhgb translation units.
+#pragma once
+
+#include "hgb_internal.cuh"
+
+namespace hgb {
+
+// ------------------------------------------------------------ TMA / mbarrier helpers ----
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 1D bulk copy global -> shared, completion signalled on bar.  dst, src 16B aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Bounded wait on a bulk-copy barrier.  A copy that never lands (it cannot, for in-bounds
+// aligned copies) would otherwise hang; on the limit the error word is set and the caller
+// proceeds with whatever the buffer holds, so the launch terminates.
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+    long spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++spins > (1L << 22)) {
+            atomicOr(err, DEV_ERR_TMA);
+            return;
+        }
+    }
+}
+
+template <typename V> struct Val;
+template <> struct Val<double> {
+    using X = double;
+    __device__ static double get(double v) { return v; }
+};
+template <> struct Val<float> {
+    using X = float;
+    __device__ static float get(float v) { return v; }
+};
+template <> struct Val<uint16_t> {   // bfloat16 bit pattern
+    using X = float;
+    __device__ static float get(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
+};
+
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+
+// Cached transpose of a CSR pattern: pntr[n+1], row[nnz] (original row of each entry, ascending
+// inside a transposed row) and map[nnz] (position of the entry in the original arrays).
+struct Transpose {
+    int n = 0;
+    int *pntr = nullptr, *row = nullptr, *map = nullptr;
+    void release();
+};
+
+// opt the SpMV kernels into their dynamic shared memory size (once per process, before capture)
+int spmv_init_attributes();
+
+int exclusive_scan(hgb_ctx *c, const int *in, int *out, int n, int *total_dev, int *scratch);
+int csr_check(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx);
+int build_transpose(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                    Transpose &T);
+
+template <typename V>
+int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                  typename Val<V>::X *y, double *dot_out, const int *skip = nullptr);
+template <typename V>
+int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                  typename Val<V>::X *y, const Transpose *T);
+
+// ILU internals used by the fused solvers (skip: device flag that turns the launches into no-ops)
+int ilu_apply_internal(hgb_ilu *M, char trans, const void *x, void *r, const int *skip = nullptr);
+hgb_dtype ilu_store(const hgb_ilu *M);
+int ilu_n(const hgb_ilu *M);
+
+// accessors of the opaque matrix handle
+const int *csr_pntr(const hgb_csr *A);
+const int *csr_indx(const hgb_csr *A);
+const void *csr_vals(const hgb_csr *A);
+int csr_rows(const hgb_csr *A);
+int csr_cols(const hgb_csr *A);
+int csr_nnz(const hgb_csr *A);
+hgb_dtype csr_dtype(const hgb_csr *A);
+hgb_ctx *csr_ctx(const hgb_csr *A);
+
+}  // namespace hgb

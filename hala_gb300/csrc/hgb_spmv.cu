@@ -1,0 +1,492 @@
+// CSR SpMV for sm_103a: row tiles staged into shared memory by the TMA bulk-copy engine
+// (cp.async.bulk + mbarrier, double-buffered, persistent CTAs), one thread per row summing its
+// entries sequentially with separately rounded multiply and add.  That is the arithmetic of the
+// reference's sparse_gemv_array<T,'N'> (sparse/hala_sparse_utils.hpp:104-112), so FP64 results
+// are bit-identical to the reference CPU path while the DRAM stream stays fully coalesced.
+#include "hgb_internal.cuh"
+#include "hgb_kernels.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace hgb {
+
+constexpr int kSpmvRows = 256;              // rows (threads) per tile
+constexpr int kSpmvSmem = 72 * 1024;        // dynamic smem per CTA: 3 CTAs per SM
+
+template <typename V>
+__host__ __device__ constexpr int spmv_cap() {
+    // entries per stage: two stages of (vals + indx) fit in kSpmvSmem with 8 entries of slack
+    return (kSpmvSmem / (2 * (int)(sizeof(V) + sizeof(int)))) / 16 * 16 - 16;
+}
+
+template <typename V>
+struct TileGeom {
+    int s, e;           // nnz range of the tile
+    int sv, ev;         // staged range of vals (aligned to 16 bytes), ev == sv when not staged
+    int si, ei;         // staged range of indx
+};
+
+template <typename V>
+__device__ __forceinline__ TileGeom<V> tile_geom(const int *pntr, int n_rows, int tile, bool tma) {
+    constexpr int VA = 16 / sizeof(V);
+    TileGeom<V> g;
+    int r0 = tile * kSpmvRows;
+    int r1 = min(r0 + kSpmvRows, n_rows);
+    g.s = __ldg(pntr + r0);
+    g.e = __ldg(pntr + r1);
+    bool staged = tma && (g.e - g.s) <= spmv_cap<V>();
+    g.sv = g.s & ~(VA - 1);
+    g.ev = staged ? (g.e & ~(VA - 1)) : g.sv;
+    g.si = g.s & ~3;
+    g.ei = staged ? (g.e & ~3) : g.si;
+    return g;
+}
+
+template <typename V>
+__device__ __forceinline__ void issue_tile(const TileGeom<V> &g, const V *vals, const int *indx, V *sv,
+                                           int *si, uint64_t *bar) {
+    uint32_t bv = (uint32_t)(g.ev - g.sv) * sizeof(V);
+    uint32_t bi = (uint32_t)(g.ei - g.si) * sizeof(int);
+    if (bv + bi == 0) {
+        mbar_arrive(bar);
+        return;
+    }
+    mbar_arrive_tx(bar, bv + bi);
+    if (bv) bulk_g2s(sv, vals + g.sv, bv, bar);
+    if (bi) bulk_g2s(si, indx + g.si, bi, bar);
+}
+
+// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (rows of A index x: square A).
+template <typename V, bool FUSE_DOT>
+__global__ void __launch_bounds__(kSpmvRows)
+spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *__restrict__ indx,
+              const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
+              typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, int tma, double *partials,
+              unsigned *counter, double *dot_out, int *err, const int *skip) {
+    using X = typename Val<V>::X;
+    if (skip && *skip) return;   // converged solver iteration replayed from a graph
+    constexpr int CAP = spmv_cap<V>() + 16;
+    extern __shared__ __align__(128) unsigned char smem[];
+    V *const sv0 = (V *)smem;
+    int *const si0 = (int *)(smem + 2 * CAP * sizeof(V));
+    __shared__ __align__(8) uint64_t bars[2];
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool use_tma = tma != 0;
+    int tile = blockIdx.x;
+    if (tid == 0) {
+        if (tile < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, tile, use_tma), vals, indx, sv0, si0, &bars[0]);
+        int t1 = tile + gridDim.x;
+        if (t1 < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, t1, use_tma), vals, indx, sv0 + CAP, si0 + CAP, &bars[1]);
+    }
+    double dsum[1] = {0.0};
+    for (int k = 0; tile < ntiles; tile += gridDim.x, k++) {
+        const int st = k & 1;
+        TileGeom<V> g = tile_geom<V>(pntr, n_rows, tile, use_tma);
+        const int r = tile * kSpmvRows + tid;
+        int ps = 0, pe = 0;
+        if (r < n_rows) {
+            ps = __ldg(pntr + r);
+            pe = __ldg(pntr + r + 1);
+        }
+        mbar_wait(&bars[st], (uint32_t)((k >> 1) & 1), err);
+        if (r < n_rows) {
+            const V *svs = sv0 + st * CAP;
+            const int *sis = si0 + st * CAP;
+            X acc = X(0);
+            for (int j = ps; j < pe; j++) {
+                V v = (j < g.ev) ? svs[j - g.sv] : __ldg(vals + j);
+                int c = (j < g.ei) ? sis[j - g.si] : __ldg(indx + j);
+                acc = add_rn(acc, mul_rn(Val<V>::get(v), __ldg(x + c)));
+            }
+            X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
+            y[r] = out;
+            if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
+        }
+        __syncthreads();   // every thread is done with stage st
+        if (tid == 0) {
+            int t2 = tile + 2 * gridDim.x;
+            if (t2 < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, t2, use_tma), vals, indx, sv0 + st * CAP, si0 + st * CAP, &bars[st]);
+        }
+    }
+    if (FUSE_DOT) {
+        grid_sum<1>(dsum, partials, counter, [&](double (&s)[1]) { *dot_out = s[0]; });
+    }
+}
+
+// transposed product by atomic scatter (stateless path): y[c] += (alpha * x[i]) * v_ic
+template <typename V>
+__global__ void spmv_t_atomic_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
+                                     const V *__restrict__ vals, typename Val<V>::X alpha,
+                                     const typename Val<V>::X *__restrict__ x, typename Val<V>::X *y) {
+    using X = typename Val<V>::X;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x) {
+        X ax = mul_rn(alpha, x[i]);
+        for (int p = __ldg(pntr + i); p < __ldg(pntr + i + 1); p++)
+            atomicAdd(y + __ldg(indx + p), mul_rn(ax, Val<V>::get(__ldg(vals + p))));
+    }
+}
+
+template <typename X>
+__global__ void scale_or_zero_kernel(long n, X beta, X *y) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        y[i] = (beta == X(0)) ? X(0) : mul_rn(beta, y[i]);
+}
+
+// transposed product through the cached transpose: one thread per column, entries in ascending
+// original row, which is the accumulation order of sparse_gemv_array<'T'> (utils:113-118).
+template <typename V>
+__global__ void spmv_t_cached_kernel(int n_cols, const int *__restrict__ pntrT, const int *__restrict__ rowT,
+                                     const int *__restrict__ mapT, const V *__restrict__ vals,
+                                     typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
+                                     typename Val<V>::X beta, typename Val<V>::X *__restrict__ y) {
+    using X = typename Val<V>::X;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += gridDim.x * blockDim.x) {
+        X acc = (beta == X(0)) ? X(0) : mul_rn(beta, y[c]);
+        for (int p = __ldg(pntrT + c); p < __ldg(pntrT + c + 1); p++) {
+            int i = __ldg(rowT + p);
+            acc = add_rn(acc, mul_rn(mul_rn(alpha, __ldg(x + i)), Val<V>::get(__ldg(vals + __ldg(mapT + p)))));
+        }
+        y[c] = acc;
+    }
+}
+
+// ------------------------------------------------------------- CSR validation ----------
+__global__ void csr_check_kernel(int n_rows, int n_cols, int nnz, const int *__restrict__ pntr,
+                                 const int *__restrict__ indx, int *err) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x) {
+        int a = pntr[i], b = pntr[i + 1];
+        if (a < 0 || b < a || b > nnz) { atomicOr(err, DEV_ERR_CSR); continue; }
+        int prev = -1;
+        for (int p = a; p < b; p++) {
+            int c = indx[p];
+            if (c <= prev || c >= n_cols) { atomicOr(err, DEV_ERR_CSR); break; }
+            prev = c;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (pntr[0] != 0 || pntr[n_rows] != nnz)) atomicOr(err, DEV_ERR_CSR);
+}
+
+// ------------------------------------------------------------- scan / transpose -------
+__global__ void scan_blocks_kernel(const int *__restrict__ in, int *__restrict__ out, int n, int *block_tot) {
+    // exclusive scan of 1024-element chunks (one per CTA of 1024 threads)
+    __shared__ int sh[1024];
+    int i = blockIdx.x * 1024 + threadIdx.x;
+    int v = (i < n) ? in[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = sh[threadIdx.x] - v;
+    if (threadIdx.x == 1023) block_tot[blockIdx.x] = sh[1023];
+}
+
+__global__ void scan_tot_kernel(int *tot, int nb, int *grand) {
+    // sequential exclusive scan of the block totals by one thread (nb is small)
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b < nb; b++) {
+            int t = tot[b];
+            tot[b] = run;
+            run += t;
+        }
+        *grand = run;
+    }
+}
+
+__global__ void scan_add_kernel(int *out, int n, const int *tot) {
+    int i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) out[i] += tot[blockIdx.x];
+}
+
+__global__ void count_cols_kernel(int nnz, const int *__restrict__ indx, int *cnt) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += gridDim.x * blockDim.x)
+        atomicAdd(cnt + indx[p], 1);
+}
+
+__global__ void fill_transpose_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
+                                      const int *__restrict__ pntrT, int *cursor, int *rowT, int *mapT) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x)
+        for (int p = pntr[i]; p < pntr[i + 1]; p++) {
+            int c = indx[p];
+            int slot = pntrT[c] + atomicAdd(cursor + c, 1);
+            rowT[slot] = i;
+            mapT[slot] = p;
+        }
+}
+
+__global__ void sort_segments_kernel(int n, const int *__restrict__ ptr, int *key, int *val) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        int a = ptr[r], b = ptr[r + 1];
+        for (int i = a + 1; i < b; i++) {   // insertion sort: segments are short
+            int k = key[i], v = val[i], j = i - 1;
+            while (j >= a && key[j] > k) {
+                key[j + 1] = key[j];
+                val[j + 1] = val[j];
+                j--;
+            }
+            key[j + 1] = k;
+            val[j + 1] = v;
+        }
+    }
+}
+
+int exclusive_scan(hgb_ctx *c, const int *in, int *out, int n, int *total_dev, int *scratch) {
+    // scratch: at least ceil(n/1024) ints
+    int nb = (n + 1023) / 1024;
+    if (nb == 0) return HGB_OK;
+    scan_blocks_kernel<<<nb, 1024, 0, c->stream>>>(in, out, n, scratch);
+    scan_tot_kernel<<<1, 32, 0, c->stream>>>(scratch, nb, total_dev);
+    scan_add_kernel<<<nb, 1024, 0, c->stream>>>(out, n, scratch);
+    return launch_check("exclusive_scan");
+}
+
+int csr_check(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx) {
+    if (n_rows <= 0) return HGB_OK;
+    csr_check_kernel<<<std::min((n_rows + 255) / 256, c->num_sms * 8), 256, 0, c->stream>>>(n_rows, n_cols, nnz,
+                                                                                           pntr, indx, c->err);
+    HGB_TRY(launch_check("csr_check_kernel"));
+    return collect_dev_error(c);
+}
+
+int build_transpose(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                    Transpose &T) {
+    T.n = n_cols;
+    size_t nb = (size_t)(n_cols + 1 + 1023) / 1024 + 1;
+    HGB_CUDA(cudaMalloc(&T.pntr, sizeof(int) * (size_t)(n_cols + 1)));
+    HGB_CUDA(cudaMalloc(&T.row, sizeof(int) * (size_t)std::max(nnz, 1)));
+    HGB_CUDA(cudaMalloc(&T.map, sizeof(int) * (size_t)std::max(nnz, 1)));
+    int *cnt = nullptr, *scratch = nullptr;
+    HGB_CUDA(cudaMalloc(&cnt, sizeof(int) * (size_t)(n_cols + 1)));
+    HGB_CUDA(cudaMalloc(&scratch, sizeof(int) * (nb + 1)));
+    int st = HGB_OK;
+    do {
+        if (cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)(n_cols + 1), c->stream) != cudaSuccess) { st = HGB_ERR_CUDA; break; }
+        int g = std::max(1, std::min((nnz + 255) / 256, c->num_sms * 8));
+        count_cols_kernel<<<g, 256, 0, c->stream>>>(nnz, indx, cnt);
+        st = exclusive_scan(c, cnt, T.pntr, n_cols + 1, scratch + nb, scratch);
+        if (st) break;
+        if (cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)(n_cols + 1), c->stream) != cudaSuccess) { st = HGB_ERR_CUDA; break; }
+        int gr = std::max(1, std::min((n_rows + 255) / 256, c->num_sms * 8));
+        fill_transpose_kernel<<<gr, 256, 0, c->stream>>>(n_rows, pntr, indx, T.pntr, cnt, T.row, T.map);
+        int gc = std::max(1, std::min((n_cols + 255) / 256, c->num_sms * 8));
+        sort_segments_kernel<<<gc, 256, 0, c->stream>>>(n_cols, T.pntr, T.row, T.map);
+        st = launch_check("build_transpose");
+        if (!st && cudaStreamSynchronize(c->stream) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "build_transpose");
+    } while (0);
+    cudaFree(cnt);
+    cudaFree(scratch);
+    return st;
+}
+
+void Transpose::release() {
+    cudaFree(pntr);
+    cudaFree(row);
+    cudaFree(map);
+    pntr = row = map = nullptr;
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename V>
+int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                  typename Val<V>::X *y, double *dot_out, const int *skip) {
+    if (n_rows <= 0) return HGB_OK;
+    int ntiles = (n_rows + kSpmvRows - 1) / kSpmvRows;
+    int grid = std::min(ntiles, c->num_sms * 3);
+    int tma = (aligned16(vals) && aligned16(indx)) ? 1 : 0;
+    if (dot_out) {
+        grid = std::min(grid, kMaxReduceBlocks);
+        spmv_n_kernel<V, true><<<grid, kSpmvRows, kSpmvSmem, c->stream>>>(
+            n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, c->partials, c->counter, dot_out, c->err, skip);
+    } else {
+        spmv_n_kernel<V, false><<<grid, kSpmvRows, kSpmvSmem, c->stream>>>(
+            n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, nullptr, nullptr, nullptr, c->err, skip);
+    }
+    return launch_check("spmv_n_kernel");
+}
+
+int spmv_init_attributes() {
+    // cudaFuncSetAttribute is per device; the context creation calls this on its device
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<uint16_t, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
+    return HGB_OK;
+}
+
+template int spmv_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, double,
+                                   const double *, double, double *, double *, const int *);
+template int spmv_n_launch<float>(hgb_ctx *, int, const int *, const int *, const float *, float,
+                                  const float *, float, float *, double *, const int *);
+template int spmv_n_launch<uint16_t>(hgb_ctx *, int, const int *, const int *, const uint16_t *, float,
+                                     const float *, float, float *, double *, const int *);
+
+template <typename V>
+int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                  typename Val<V>::X *y, const Transpose *T) {
+    using X = typename Val<V>::X;
+    if (n_cols <= 0) return HGB_OK;
+    int gc = std::max(1, std::min((n_cols + 255) / 256, c->num_sms * 8));
+    if (T) {
+        spmv_t_cached_kernel<V><<<gc, 256, 0, c->stream>>>(n_cols, T->pntr, T->row, T->map, vals, alpha, x, beta, y);
+        return launch_check("spmv_t_cached_kernel");
+    }
+    scale_or_zero_kernel<X><<<gc, 256, 0, c->stream>>>(n_cols, beta, y);
+    if (n_rows > 0) {
+        int gr = std::max(1, std::min((n_rows + 255) / 256, c->num_sms * 8));
+        spmv_t_atomic_kernel<V><<<gr, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, y);
+    }
+    return launch_check("spmv_t_atomic_kernel");
+}
+
+template int spmv_t_launch<double>(hgb_ctx *, int, int, const int *, const int *, const double *, double,
+                                   const double *, double, double *, const Transpose *);
+template int spmv_t_launch<float>(hgb_ctx *, int, int, const int *, const int *, const float *, float,
+                                  const float *, float, float *, const Transpose *);
+
+}  // namespace hgb
+
+using namespace hgb;
+
+struct hgb_csr {
+    hgb_ctx *ctx;
+    int n_rows, n_cols, nnz;
+    const int *pntr, *indx;
+    const void *vals;
+    hgb_dtype dtype;
+    Transpose T;
+    bool has_T = false;
+};
+
+namespace hgb {
+const int *csr_pntr(const hgb_csr *A) { return A->pntr; }
+const int *csr_indx(const hgb_csr *A) { return A->indx; }
+const void *csr_vals(const hgb_csr *A) { return A->vals; }
+int csr_rows(const hgb_csr *A) { return A->n_rows; }
+int csr_cols(const hgb_csr *A) { return A->n_cols; }
+int csr_nnz(const hgb_csr *A) { return A->nnz; }
+hgb_dtype csr_dtype(const hgb_csr *A) { return A->dtype; }
+hgb_ctx *csr_ctx(const hgb_csr *A) { return A->ctx; }
+}  // namespace hgb
+
+static int check_spmv_args(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                           const int *indx, const void *vals, const void *x, const void *y) {
+    if (!c) return fail(HGB_ERR_ARG, "spmv: null context");
+    if (n_rows < 0 || n_cols < 0 || nnz < 0) return fail(HGB_ERR_ARG, "spmv: negative size");
+    if (trans != 'N' && trans != 'n' && trans != 'T' && trans != 't' && trans != 'C' && trans != 'c')
+        return fail(HGB_ERR_ARG, "spmv: trans '%c'", trans);
+    if (n_rows > 0 && !pntr) return fail(HGB_ERR_ARG, "spmv: null pntr");
+    if (nnz > 0 && (!indx || !vals)) return fail(HGB_ERR_ARG, "spmv: null indx/vals");
+    bool nt = (trans == 'N' || trans == 'n');
+    if ((nt ? n_rows : n_cols) > 0 && !y) return fail(HGB_ERR_ARG, "spmv: null y");
+    if ((nt ? n_cols : n_rows) > 0 && !x && nnz > 0) return fail(HGB_ERR_ARG, "spmv: null x");
+    return HGB_OK;
+}
+
+extern "C" {
+
+int hgb_spmv_f64(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                 const double *vals, double alpha, const double *x, double beta, double *y) {
+    HGB_TRY(check_spmv_args(c, trans, n_rows, n_cols, nnz, pntr, indx, vals, x, y));
+    DeviceGuard g(c->device);
+    if (trans == 'N' || trans == 'n') return spmv_n_launch<double>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, nullptr);
+    return spmv_t_launch<double>(c, n_rows, n_cols, pntr, indx, vals, alpha, x, beta, y, nullptr);
+}
+
+int hgb_spmv_f32(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                 const float *vals, float alpha, const float *x, float beta, float *y) {
+    HGB_TRY(check_spmv_args(c, trans, n_rows, n_cols, nnz, pntr, indx, vals, x, y));
+    DeviceGuard g(c->device);
+    if (trans == 'N' || trans == 'n') return spmv_n_launch<float>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, nullptr);
+    return spmv_t_launch<float>(c, n_rows, n_cols, pntr, indx, vals, alpha, x, beta, y, nullptr);
+}
+
+int hgb_spmv_bf16f32(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                     const int *indx, const uint16_t *vals, float alpha, const float *x, float beta, float *y) {
+    HGB_TRY(check_spmv_args(c, trans, n_rows, n_cols, nnz, pntr, indx, vals, x, y));
+    if (trans != 'N' && trans != 'n') return fail(HGB_ERR_UNSUPPORTED, "spmv_bf16f32: only trans 'N'");
+    DeviceGuard g(c->device);
+    return spmv_n_launch<uint16_t>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, nullptr);
+}
+
+int hgb_csr_create(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                   const void *vals, hgb_dtype dtype, hgb_csr **out) {
+    if (!out) return fail(HGB_ERR_ARG, "csr_create: null output");
+    *out = nullptr;
+    HGB_TRY(check_spmv_args(c, 'N', n_rows, n_cols, nnz, pntr, indx, vals, pntr, pntr));
+    if (dtype != HGB_F64 && dtype != HGB_F32 && dtype != HGB_BF16) return fail(HGB_ERR_ARG, "csr_create: dtype");
+    DeviceGuard g(c->device);
+    HGB_TRY(csr_check(c, n_rows, n_cols, nnz, pntr, indx));
+    hgb_csr *A = new hgb_csr();
+    A->ctx = c;
+    A->n_rows = n_rows;
+    A->n_cols = n_cols;
+    A->nnz = nnz;
+    A->pntr = pntr;
+    A->indx = indx;
+    A->vals = vals;
+    A->dtype = dtype;
+    *out = A;
+    return HGB_OK;
+}
+
+int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double beta, void *y) {
+    if (!A) return fail(HGB_ERR_ARG, "csr_gemv: null matrix");
+    hgb_ctx *c = A->ctx;
+    HGB_TRY(check_spmv_args(c, trans, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->vals, x, y));
+    DeviceGuard g(c->device);
+    bool nt = (trans == 'N' || trans == 'n');
+    if (nt) {
+        switch (A->dtype) {
+            case HGB_F64: return spmv_n_launch<double>(c, A->n_rows, A->pntr, A->indx, (const double *)A->vals, alpha, (const double *)x, beta, (double *)y, nullptr, nullptr);
+            case HGB_F32: return spmv_n_launch<float>(c, A->n_rows, A->pntr, A->indx, (const float *)A->vals, (float)alpha, (const float *)x, (float)beta, (float *)y, nullptr, nullptr);
+            default: return spmv_n_launch<uint16_t>(c, A->n_rows, A->pntr, A->indx, (const uint16_t *)A->vals, (float)alpha, (const float *)x, (float)beta, (float *)y, nullptr, nullptr);
+        }
+    }
+    if (A->dtype == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "csr_gemv: transpose of a bf16 matrix");
+    if (!A->has_T) {
+        HGB_TRY(build_transpose(c, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->T));
+        A->has_T = true;
+    }
+    if (A->dtype == HGB_F64)
+        return spmv_t_launch<double>(c, A->n_rows, A->n_cols, A->pntr, A->indx, (const double *)A->vals, alpha, (const double *)x, beta, (double *)y, &A->T);
+    return spmv_t_launch<float>(c, A->n_rows, A->n_cols, A->pntr, A->indx, (const float *)A->vals, (float)alpha, (const float *)x, (float)beta, (float *)y, &A->T);
+}
+
+int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out) {
+    if (!A || !dot_out) return fail(HGB_ERR_ARG, "csr_gemv_dot: bad arguments");
+    if (A->n_rows != A->n_cols) return fail(HGB_ERR_ARG, "csr_gemv_dot: square matrix required");
+    hgb_ctx *c = A->ctx;
+    DeviceGuard g(c->device);
+    switch (A->dtype) {
+        case HGB_F64: return spmv_n_launch<double>(c, A->n_rows, A->pntr, A->indx, (const double *)A->vals, 1.0, (const double *)x, 0.0, (double *)y, dot_out, nullptr);
+        case HGB_F32: return spmv_n_launch<float>(c, A->n_rows, A->pntr, A->indx, (const float *)A->vals, 1.0f, (const float *)x, 0.0f, (float *)y, dot_out, nullptr);
+        default: return spmv_n_launch<uint16_t>(c, A->n_rows, A->pntr, A->indx, (const uint16_t *)A->vals, 1.0f, (const float *)x, 0.0f, (float *)y, dot_out, nullptr);
+    }
+}
+
+int hgb_csr_destroy(hgb_csr *A) {
+    if (!A) return HGB_OK;
+    DeviceGuard g(A->ctx->device);
+    if (A->has_T) A->T.release();
+    delete A;
+    return HGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+/*
+ * hgb.h — C ABI of the GB300-native sparse Krylov path (libhgb.so, sm_103a kernels).
+ *
+ * This is the boundary the reference's GPU backend crosses today through cuSPARSE / cuBLAS
+ * (gpu/hala_cuda_sparse_general.hpp, gpu/hala_cuda_sparse_triangular.hpp, gpu/hala_gpu_ilu.hpp,
+ * gpu/hala_gpu_blas1.hpp).  Every entry point below replaces one of those library calls or one
+ * of the reference objects built on them; the comment on each cites the reference interface.
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers on the context's device, unless a name says host.
+ *  - CSR matrices use int32 row pointers (pntr[n+1]) and int32 column indices (indx[nnz]) with
+ *    columns sorted ascending inside each row, zero-based (sparse/hala_sparse_utils.hpp:31-40).
+ *  - Work is ordered on the context's stream; calls that return a host scalar synchronise it.
+ *  - Return value: HGB_OK (0) or an hgb_status code; hgb_last_error() gives a message.  The C++
+ *    layer (include/hala_gb/) turns non-zero codes into std::runtime_error, as the reference's
+ *    check_cuda() does (gpu/hala_cuda_common.hpp:78-152).
+ *  - Handles (context, matrix, ILU, triangular) are not safe for concurrent use from several
+ *    host threads or streams; use one per stream.
+ */
+#ifndef HGB_H
+#define HGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hgb_status {
+    HGB_OK = 0,
+    HGB_ERR_ARG = 1,           /* invalid argument (size, pointer, trans/uplo/diag character)   */
+    HGB_ERR_CSR = 2,           /* malformed CSR: pntr not monotone, column out of range or
+                                  unsorted, or (ILU / triangular) a missing diagonal entry       */
+    HGB_ERR_ZERO_PIVOT = 3,    /* ILU(0) met an exactly zero pivot (factor still produced)      */
+    HGB_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up (result is not valid)      */
+    HGB_ERR_NOT_CONVERGED = 5, /* solver stopped at its iteration limit above the tolerance     */
+    HGB_ERR_CUDA = 6,          /* a CUDA runtime call failed                                    */
+    HGB_ERR_ALLOC = 7,         /* device or host allocation failed                              */
+    HGB_ERR_UNSUPPORTED = 8    /* combination not implemented (e.g. transpose on a bf16 matrix) */
+} hgb_status;
+
+typedef enum hgb_dtype { HGB_F64 = 0, HGB_F32 = 1, HGB_BF16 = 2 } hgb_dtype;
+
+typedef struct hgb_ctx hgb_ctx;
+typedef struct hgb_csr hgb_csr;
+typedef struct hgb_ilu hgb_ilu;
+typedef struct hgb_tri hgb_tri;
+
+/* Outcome of a solve (the reference returns only the iteration count). */
+typedef struct hgb_solve_info {
+    int iterations;      /* reference convention: CG counts 1 + loop SpMVs (cg.hpp:125,130);
+                            GMRES counts operator+preconditioner applications (gmres.hpp:176,189);
+                            iterative refinement counts inner iterations                        */
+    int outer;           /* refinement sweeps (IR) or restarts (GMRES); 0 for plain CG          */
+    double residual;     /* last residual norm the stopping test saw                            */
+    double true_residual;/* ||b - A x||_2 recomputed in FP64 at exit (IR only; else -1)         */
+    long long kernel_launches; /* kernels this solve executed (graph-replayed launches included) */
+} hgb_solve_info;
+
+/* ------------------------------------------------------------------ library / errors ---- */
+const char *hgb_status_string(int status);
+const char *hgb_last_error(void);    /* thread-local message of the last failing call */
+int hgb_version(void);               /* 10000*major + 100*minor + patch */
+
+/* -------------------------------------------------- engine (gpu_engine, engine.hpp:47) --- */
+/* gpu_engine(device) constructor, gpu/hala_gpu_engine.hpp:60 */
+int hgb_ctx_create(int device, hgb_ctx **ctx);
+int hgb_ctx_destroy(hgb_ctx *ctx);
+/* gpu_engine::set_stream, gpu/hala_gpu_engine.hpp:86-90 (stream is a cudaStream_t) */
+int hgb_ctx_set_stream(hgb_ctx *ctx, void *stream);
+int hgb_ctx_synchronize(hgb_ctx *ctx);
+
+/* ------------------------------------------------------- BLAS-1 (gpu/hala_gpu_blas1.hpp) --- */
+/* result: host pointer (synchronises) when result_on_device == 0, else device pointer.
+ * dot: :179-198 (cublasXdot); nrm2: :102-121 (cublasXnrm2); axpy: :205-222; scal: :229-245;
+ * copy (vcopy): :49-62.  alpha is a host scalar (the reference uses CUBLAS_POINTER_MODE_HOST). */
+int hgb_dot_f64(hgb_ctx *ctx, int n, const double *x, const double *y, double *result,
+                int result_on_device);
+int hgb_dot_f32(hgb_ctx *ctx, int n, const float *x, const float *y, float *result,
+                int result_on_device);
+int hgb_nrm2_f64(hgb_ctx *ctx, int n, const double *x, double *result, int result_on_device);
+int hgb_nrm2_f32(hgb_ctx *ctx, int n, const float *x, float *result, int result_on_device);
+int hgb_axpy_f64(hgb_ctx *ctx, int n, double alpha, const double *x, double *y);
+int hgb_axpy_f32(hgb_ctx *ctx, int n, float alpha, const float *x, float *y);
+int hgb_scal_f64(hgb_ctx *ctx, int n, double alpha, double *x);
+int hgb_scal_f32(hgb_ctx *ctx, int n, float alpha, float *x);
+int hgb_copy_f64(hgb_ctx *ctx, int n, const double *x, double *y);
+int hgb_copy_f32(hgb_ctx *ctx, int n, const float *x, float *y);
+/* set_zero(gpu_engine, ...), gpu/hala_gpu_engine.hpp:336-352 */
+int hgb_set_zero(hgb_ctx *ctx, size_t bytes, void *x);
+
+/* ------------------------------------------------ dense gemv (gpu/hala_gpu_blas2.hpp:40) --- */
+/* y = alpha * op(W) x + beta * y, W column-major m x k (ld = m): the GMRES Krylov project and
+ * combine, hex/solvers/hala_solvers_gmres.hpp:67-77 (tall-skinny, k <= 64). */
+int hgb_gemv_f64(hgb_ctx *ctx, char trans, int m, int k, double alpha, const double *W,
+                 const double *x, double beta, double *y);
+
+/* ------------------------------------------ SpMV (sparse_gemv(gpu_engine,...), :408-419) --- */
+/* y = alpha * op(A) x + beta * y; A is n_rows x n_cols CSR.  trans 'N', 'T' or 'C' (real: C==T).
+ * beta == 0 does not read y.  'N' rows are summed sequentially in column order without fused
+ * multiply-add, the arithmetic of sparse_gemv_array (sparse/hala_sparse_utils.hpp:104-112).
+ * 'T' without a matrix handle scatters with atomics (order not fixed). */
+int hgb_spmv_f64(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                 const int *indx, const double *vals, double alpha, const double *x, double beta,
+                 double *y);
+int hgb_spmv_f32(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                 const int *indx, const float *vals, float alpha, const float *x, float beta,
+                 float *y);
+/* bf16 values (uint16 bit patterns), fp32 vectors, fp32 accumulation ('N' only) */
+int hgb_spmv_bf16f32(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                     const int *indx, const uint16_t *vals, float alpha, const float *x,
+                     float beta, float *y);
+
+/* ---------------------- sparse matrix object (gpu_sparse_matrix, general.hpp:192-375) ------ */
+/* Non-owning view of pntr/indx/vals (general.hpp:202) plus cached analysis: the row tiling of
+ * the SpMV kernel and, on first transposed use, a transpose that makes op='T' deterministic and
+ * identical to sparse_gemv_array<'T'> (utils:113-118).  vals dtype: F64, F32 or BF16. */
+int hgb_csr_create(hgb_ctx *ctx, int n_rows, int n_cols, int nnz, const int *pntr,
+                   const int *indx, const void *vals, hgb_dtype dtype, hgb_csr **A);
+/* gpu_sparse_matrix::gemv, general.hpp:265-277.  x/y are double for F64, float otherwise. */
+int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double beta, void *y);
+/* y = A x and *dot_out (device) = <x, y> in one pass (the fused SpMV + BLAS-1 epilogue) */
+int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out_device);
+int hgb_csr_destroy(hgb_csr *A);
+
+/* ------------------------------------------------------------ pattern analysis --------- */
+/* get_diagonal_index, sparse/hala_sparse_core.hpp:45-60; HGB_ERR_CSR if a diagonal is missing */
+int hgb_diag_index(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx, int *diag);
+
+/* ------------------------------------------------ ILU(0) (gpu_ilu, gpu_ilu.hpp:45-185) ----- */
+/* make_ilu(gpu_engine, pntr, indx, vals, policy), gpu_ilu.hpp:54-109,192.
+ * Factorises a copy of vals (the pattern is aliased, as in the reference) with the row-wise IKJ
+ * order of factorize_ilu_array (sparse/hala_sparse_utils.hpp:229-255) and no fused multiply-add,
+ * so the F64 factor is bit-identical to the reference CPU factor.  vals_dtype F64 or F32 selects
+ * the factorisation precision; store selects the precision the triangular solves read:
+ * F64 (vectors double), F32 or BF16 (vectors float; pivots kept in FP64, the division by the
+ * pivot done in FP64).  policy 'L'/'N' is accepted for signature parity; level scheduling is
+ * always used.  Returns HGB_ERR_ZERO_PIVOT (with a valid handle) when a pivot is exactly 0. */
+int hgb_ilu0_create(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx,
+                    const void *vals, hgb_dtype vals_dtype, hgb_dtype store, char policy,
+                    hgb_ilu **ilu);
+/* gpu_ilu::apply(x, r), gpu_ilu.hpp:150-164: r = U^-1 L^-1 x (trans 'N'), the arithmetic of
+ * apply_ilu_array (utils:263-276); trans 'T': r = (LU)^-T x (adjoint).  x and r may alias. */
+int hgb_ilu0_apply(hgb_ilu *ilu, char trans, const void *x, void *r);
+/* device copies of the factor (values in the factorisation precision) and diagonal index */
+int hgb_ilu0_export(hgb_ilu *ilu, void *factor_vals, int *diag);
+/* level sets of the forward ('L') / backward ('U') solve: level[n] (device), *nlevels (host) */
+int hgb_ilu0_levels(hgb_ilu *ilu, char uplo, int *level, int *nlevels);
+int hgb_ilu0_destroy(hgb_ilu *ilu);
+
+/* ------------------------- triangular matrix (gpu_triangular_matrix, triangular.hpp:38) ---- */
+/* make_triangular_matrix(gpu_engine, uplo, diag, pntr, indx, vals): the triangle of a CSR
+ * matrix selected by uplo ('L'/'U'), unit or non-unit diagonal ('U'/'N').  The CSR may hold
+ * the other triangle too (ignored), as the reference's fill mode does (general.hpp:97-123). */
+int hgb_tri_create(hgb_ctx *ctx, char uplo, char diag, int n, int nnz, const int *pntr,
+                   const int *indx, const void *vals, hgb_dtype dtype, hgb_tri **tri);
+/* gpu_triangular_matrix::trsv, triangular.hpp:341-354: op(T) x = alpha b, with the arithmetic
+ * of sparse_trsv_array (sparse/hala_sparse_utils.hpp:284-336). */
+int hgb_tri_solve(hgb_tri *tri, char trans, double alpha, const void *b, void *x);
+int hgb_tri_destroy(hgb_tri *tri);
+
+/* ------------------------------------------------------------------- solvers ---------- */
+/* solve_cg / solve_cg_ilu over gpu_engine (hex/solvers/hala_solvers_cg.hpp:181-264,295-326),
+ * fused: device-resident scalars, the SpMV+dot and axpy+nrm2 fused, iterations replayed from a
+ * CUDA graph.  M may be NULL (identity preconditioner).  Stop: iterations == max_iter or
+ * ||r||_2 < tol (absolute, as the reference; pass tol*||b|| for a relative target).
+ * Precision follows A (F64: x,b double; F32/BF16: float). */
+int hgb_cg_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, const void *b, void *x, double tol,
+                 int max_iter, hgb_solve_info *info);
+/* Mixed precision iterative refinement: FP64 outer residual, update and stopping test on A64
+ * (F64); inner ILU(0)-PCG on A_inner (F32 or BF16 values, FP32 vectors and accumulation) with
+ * M_inner (store F32 or BF16, FP64 pivots), each inner solve to ||r|| < inner_rtol * ||r0||.
+ * Stops when ||b - A x||_2 < tol.  No reference counterpart. */
+int hgb_ir_pcg_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner,
+                     const double *b, double *x, double tol, double inner_rtol, int max_inner,
+                     int max_outer, hgb_solve_info *info);
+/* solve_gmres / solve_gmres_ilu over gpu_engine (hex/solvers/hala_solvers_gmres.hpp:127-267):
+ * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations on
+ * the host in the reference's order.  max_iter bounds the restarts, tol is absolute on the
+ * preconditioned residual estimate.  F64 or F32 (A's precision). */
+int hgb_gmres_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int restart, const void *b, void *x,
+                    double tol, int max_iter, hgb_solve_info *info);
+/* mixed_engine form (wax/hala_lib_extensions.hpp:68; solve_cg_ilu(mixed_engine,...),
+ * hala_solvers_cg.hpp:330-340): HOST pntr/indx/vals/b/x, loaded to the device per call, solved
+ * with the device factor M, x written back to the host.  FP64. */
+int hgb_mixed_cg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const int *indx_host,
+                       const double *vals_host, hgb_ilu *M, const double *b_host, double *x_host,
+                       double tol, int max_iter, hgb_solve_info *info);
+
+/* Host-buffer form of hgb_ir_pcg_solve: HOST pntr/indx/vals (FP64) and b/x are loaded per call,
+ * the inner matrix is converted on the device to M_inner's store precision (F32 or BF16), the
+ * refinement runs as hgb_ir_pcg_solve and x is written back to the host. */
+int hgb_mixed_ir_pcg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const int *indx_host,
+                           const double *vals_host, hgb_ilu *M_inner, const double *b_host,
+                           double *x_host, double tol, double inner_rtol, int max_inner,
+                           int max_outer, hgb_solve_info *info);
+
+/* ----------------------------------------------------------- fault-path self test ------ */
+/* Launches one bounded device wait on a value nothing ever publishes; returns HGB_ERR_TIMEOUT
+ * after spin_limit polls while leaving the context usable.  Test hook for the timeout path. */
+int hgb_selftest_wait_timeout(hgb_ctx *ctx, int spin_limit);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

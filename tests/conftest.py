@@ -1,0 +1,30 @@
+"""Shared fixtures.  GPU tests carry @pytest.mark.gpu and run only on a CUDA machine."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libhgb.so")
+
+
+@pytest.fixture(scope="session")
+def eng():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test collected without a CUDA device")
+    from hala_gb300 import build
+    build.build()
+    from hala_gb300 import engine as E
+    return E.gpu_engine(0)
+
+
+@pytest.fixture
+def rng():
+    return np.random.default_rng(1234)

@@ -1,0 +1,171 @@
+"""ILU(0) factorisation, level sets, ILU apply and triangular solves on the GPU vs the oracle.
+
+The FP64 factor, the level sets and the FP64 / FP32 applies are compared BIT-EXACTLY (same
+per-entry operation order, no fused multiply-add); stores with FP64 pivots within 1e-6."""
+import glob
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from hala_gb300 import engine as E
+from hala_gb300 import problems as P
+from hala_gb300.hgb import HgbError, HGB_ERR_TIMEOUT
+from hala_gb300 import hgb as H
+from oracle import oracle as O
+from tests import refcases as R
+
+pytestmark = pytest.mark.gpu
+dev = torch.device("cuda")
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def T(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+MATS = {
+    "aniso3d_20": lambda rng: P.aniso3d(20, 19, 18),
+    "poisson2d_70": lambda rng: P.poisson2d(70, 33),
+    "convdiff3d_14": lambda rng: P.convdiff3d(14),
+    "random_400": lambda rng: P.random_csr(400, 0.02, rng),
+    "ilu3": lambda rng: (R.ILU3["pntr"], R.ILU3["indx"], R.ILU3["vals"]),
+}
+
+
+@pytest.mark.parametrize("name", list(MATS))
+def test_factor_levels_apply_bit_exact(eng, rng, name):
+    p, i, v = MATS[name](rng)
+    n = len(p) - 1
+    fo, do, st = O.ilu_factor(p, i, v)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    f, d = ilu.factor()
+    assert np.array_equal(d.cpu().numpy(), do)
+    assert np.array_equal(f.cpu().numpy().view(np.uint64), fo.view(np.uint64))
+    for uplo in "LU":
+        lev, nl = ilu.levels(uplo)
+        lo, nlo = O.levels(p, i, do, uplo)
+        assert nl == nlo and np.array_equal(lev.cpu().numpy(), lo)
+    for _ in range(3):       # repeated applies reuse the pending-state buffers
+        x = rng.standard_normal(n)
+        r = ilu.apply(T(x))
+        assert np.array_equal(r.cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
+        rt = ilu.apply(T(x), trans="T")
+        assert np.array_equal(rt.cpu().numpy(), O.ilu_apply(p, i, do, fo, x, trans="T"))
+    # in place
+    gx = T(x)
+    ilu.apply(gx, gx)
+    assert np.array_equal(gx.cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
+
+
+def test_reference_ilu_golden(eng):
+    c = R.ILU3
+    ilu = E.make_ilu(eng, T(c["pntr"]), T(c["indx"]), T(c["vals"]))
+    f, d = ilu.factor()
+    assert np.array_equal(d.cpu().numpy(), c["diag"])
+    assert R.testvec(f.cpu().numpy(), c["ilu"])
+    assert R.testvec(ilu.apply(T(c["x"])).cpu().numpy(), c["apply"])
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))))
+def test_gpu_matches_reference_fixture(eng, path):
+    g = np.load(path)
+    p, i, v = g["pntr"], g["indx"], g["vals"]
+    n = len(p) - 1
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    f, d = ilu.factor()
+    assert np.array_equal(d.cpu().numpy(), g["diag"])
+    assert np.array_equal(f.cpu().numpy().view(np.uint64), g["ilu"].view(np.uint64))
+    assert np.array_equal(ilu.apply(T(g["x"])).cpu().numpy(), g["apply"])
+    y = torch.zeros(n, dtype=torch.float64, device=dev)
+    E.sparse_gemv(eng, "N", n, n, 1.0, T(p), T(i), T(v), T(g["x"]), 0.0, y)
+    assert np.array_equal(y.cpu().numpy(), g["spmv_n"])
+    A = E.make_sparse_matrix(eng, n, T(p), T(i), T(v))
+    y.zero_()
+    A.gemv("T", 1.0, T(g["x"]), 0.0, y)
+    assert np.array_equal(y.cpu().numpy(), g["spmv_t"])
+
+
+def test_f32_factor_and_apply_bit_exact(eng, rng):
+    p, i, v = P.aniso3d(16)
+    n = len(p) - 1
+    v32 = v.astype(np.float32)
+    fo, do, _ = O.ilu_factor(p, i, v32)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v32))
+    f, _ = ilu.factor()
+    assert np.array_equal(f.cpu().numpy().view(np.uint32), fo.view(np.uint32))
+    x = rng.standard_normal(n).astype(np.float32)
+    assert np.array_equal(ilu.apply(T(x)).cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
+
+
+@pytest.mark.parametrize("store", [torch.float32, torch.bfloat16])
+def test_mixed_store_apply(eng, rng, store):
+    p, i, v = P.aniso3d(18)
+    n = len(p) - 1
+    fo, do, _ = O.ilu_factor(p, i, v)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v), store=store)
+    x = rng.standard_normal(n).astype(np.float32)
+    r = ilu.apply(T(x)).cpu().numpy().astype(np.float64)
+    ref = O.ilu_apply(p, i, do, fo, x.astype(np.float64))
+    tol = 1e-5 if store == torch.float32 else 2e-2
+    assert np.linalg.norm(r - ref) <= tol * np.linalg.norm(ref)
+
+
+def test_triangular_goldens(eng):
+    X = R.TRSV_X
+    L, U = R.TRSV_L, R.TRSV_U
+    cases = [(L, L["vals"], "L", "N", "N", R.TRSV_A), (L, L["vals"], "L", "N", "T", R.TRSV_A.T),
+             (L, R.TRSV_LU_VALS, "L", "U", "N", R.TRSV_AU), (U, U["vals"], "U", "N", "N", R.TRSV_A.T),
+             (U, U["vals"], "U", "N", "T", R.TRSV_A)]
+    for c, vals, uplo, diagc, trans, M in cases:
+        tri = E.make_triangular_matrix(eng, uplo, diagc, T(c["pntr"]), T(c["indx"]), T(vals))
+        x = torch.zeros(3, dtype=torch.float64, device=dev)
+        E.sparse_trsv(trans, tri, 0.5, T(2.0 * M @ X), x)
+        assert R.testvec(x.cpu().numpy(), X), (uplo, diagc, trans)
+
+
+def test_triangular_bit_exact(eng, rng):
+    p, i, v = P.random_csr(300, 0.03, rng)
+    d = O.diag_index(p, i)
+    up, ui, lp, li = O.split_pattern(p, i, d)
+    uv, lv = O.split_values("U", "N", p, v, up, lp)
+    lv = lv.copy()
+    lv[lp[1:] - 1] = 1.0 + np.abs(rng.standard_normal(len(p) - 1))
+    n = len(p) - 1
+    b = rng.standard_normal(n)
+    for tp, ti, tv, uplo in ((lp, li, lv, "L"), (up, ui, uv, "U")):
+        for diagc in "NU":
+            tri = E.make_triangular_matrix(eng, uplo, diagc, T(tp), T(ti), T(tv))
+            for trans in "NT":
+                x = torch.zeros(n, dtype=torch.float64, device=dev)
+                E.sparse_trsv(trans, tri, 0.5, T(b), x)
+                ref = O.trsv(uplo, diagc, trans, 0.5, tp, ti, tv, b)
+                assert np.array_equal(x.cpu().numpy(), ref), (uplo, diagc, trans)
+    # b and x the same buffer
+    tri = E.make_triangular_matrix(eng, "L", "N", T(lp), T(li), T(lv))
+    gb = T(b)
+    E.sparse_trsv("N", tri, 1.0, gb, gb)
+    assert np.array_equal(gb.cpu().numpy(), O.trsv("L", "N", "N", 1.0, lp, li, lv, b))
+
+
+def test_zero_pivot_is_reported(eng):
+    # a_11 - l*a_01 = 0 exactly: [[1,1],[1,1]] has a zero second pivot
+    p, i, v = R.I(0, 2, 4), R.I(0, 1, 0, 1), R.D(1, 1, 1, 1)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    assert ilu.zero_pivot
+    f, _ = ilu.factor()
+    fo, _, st = O.ilu_factor(p, i, v)
+    assert st != 0 and np.array_equal(f.cpu().numpy(), fo)
+
+
+def test_bounded_wait_times_out_and_context_survives(eng, rng):
+    st = H.lib().hgb_selftest_wait_timeout(eng.h, 1000)
+    assert st == HGB_ERR_TIMEOUT
+    with pytest.raises(HgbError):
+        H.check(st)
+    p, i, v = P.aniso3d(10)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    fo, do, _ = O.ilu_factor(p, i, v)
+    x = rng.standard_normal(len(p) - 1)
+    assert np.array_equal(ilu.apply(T(x)).cpu().numpy(), O.ilu_apply(p, i, do, fo, x))

@@ -1,0 +1,157 @@
+"""CG / PCG / GMRES / iterative refinement on the GPU vs the oracle (the reference's algorithms).
+
+Solves must reach the same residual target with iteration counts within 5% of the oracle's
+(reductions are parallel, so the Krylov recurrences are not bit-identical); the reference's
+own solver tests are replayed with its tolerances (sum|x - xref| / correction < 1e-14)."""
+import numpy as np
+import pytest
+import torch
+
+from hala_gb300 import engine as E
+from hala_gb300 import problems as P
+from oracle import oracle as O
+from tests import refcases as R
+
+pytestmark = pytest.mark.gpu
+dev = torch.device("cuda")
+
+
+def T(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def within5(a, b):
+    return abs(a - b) <= max(1, int(round(0.05 * b)))
+
+
+def test_reference_cg_goldens(eng):
+    c = R.TRIDIAG5
+    b = R.dense(c) @ R.XREF5
+    gp, gi, gv = T(c["pntr"]), T(c["indx"]), T(c["vals"])
+    ilu = E.make_ilu(eng, gp, gi, gv)
+    x = torch.zeros(5, dtype=torch.float64, device=dev)
+    it = E.solve_cg(eng, E.stop_criteria(2), gp, gi, gv, T(b), x, ilu=ilu)
+    assert it == 2 and R.testvec(x.cpu().numpy(), R.XREF5)
+    c = R.CYCLIC5
+    b = R.dense(c) @ R.XREF5
+    gp, gi, gv = T(c["pntr"]), T(c["indx"]), T(c["vals"])
+    x = T(R.CG_X0)
+    E.solve_cg_ilu(eng, 1e-9, gp, gi, gv, T(b), x)
+    assert R.testvec(x.cpu().numpy(), R.XREF5, np.linalg.norm(R.XREF5))
+
+
+def test_reference_gmres_goldens(eng):
+    c = R.TRIDIAG5
+    b = R.dense(c) @ R.XREF5
+    gp, gi, gv = T(c["pntr"]), T(c["indx"]), T(c["vals"])
+    x = torch.zeros(5, dtype=torch.float64, device=dev)
+    E.solve_gmres_ilu(eng, E.stop_criteria(2), 2, gp, gi, gv, T(b), x)
+    assert R.testvec(x.cpu().numpy(), R.XREF5)
+    c = R.NONSYM5
+    b = R.dense(c) @ R.XREF5
+    gp, gi, gv = T(c["pntr"]), T(c["indx"]), T(c["vals"])
+    x = torch.zeros(5, dtype=torch.float64, device=dev)
+    E.solve_gmres_ilu(eng, 1e-9, 6, gp, gi, gv, T(b), x)
+    assert R.testvec(x.cpu().numpy(), R.XREF5)
+
+
+@pytest.mark.parametrize("precond", [False, True])
+@pytest.mark.parametrize("mat", ["poisson2d", "aniso3d"])
+def test_cg_matches_oracle(eng, rng, precond, mat):
+    p, i, v = P.poisson2d(64) if mat == "poisson2d" else P.aniso3d(24)
+    n = len(p) - 1
+    xt = rng.uniform(-1, 1, n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    xo, ito, _ = O.cg(p, i, v, b, tol=tol, diag=do if precond else None, ilu=fo if precond else None)
+    gp, gi, gv = T(p), T(i), T(v)
+    ilu = E.make_ilu(eng, gp, gi, gv) if precond else None
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    it = E.solve_cg(eng, E.stop_criteria(tol), gp, gi, gv, T(b), x, ilu=ilu)
+    assert within5(it, ito), (it, ito)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < 2 * tol
+    assert np.linalg.norm(xs - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
+def test_cg_iteration_limit(eng, rng):
+    p, i, v = P.poisson2d(40)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    gp, gi, gv = T(p), T(i), T(v)
+    it = E.solve_cg(eng, E.stop_criteria(17), gp, gi, gv, T(b), x)
+    xo, ito, _ = O.cg(p, i, v, b, max_iter=17)
+    assert it == ito == 17
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-10 * np.linalg.norm(xo)
+
+
+def test_gmres_matches_oracle(eng, rng):
+    p, i, v = P.convdiff3d(16)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    pb = O.ilu_apply(p, i, do, fo, b)
+    tol = 1e-9 * np.linalg.norm(pb)
+    xo, ito = O.gmres(p, i, v, b, 30, tol=tol, diag=do, ilu=fo)
+    gp, gi, gv = T(p), T(i), T(v)
+    ilu = E.make_ilu(eng, gp, gi, gv)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    it = E.solve_gmres(eng, E.stop_criteria(tol), 30, gp, gi, gv, T(b), x, ilu=ilu)
+    assert within5(it, ito), (it, ito)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("inner", [torch.float32, torch.bfloat16])
+def test_ir_pcg_reaches_fp64_accuracy(eng, rng, inner):
+    p, i, v = P.aniso3d(32)
+    n = len(p) - 1
+    xt = rng.standard_normal(n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    xo, _, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    gvi = gv.to(torch.float32 if inner == torch.float32 else torch.bfloat16)
+    Ai = E.make_sparse_matrix(eng, n, gp, gi, gvi)
+    Mi = E.make_ilu(eng, gp, gi, gv, store=inner)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    info = E.solve_ir_pcg(eng, A64, Ai, Mi, T(b), x, tol, inner_rtol=1e-4 if inner == torch.float32 else 1e-2)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
+    assert info.outer >= 2
+    # error against the FP64 oracle solution
+    assert np.linalg.norm(xs - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
+def test_fp32_cg(eng, rng):
+    p, i, v = P.aniso3d(20)
+    n = len(p) - 1
+    v32 = v.astype(np.float32)
+    b = rng.uniform(-1, 1, n).astype(np.float32)
+    gp, gi, gv = T(p), T(i), T(v32)
+    ilu = E.make_ilu(eng, gp, gi, gv)
+    x = torch.zeros(n, dtype=torch.float32, device=dev)
+    tol = 1e-5 * float(np.linalg.norm(b))
+    it = E.solve_cg(eng, E.stop_criteria(tol), gp, gi, gv, T(b), x, ilu=ilu)
+    fo, do, _ = O.ilu_factor(p, i, v32)
+    _, ito, _ = O.cg(p, i, v32, b, tol=np.float32(tol), diag=do, ilu=fo)
+    assert within5(it, ito), (it, ito)
+
+
+def test_mixed_engine_host_buffers(eng, rng):
+    p, i, v = P.aniso3d(16)
+    n = len(p) - 1
+    xt = rng.standard_normal(n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    x = np.zeros(n)
+    info = E.solve_cg_mixed(eng, E.stop_criteria(tol), p, i, v, ilu, b, x)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    _, ito, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
+    assert within5(info.iterations, ito)
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, x)) < 2 * tol
