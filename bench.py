@@ -24,7 +24,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "PCG solves/s (128³ Poisson, 1e-10 rel res) mixed vs FP64; SpMV GB/s vs HBM peak"
-GRID = 128
+GRID = int(os.environ.get("HGB_BENCH_GRID", "128"))
 COEF = (1.0, 1.0, 0.01)
 RTOL = 1e-10
 SEED = 2
@@ -179,7 +179,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=None, help="grid edge (default 128: the headline workload)")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="only the SpMV and ILU-apply launches (for profiling captures)")
     args = ap.parse_args()
+    if args.grid:
+        global GRID
+        GRID = args.grid
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -219,6 +225,25 @@ def main():
     setup32 = time.perf_counter() - t0
     flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
+    if args.kernels_only:
+        y64 = torch.empty(n, dtype=torch.float64, device=dev)
+        y32 = torch.empty(n, dtype=torch.float32, device=dev)
+        xs32 = gb.float()
+        Ab = E.make_sparse_matrix(eng, n, gp, gi, gv.to(torch.bfloat16))
+        for _ in range(3):
+            flush_l2(flush)
+            A64.gemv("N", 1.0, gb, 0.0, y64)
+            flush_l2(flush)
+            A32.gemv("N", 1.0, xs32, 0.0, y32)
+            flush_l2(flush)
+            Ab.gemv("N", 1.0, xs32, 0.0, y32)
+            flush_l2(flush)
+            M64.apply(gb, y64)
+            flush_l2(flush)
+            M32.apply(xs32, y32)
+        torch.cuda.synchronize()
+        print(json.dumps({"kernels_only": True, "n": n, "nnz": nnz}))
+        return
 
     def timed(fn, steps, warm):
         for _ in range(warm):

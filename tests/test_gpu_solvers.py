@@ -123,8 +123,11 @@ def test_ir_pcg_reaches_fp64_accuracy(eng, rng, inner):
     xs = x.cpu().numpy()
     assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
     assert info.outer >= 2
-    # error against the FP64 oracle solution
-    assert np.linalg.norm(xs - xo) <= 1e-8 * np.linalg.norm(xo)
+    # error against the exact solution, no worse than the FP64 oracle's own (same residual target;
+    # both errors are conditioning x 1e-10, so they are compared rather than the two iterates)
+    err, err_o = np.linalg.norm(xs - xt), np.linalg.norm(xo - xt)
+    assert err <= 5 * err_o + 1e-12 * np.linalg.norm(xt), (err, err_o)
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
 
 
 def test_fp32_cg(eng, rng):
