@@ -17,6 +17,7 @@
 #include "hgb_kernels.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 namespace hgb {
@@ -57,7 +58,6 @@ __device__ __forceinline__ int wait_level(const int *lev, int j, int *err) {
             atomicOr(err, DEV_ERR_TIMEOUT);
             return 0;
         }
-        if (spins > 256) __nanosleep(64);
         v = ld_acquire(lev + j);
     }
     return v;
@@ -312,6 +312,34 @@ struct SolveArgs {
     const int *skip;                 // optional device flag: the launch is a no-op when set
 };
 
+// Polls up to 8 pending solution entries together (one L2 round trip when they are ready).
+template <typename X>
+__device__ __forceinline__ void wait_values(const X *out, const int (&jj)[8], X (&xv)[8], int cnt, int *err) {
+    unsigned pending = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        if (k < cnt) {
+            xv[k] = ld_relaxed(out + jj[k]);
+            if (Pending<X>::is(xv[k])) pending |= 1u << k;
+        }
+    int spins = 0;
+    while (pending) {
+        if (++spins > kSpinLimit) {
+            atomicOr(err, DEV_ERR_TIMEOUT);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (pending & (1u << k)) xv[k] = Pending<X>::canon(Pending<X>::value());
+            return;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (pending & (1u << k)) {
+                xv[k] = ld_relaxed(out + jj[k]);
+                if (!Pending<X>::is(xv[k])) pending &= ~(1u << k);
+            }
+    }
+}
+
 template <typename V, typename X>
 __global__ void __launch_bounds__(256) trsv_kernel(SolveArgs A, const V *__restrict__ vals, X alpha,
                                                    const X *in, X *out, X *pend_a, X *pend_b) {
@@ -330,19 +358,32 @@ __global__ void __launch_bounds__(256) trsv_kernel(SolveArgs A, const V *__restr
             if (A.lower) { a = __ldg(A.pntr + row); b = d; }
             else { a = d + 1; b = __ldg(A.pntr + row + 1); }
             const X xin = in[row];
+            const X dval = A.unit ? X(1) : Val<V>::get(__ldg(vals + (A.map ? __ldg(A.map + d) : d)));
             X acc = (A.mode == MODE_ILU) ? xin : X(0);
-            for (int k = 0; k < b - a; k++) {
-                const int p = A.rev ? b - 1 - k : a + k;
-                const int j = __ldg(A.indx + p);
-                const X v = Val<V>::get(__ldg(vals + (A.map ? __ldg(A.map + p) : p)));
-                const X xj = wait_value<X>(out + j, A.err);
-                if (A.mode == MODE_ILU) acc = sub_rn(acc, mul_rn(v, xj));
-                else acc = add_rn(acc, mul_rn(v, xj));
+            const int len = b - a;
+            for (int k0 = 0; k0 < len; k0 += 8) {
+                const int cnt = min(8, len - k0);
+                int jj[8];
+                X vv[8], xv[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    if (k < cnt) {
+                        const int p = A.rev ? b - 1 - (k0 + k) : a + k0 + k;
+                        jj[k] = __ldg(A.indx + p);
+                        vv[k] = Val<V>::get(__ldg(vals + (A.map ? __ldg(A.map + p) : p)));
+                    }
+                wait_values<X>(out, jj, xv, cnt, A.err);
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    if (k < cnt) {
+                        if (A.mode == MODE_ILU) acc = sub_rn(acc, mul_rn(vv[k], xv[k]));
+                        else acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+                    }
             }
             if (A.mode == MODE_TRSV) acc = sub_rn(mul_rn(alpha, xin), acc);
             if (!A.unit) {
                 if (A.piv) acc = (X)__ddiv_rn((double)acc, __ldg(A.piv + row));
-                else acc = div_rn(acc, Val<V>::get(__ldg(vals + (A.map ? __ldg(A.map + d) : d))));
+                else acc = div_rn(acc, dval);
             }
             st_relaxed(out + row, Pending<X>::canon(acc));
             if (pend_a) pend_a[row] = Pending<X>::value();
@@ -372,6 +413,17 @@ static int fill_pending(hgb_ctx *c, long n, X *p) {
     return launch_check("fill_pending_kernel");
 }
 
+// CTAs (of 8 warps) per SM for the sync-free solves.  More warps hold tasks further ahead of
+// the wavefront, all of them polling L2; HGB_TRSV_BLOCKS_PER_SM overrides the default.
+static int trsv_blocks_per_sm() {
+    static int v = [] {
+        const char *e = getenv("HGB_TRSV_BLOCKS_PER_SM");
+        int k = e ? atoi(e) : 4;
+        return (k >= 1 && k <= 8) ? k : 4;
+    }();
+    return v;
+}
+
 template <typename V, typename X>
 static int launch_solve(hgb_ctx *c, const Schedule &S, SolveArgs A, const V *vals, X alpha, const X *in, X *out,
                         X *pend_a, X *pend_b) {
@@ -381,7 +433,7 @@ static int launch_solve(hgb_ctx *c, const Schedule &S, SolveArgs A, const V *val
     A.perm = S.perm;
     A.ticket = S.ticket;
     A.err = c->err;
-    int blocks = std::max(1, std::min((S.ntasks + 7) / 8, c->num_sms * 8));
+    int blocks = std::max(1, std::min((S.ntasks + 7) / 8, c->num_sms * trsv_blocks_per_sm()));
     trsv_kernel<V, X><<<blocks, 256, 0, c->stream>>>(A, vals, alpha, in, out, pend_a, pend_b);
     return launch_check("trsv_kernel");
 }

@@ -183,7 +183,6 @@ __device__ __forceinline__ T wait_value(const T *p, int *err, int limit = kSpinL
             atomicOr(err, DEV_ERR_TIMEOUT);
             return Pending<T>::canon(Pending<T>::value());
         }
-        if (spins > 256) __nanosleep(64);   // back off only once the value is clearly late
         v = ld_relaxed(p);
     }
     return v;

@@ -101,10 +101,23 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
             const V *svs = sv0 + st * CAP;
             const int *sis = si0 + st * CAP;
             X acc = X(0);
-            for (int j = ps; j < pe; j++) {
-                V v = (j < g.ev) ? svs[j - g.sv] : __ldg(vals + j);
-                int c = (j < g.ei) ? sis[j - g.si] : __ldg(indx + j);
-                acc = add_rn(acc, mul_rn(Val<V>::get(v), __ldg(x + c)));
+            // up to 8 entries at a time: all x gathers in flight together, then the sum in
+            // column order (the reference's sequential order, so the result keeps its bits)
+            for (int j0 = ps; j0 < pe; j0 += 8) {
+                X xv[8], vv[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int j = j0 + k;
+                    if (j < pe) {
+                        V v = (j < g.ev) ? svs[j - g.sv] : __ldg(vals + j);
+                        int c = (j < g.ei) ? sis[j - g.si] : __ldg(indx + j);
+                        vv[k] = Val<V>::get(v);
+                        xv[k] = __ldg(x + c);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
             }
             X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
             y[r] = out;

@@ -367,3 +367,50 @@ def solve_ir_pcg_mixed(engine, tol, pntr_h, indx_h, vals_h, ilu_inner, b_h, x_h,
                                           x_h.ctypes.data_as(C.c_void_p), float(tol), float(inner_rtol),
                                           int(max_inner), int(max_outer), C.byref(info)), "solve_ir_pcg (mixed)")
     return info
+
+
+class gpu_batch:
+    """Many independent SPD systems (block-diagonal CSR, FP32 values) solved in one persistent
+    launch with FP64 refinement (hgb_batch_*; no reference counterpart)."""
+
+    def __init__(self, engine, sys_ptr, pntr, indx, vals):
+        _need(sys_ptr, torch.int32, "sys_ptr"); _need(pntr, torch.int32, "pntr"); _need(indx, torch.int32, "indx")
+        _need(vals, torch.float32, "vals")
+        self.engine = engine
+        self.S = sys_ptr.numel() - 1
+        self.n = pntr.numel() - 1
+        self._keep = (sys_ptr, pntr, indx, vals)
+        h = C.c_void_p()
+        check(_h.lib().hgb_batch_create(engine.h, self.S, _p(sys_ptr), self.n, indx.numel(), _p(pntr), _p(indx),
+                                        _p(vals), C.byref(h)), "batch_create")
+        self.h = h
+
+    @property
+    def config(self):
+        c = _h.BatchConfig()
+        check(_h.lib().hgb_batch_get_config(self.h, C.byref(c)), "batch config")
+        return (c.block_threads, c.warp_max_n)
+
+    def set_config(self, block_threads, warp_max_n):
+        c = _h.BatchConfig(block_threads, warp_max_n)
+        check(_h.lib().hgb_batch_set_config(self.h, C.byref(c)), "batch config")
+
+    def autotune(self, b, x, rtol, cache_path=None):
+        c = _h.BatchConfig()
+        check(_h.lib().hgb_batch_autotune(self.h, _p(b), _p(x), float(rtol),
+                                          cache_path.encode() if cache_path else None, C.byref(c)), "batch autotune")
+        return (c.block_threads, c.warp_max_n)
+
+    def solve(self, b, x, rtol=1e-8, inner_rtol=1e-4, max_inner=1000, max_outer=20, iters=None, relres=None):
+        _need(b, torch.float64, "b"); _need(x, torch.float64, "x")
+        check(_h.lib().hgb_batch_cg_solve(self.h, _p(b), _p(x), float(rtol), float(inner_rtol), int(max_inner),
+                                          int(max_outer), _p(iters), _p(relres)), "batch_cg_solve")
+        return x
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                _h.lib().hgb_batch_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

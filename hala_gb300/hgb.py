@@ -28,6 +28,10 @@ class SolveInfo(C.Structure):
                 ("true_residual", C.c_double), ("kernel_launches", C.c_longlong)]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("block_threads", C.c_int), ("warp_max_n", C.c_int)]
+
+
 _lib = None
 vp, i32, f64, f32, ch = C.c_void_p, C.c_int, C.c_double, C.c_float, C.c_char
 
@@ -72,6 +76,12 @@ _SIGS = {
     "hgb_gmres_solve": ([vp, vp, vp, i32, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_mixed_cg_solve": ([vp, i32, i32, vp, vp, vp, vp, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_mixed_ir_pcg_solve": ([vp, i32, i32, vp, vp, vp, vp, vp, vp, f64, f64, i32, i32, C.POINTER(SolveInfo)], i32),
+    "hgb_batch_create": ([vp, i32, vp, i32, i32, vp, vp, vp, C.POINTER(vp)], i32),
+    "hgb_batch_set_config": ([vp, vp], i32),
+    "hgb_batch_get_config": ([vp, vp], i32),
+    "hgb_batch_cg_solve": ([vp, vp, vp, f64, f64, i32, i32, vp, vp], i32),
+    "hgb_batch_autotune": ([vp, vp, vp, f64, C.c_char_p, vp], i32),
+    "hgb_batch_destroy": ([vp], i32),
     "hgb_selftest_wait_timeout": ([vp, i32], i32),
 }
 

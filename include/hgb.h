@@ -46,6 +46,7 @@ typedef struct hgb_ctx hgb_ctx;
 typedef struct hgb_csr hgb_csr;
 typedef struct hgb_ilu hgb_ilu;
 typedef struct hgb_tri hgb_tri;
+typedef struct hgb_batch hgb_batch;
 
 /* Outcome of a solve (the reference returns only the iteration count). */
 typedef struct hgb_solve_info {
@@ -195,6 +196,30 @@ int hgb_mixed_ir_pcg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, c
                            const double *vals_host, hgb_ilu *M_inner, const double *b_host,
                            double *x_host, double tol, double inner_rtol, int max_inner,
                            int max_outer, hgb_solve_info *info);
+
+/* ------------------------------------------ batched independent systems (no reference
+ * counterpart: the reference's batch is one matrix with many right-hand sides) -------------- */
+/* Launch shape of the batched solver: threads per CTA (128, 256 or 512) and the largest system
+ * solved by a single warp (larger systems get a whole CTA). */
+typedef struct hgb_batch_config { int block_threads; int warp_max_n; } hgb_batch_config;
+/* A batch of S independent systems stored as one block-diagonal CSR with FP32 values and global
+ * column indices; sys_ptr[S+1] (device) holds the first row of each system.  Every column of a
+ * system's rows must lie inside that system (checked, HGB_ERR_CSR).  Systems up to 4096 rows. */
+int hgb_batch_create(hgb_ctx *ctx, int num_systems, const int *sys_ptr, int n_total, int nnz,
+                     const int *pntr, const int *indx, const float *vals, hgb_batch **batch);
+int hgb_batch_set_config(hgb_batch *batch, const hgb_batch_config *cfg);
+int hgb_batch_get_config(hgb_batch *batch, hgb_batch_config *cfg);
+/* Solves every system in ONE persistent kernel launch, replayed from a CUDA graph: FP32 CG
+ * (inner relative tolerance inner_rtol, at most max_inner iterations) inside FP64 refinement
+ * until ||b_s - A_s x_s|| <= rtol ||b_s|| for each system s (at most max_outer sweeps).  x holds
+ * the initial guesses.  iters[S] / relres[S] (device, optional) receive per-system totals. */
+int hgb_batch_cg_solve(hgb_batch *batch, const double *b, double *x, double rtol, double inner_rtol,
+                       int max_inner, int max_outer, int *iters, double *relres);
+/* Times the launch shapes on this batch (x is overwritten) and keeps the fastest; the choice
+ * is cached under a size-histogram key in cache_path (text, may be NULL). */
+int hgb_batch_autotune(hgb_batch *batch, const double *b, double *x, double rtol,
+                       const char *cache_path, hgb_batch_config *best);
+int hgb_batch_destroy(hgb_batch *batch);
 
 /* ----------------------------------------------------------- fault-path self test ------ */
 /* Launches one bounded device wait on a value nothing ever publishes; returns HGB_ERR_TIMEOUT
