@@ -15,9 +15,11 @@
 //    value is its own ready flag (one L2 round trip per dependency).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
+#include "hgb_bsolve.cuh"
 
 #include <algorithm>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 namespace hgb {
@@ -112,9 +114,6 @@ __global__ void __launch_bounds__(256) levels_kernel(int n, const int *__restric
     }
 }
 
-template <typename T> __device__ __forceinline__ T div_rn(T a, T b);
-template <> __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
-template <> __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 
 template <typename T> __device__ __forceinline__ T ld_val(const T *p) { return ld_relaxed(p); }
 
@@ -413,6 +412,15 @@ static int fill_pending(hgb_ctx *c, long n, X *p) {
     return launch_check("fill_pending_kernel");
 }
 
+// 0: block-local level schedule (default); 1: global level tasks (HGB_ILU_SOLVER=levels)
+static int ilu_solver_kind() {
+    static int v = [] {
+        const char *e = getenv("HGB_ILU_SOLVER");
+        return (e && std::string(e) == "levels") ? 1 : 0;
+    }();
+    return v;
+}
+
 // CTAs (of 8 warps) per SM for the sync-free solves.  More warps hold tasks further ahead of
 // the wavefront, all of them polling L2; HGB_TRSV_BLOCKS_PER_SM overrides the default.
 static int trsv_blocks_per_sm() {
@@ -488,6 +496,9 @@ struct hgb_ilu {
     void *svalsT = nullptr;
     double *pivT = nullptr;     // same pivots as piv (diagonal entries are their own transpose)
     Schedule LT, UT;
+    // block-local level schedules (hgb_bsolve.cu); the global-level kernel is the fallback
+    bool use_bs = false, use_bsT = false;
+    BlockSolve BL, BU, BLT, BUT;
 };
 
 namespace hgb {
@@ -511,6 +522,10 @@ static void ilu_free(hgb_ilu *M) {
         M->LT.release();
         M->UT.release();
     }
+    M->BL.release();
+    M->BU.release();
+    M->BLT.release();
+    M->BUT.release();
     delete M;
 }
 
@@ -522,6 +537,12 @@ static int ilu_apply_n(hgb_ilu *M, const void *x, void *r, const int *skip) {
         HGB_TRY(fill_pending<X>(c, M->n, tmp));
         M->tmp_ready = true;
         M->tmp_epoch = c->error_epoch;
+    }
+    if (M->use_bs) {
+        // forward: unit lower, tmp <- L^-1 x (r reset to pending); backward: r <- U^-1 tmp
+        HGB_TRY(bsolve_launch<V, X>(c, M->BL, MODE_ILU, 1, X(1), (const X *)x, tmp, (X *)r, nullptr, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BU, MODE_ILU, 0, X(1), tmp, (X *)r, tmp, nullptr, skip));
+        return HGB_OK;
     }
     SolveArgs A{};
     A.pntr = M->pntr;
@@ -559,6 +580,15 @@ static int ilu_build_T(hgb_ilu *M) {
     // U^T is the lower triangle of the transposed pattern, L^T its upper triangle
     HGB_TRY(analyse(c, M->n, M->T.pntr, M->T.row, M->diagT, 1, M->LT));
     HGB_TRY(analyse(c, M->n, M->T.pntr, M->T.row, M->diagT, 0, M->UT));
+    if (M->use_bs) {
+        const int R = bsolve_rows((int)xsize(M->store));
+        int st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 1, 0, R, M->BLT);
+        if (!st) st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 0, 1, R, M->BUT);
+        if (!st) st = bsolve_load_values(c, M->BLT, M->svalsT, (int)vsize(M->store), M->piv);
+        if (!st) st = bsolve_load_values(c, M->BUT, M->svalsT, (int)vsize(M->store), nullptr);
+        if (st == HGB_OK) M->use_bsT = true;
+        else if (st != HGB_ERR_UNSUPPORTED) return st;
+    }
     M->has_T = true;
     return HGB_OK;
 }
@@ -575,6 +605,11 @@ static int ilu_apply_t(hgb_ilu *M, const void *x, void *r, const int *skip) {
         HGB_TRY(fill_pending<X>(c, M->n, tmp));
         M->tmp_ready = true;
         M->tmp_epoch = c->error_epoch;
+    }
+    if (M->use_bsT) {
+        HGB_TRY(bsolve_launch<V, X>(c, M->BLT, MODE_TRSV, 0, X(1), (const X *)x, tmp, (X *)r, nullptr, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BUT, MODE_TRSV, 1, X(1), tmp, (X *)r, tmp, nullptr, skip));
+        return HGB_OK;
     }
     SolveArgs A{};
     A.pntr = M->T.pntr;
@@ -669,6 +704,15 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
             if ((st = launch_check("ilu store conversion"))) break;
         }
         if (cudaMalloc(&M->tmp, xsize(store) * n) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
+        if (ilu_solver_kind() == 0) {
+            const int R = bsolve_rows((int)xsize(store));
+            int bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 1, 0, R, M->BL);
+            if (!bs) bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 0, 0, R, M->BU);
+            if (!bs) bs = bsolve_load_values(c, M->BL, M->svals, (int)vsize(store), nullptr);
+            if (!bs) bs = bsolve_load_values(c, M->BU, M->svals, (int)vsize(store), M->piv);
+            if (bs == HGB_OK) M->use_bs = true;
+            else if (bs != HGB_ERR_UNSUPPORTED) { st = bs; break; }
+        }
         if (cudaStreamSynchronize(c->stream) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
     } while (0);
     if (st) {

@@ -73,6 +73,8 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
@@ -106,6 +108,13 @@ int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int
 int ilu_apply_internal(hgb_ilu *M, char trans, const void *x, void *r, const int *skip = nullptr);
 hgb_dtype ilu_store(const hgb_ilu *M);
 int ilu_n(const hgb_ilu *M);
+
+// transposed operator for the adjoint solves: build (once) the cached transpose, then
+// y = alpha A^T x + beta y with an optional fused <dot_x, y>
+int csr_ensure_transpose(hgb_csr *A);
+template <typename V>
+int spmv_t_fused_launch(hgb_csr *A, typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                        typename Val<V>::X *y, const typename Val<V>::X *dot_x, double *dot_out, const int *skip);
 
 // accessors of the opaque matrix handle
 const int *csr_pntr(const hgb_csr *A);

@@ -133,20 +133,29 @@ struct CgWork {
 };
 
 template <typename V, typename X>
-static int spmv_A(hgb_ctx *c, hgb_csr *A, X alpha, const X *x, X beta, X *y, double *dot, const int *skip) {
+static int spmv_A(hgb_ctx *c, hgb_csr *A, X alpha, const X *x, X beta, X *y, double *dot, const int *skip,
+                  bool trans = false) {
+    if (trans) return spmv_t_fused_launch<V>(A, alpha, x, beta, y, x, dot, skip);
     return spmv_n_launch<V>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const V *)csr_vals(A), alpha, x, beta, y, dot,
                             skip);
+}
+template <>
+int spmv_A<uint16_t, float>(hgb_ctx *c, hgb_csr *A, float alpha, const float *x, float beta, float *y, double *dot,
+                           const int *skip, bool trans) {
+    if (trans) return fail(HGB_ERR_UNSUPPORTED, "transposed product of a bf16 matrix");
+    return spmv_n_launch<uint16_t>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const uint16_t *)csr_vals(A), alpha, x,
+                                   beta, y, dot, skip);
 }
 
 // One CG iteration: the launches captured into the graph.
 template <typename V, typename X>
-static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, long n) {
+static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, long n, bool trans) {
     SolverScalars *s = c->scal;
     const int *done = &s->done;
-    HGB_TRY(spmv_A<V, X>(c, A, X(1), w.p, X(0), w.Ap, &s->pap, done));
+    HGB_TRY(spmv_A<V, X>(c, A, X(1), w.p, X(0), w.Ap, &s->pap, done, trans));
     cg_update_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, s, w.p, w.Ap, x, w.r, c->partials, c->counter);
     X *z = M ? w.z : w.r;
-    if (M) HGB_TRY(ilu_apply_internal(M, 'N', w.r, w.z, done));
+    if (M) HGB_TRY(ilu_apply_internal(M, trans ? 'T' : 'N', w.r, w.z, done));
     cg_rz_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
     cg_p_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, w.p, z);
     return launch_check("cg iteration");
@@ -158,7 +167,7 @@ static int cg_launches_per_iter(bool precond) { return precond ? 6 : 4; }
 
 template <typename V, typename X>
 static int cg_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const X *b, X *x, double tol2, double rel, int max_iter,
-                  bool zero_x0, int *iters, double *rr_out, long long *launches) {
+                  bool zero_x0, int *iters, double *rr_out, long long *launches, bool trans = false) {
     const long n = csr_rows(A);
     CaptureStream cs(c);
     CgWork<X> w;
@@ -173,16 +182,17 @@ static int cg_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const X *b, X *x, double t
         *launches += 1 + (zero_x0 ? 0 : 1) + (M ? 2 : 0) + 2;   // init, SpMV, L/U solves, copy, <r,z>
         // r = b - A x  (r = b; r += -1 * A x)
         if (cudaMemcpyAsync(w.r, b, sizeof(X) * n, cudaMemcpyDeviceToDevice, c->stream)) { st = cuda_fail(cudaGetLastError(), "cg"); break; }
-        if (!zero_x0 && (st = spmv_A<V, X>(c, A, X(-1), x, X(1), w.r, nullptr, nullptr))) break;
+        if (trans && (st = csr_ensure_transpose(A))) break;
+        if (!zero_x0 && (st = spmv_A<V, X>(c, A, X(-1), x, X(1), w.r, nullptr, nullptr, trans))) break;
         X *z = M ? w.z : w.r;
-        if (M && (st = ilu_apply_internal(M, 'N', w.r, w.z, nullptr))) break;
+        if (M && (st = ilu_apply_internal(M, trans ? 'T' : 'N', w.r, w.z, nullptr))) break;
         copy_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, z, w.p);
         cg_rz_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 1);
         if ((st = launch_check("cg init"))) break;
         // capture ITERS_PER_GRAPH iterations
         cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
         if (cudaStreamBeginCapture(c->stream, mode)) { st = cuda_fail(cudaGetLastError(), "begin capture"); break; }
-        for (int k = 0; k < kItersPerGraph && !st; k++) st = cg_iteration<V, X>(c, A, M, w, x, n);
+        for (int k = 0; k < kItersPerGraph && !st; k++) st = cg_iteration<V, X>(c, A, M, w, x, n, trans);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
         if (st) break;
         if (ce != cudaSuccess) { st = cuda_fail(ce, "end capture"); break; }
@@ -207,11 +217,12 @@ static int cg_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const X *b, X *x, double t
 }
 
 static int true_residual(hgb_ctx *c, hgb_csr *A64, const double *b, const double *x, double *r, double *res,
-                         long long *launches) {
+                         long long *launches, bool trans = false) {
     *launches += 2;
     const long n = csr_rows(A64);
     HGB_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
-    HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r, nullptr, nullptr));
+    if (trans) HGB_TRY(csr_ensure_transpose(A64));
+    HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r, nullptr, nullptr, trans));
     residual_norm_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, r, c->partials, c->counter, c->result);
     HGB_TRY(launch_check("residual_norm_kernel"));
     HGB_CUDA(cudaMemcpyAsync(c->host_result, c->result, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -228,7 +239,14 @@ extern "C" {
 
 int hgb_cg_solve(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const void *b, void *x, double tol, int max_iter,
                  hgb_solve_info *info) {
+    return hgb_cg_solve_op(c, A, M, 'N', b, x, tol, max_iter, info);
+}
+
+int hgb_cg_solve_op(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, char trans, const void *b, void *x, double tol, int max_iter,
+                    hgb_solve_info *info) {
     if (!c || !A || !b || !x) return fail(HGB_ERR_ARG, "cg_solve: bad arguments");
+    const bool tr = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
+    if (!tr && trans != 'N' && trans != 'n') return fail(HGB_ERR_ARG, "cg_solve: trans '%c'", trans);
     if (csr_rows(A) != csr_cols(A)) return fail(HGB_ERR_ARG, "cg_solve: square matrix required");
     if (max_iter < 1) return fail(HGB_ERR_ARG, "cg_solve: max_iter < 1");
     DeviceGuard g(c->device);
@@ -243,9 +261,9 @@ int hgb_cg_solve(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const void *b, void *x, dou
     double tol2 = tol * tol;
     long long launches = 0;
     int st;
-    if (dt == HGB_F64) st = cg_run<double, double>(c, A, M, (const double *)b, (double *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches);
-    else if (dt == HGB_F32) st = cg_run<float, float>(c, A, M, (const float *)b, (float *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches);
-    else st = cg_run<uint16_t, float>(c, A, M, (const float *)b, (float *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches);
+    if (dt == HGB_F64) st = cg_run<double, double>(c, A, M, (const double *)b, (double *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches, tr);
+    else if (dt == HGB_F32) st = cg_run<float, float>(c, A, M, (const float *)b, (float *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches, tr);
+    else st = cg_run<uint16_t, float>(c, A, M, (const float *)b, (float *)x, tol2, 0.0, max_iter, false, &it, &rr, &launches, tr);
     if (st) return st;
     if (info) {
         info->iterations = it;
@@ -259,7 +277,15 @@ int hgb_cg_solve(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const void *b, void *x, dou
 
 int hgb_ir_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, const double *b, double *x, double tol,
                      double inner_rtol, int max_inner, int max_outer, hgb_solve_info *info) {
+    return hgb_ir_pcg_solve_op(c, A64, Ai, Mi, 'N', b, x, tol, inner_rtol, max_inner, max_outer, info);
+}
+
+int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char trans, const double *b, double *x,
+                        double tol, double inner_rtol, int max_inner, int max_outer, hgb_solve_info *info) {
     if (!c || !A64 || !Ai || !b || !x) return fail(HGB_ERR_ARG, "ir_pcg: bad arguments");
+    const bool tr = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
+    if (!tr && trans != 'N' && trans != 'n') return fail(HGB_ERR_ARG, "ir_pcg: trans '%c'", trans);
+    if (tr && csr_dtype(Ai) == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "ir_pcg: transposed solve with a bf16 matrix");
     if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the outer matrix must be F64");
     if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the inner matrix must be F32 or BF16");
     if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the inner preconditioner must store F32 or BF16");
@@ -279,7 +305,7 @@ int hgb_ir_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, const d
             break;
         }
         for (;;) {
-            if ((st = true_residual(c, A64, b, x, r64, &res, &launches))) break;
+            if ((st = true_residual(c, A64, b, x, r64, &res, &launches, tr))) break;
             if (res < tol || outer >= max_outer || !(res == res)) break;
             f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, r32);
             zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d32);
@@ -287,7 +313,7 @@ int hgb_ir_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, const d
             double rr = 0.0;
             launches += 3;   // residual cast, zero, update
             if (csr_dtype(Ai) == HGB_F32)
-                st = cg_run<float, float>(c, Ai, Mi, r32, d32, 0.0, inner_rtol, max_inner, true, &it, &rr, &launches);
+                st = cg_run<float, float>(c, Ai, Mi, r32, d32, 0.0, inner_rtol, max_inner, true, &it, &rr, &launches, tr);
             else
                 st = cg_run<uint16_t, float>(c, Ai, Mi, r32, d32, 0.0, inner_rtol, max_inner, true, &it, &rr, &launches);
             if (st) break;

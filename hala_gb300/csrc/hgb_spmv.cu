@@ -155,12 +155,18 @@ __global__ void scale_or_zero_kernel(long n, X beta, X *y) {
 
 // transposed product through the cached transpose: one thread per column, entries in ascending
 // original row, which is the accumulation order of sparse_gemv_array<'T'> (utils:113-118).
-template <typename V>
+// FUSE_DOT additionally reduces <x', y> with x' = the vector y is paired with (dot_x, indexed by
+// column), for the CG on the transposed operator.
+template <typename V, bool FUSE_DOT>
 __global__ void spmv_t_cached_kernel(int n_cols, const int *__restrict__ pntrT, const int *__restrict__ rowT,
                                      const int *__restrict__ mapT, const V *__restrict__ vals,
                                      typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
-                                     typename Val<V>::X beta, typename Val<V>::X *__restrict__ y) {
+                                     typename Val<V>::X beta, typename Val<V>::X *__restrict__ y,
+                                     const typename Val<V>::X *__restrict__ dot_x, double *partials,
+                                     unsigned *counter, double *dot_out, const int *skip) {
     using X = typename Val<V>::X;
+    if (skip && *skip) return;
+    double dsum[1] = {0.0};
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += gridDim.x * blockDim.x) {
         X acc = (beta == X(0)) ? X(0) : mul_rn(beta, y[c]);
         for (int p = __ldg(pntrT + c); p < __ldg(pntrT + c + 1); p++) {
@@ -168,7 +174,9 @@ __global__ void spmv_t_cached_kernel(int n_cols, const int *__restrict__ pntrT, 
             acc = add_rn(acc, mul_rn(mul_rn(alpha, __ldg(x + i)), Val<V>::get(__ldg(vals + __ldg(mapT + p)))));
         }
         y[c] = acc;
+        if (FUSE_DOT) dsum[0] += (double)dot_x[c] * (double)acc;
     }
+    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
 }
 
 // ------------------------------------------------------------- CSR validation ----------
@@ -357,7 +365,8 @@ int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int
     if (n_cols <= 0) return HGB_OK;
     int gc = std::max(1, std::min((n_cols + 255) / 256, c->num_sms * 8));
     if (T) {
-        spmv_t_cached_kernel<V><<<gc, 256, 0, c->stream>>>(n_cols, T->pntr, T->row, T->map, vals, alpha, x, beta, y);
+        spmv_t_cached_kernel<V, false><<<gc, 256, 0, c->stream>>>(n_cols, T->pntr, T->row, T->map, vals, alpha, x,
+                                                                 beta, y, nullptr, nullptr, nullptr, nullptr, nullptr);
         return launch_check("spmv_t_cached_kernel");
     }
     scale_or_zero_kernel<X><<<gc, 256, 0, c->stream>>>(n_cols, beta, y);
@@ -388,6 +397,42 @@ struct hgb_csr {
 };
 
 namespace hgb {
+template <typename T>
+__global__ void pattern_grad_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, T alpha,
+                                    const T *__restrict__ lam, const T *__restrict__ u, T *__restrict__ grad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_rows; i += gridDim.x * blockDim.x) {
+        const T li = alpha * lam[i];
+        for (int p = pntr[i]; p < pntr[i + 1]; p++) grad[p] = li * u[indx[p]];
+    }
+}
+
+int csr_ensure_transpose(hgb_csr *A) {
+    if (A->has_T) return HGB_OK;
+    DeviceGuard g(A->ctx->device);
+    HGB_TRY(build_transpose(A->ctx, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->T));
+    A->has_T = true;
+    return HGB_OK;
+}
+
+template <typename V>
+int spmv_t_fused_launch(hgb_csr *A, typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                        typename Val<V>::X *y, const typename Val<V>::X *dot_x, double *dot_out, const int *skip) {
+    hgb_ctx *c = A->ctx;
+    if (!A->has_T) return fail(HGB_ERR_ARG, "transposed product before the transpose was built");
+    const int n = A->n_cols;
+    if (n <= 0) return HGB_OK;
+    int gc = std::max(1, std::min((n + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks)));
+    if (dot_out)
+        spmv_t_cached_kernel<V, true><<<gc, 256, 0, c->stream>>>(n, A->T.pntr, A->T.row, A->T.map, (const V *)A->vals,
+                                                                alpha, x, beta, y, dot_x, c->partials, c->counter, dot_out, skip);
+    else
+        spmv_t_cached_kernel<V, false><<<gc, 256, 0, c->stream>>>(n, A->T.pntr, A->T.row, A->T.map, (const V *)A->vals,
+                                                                 alpha, x, beta, y, nullptr, nullptr, nullptr, nullptr, skip);
+    return launch_check("spmv_t_cached_kernel");
+}
+template int spmv_t_fused_launch<double>(hgb_csr *, double, const double *, double, double *, const double *, double *, const int *);
+template int spmv_t_fused_launch<float>(hgb_csr *, float, const float *, float, float *, const float *, double *, const int *);
+
 const int *csr_pntr(const hgb_csr *A) { return A->pntr; }
 const int *csr_indx(const hgb_csr *A) { return A->indx; }
 const void *csr_vals(const hgb_csr *A) { return A->vals; }
@@ -492,6 +537,20 @@ int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out) {
         case HGB_F32: return spmv_n_launch<float>(c, A->n_rows, A->pntr, A->indx, (const float *)A->vals, 1.0f, (const float *)x, 0.0f, (float *)y, dot_out, nullptr);
         default: return spmv_n_launch<uint16_t>(c, A->n_rows, A->pntr, A->indx, (const uint16_t *)A->vals, 1.0f, (const float *)x, 0.0f, (float *)y, dot_out, nullptr);
     }
+}
+
+int hgb_csr_pattern_grad(hgb_csr *A, double alpha, const void *lam, const void *u, void *grad) {
+    if (!A || !lam || !u || !grad) return fail(HGB_ERR_ARG, "csr_pattern_grad: bad arguments");
+    if (A->dtype == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "csr_pattern_grad: F64 or F32 matrices");
+    hgb_ctx *c = A->ctx;
+    DeviceGuard g(c->device);
+    if (A->n_rows == 0) return HGB_OK;
+    int gr = std::max(1, std::min((A->n_rows + 255) / 256, c->num_sms * 8));
+    if (A->dtype == HGB_F64)
+        pattern_grad_kernel<double><<<gr, 256, 0, c->stream>>>(A->n_rows, A->pntr, A->indx, alpha, (const double *)lam, (const double *)u, (double *)grad);
+    else
+        pattern_grad_kernel<float><<<gr, 256, 0, c->stream>>>(A->n_rows, A->pntr, A->indx, (float)alpha, (const float *)lam, (const float *)u, (float *)grad);
+    return launch_check("pattern_grad_kernel");
 }
 
 int hgb_csr_destroy(hgb_csr *A) {

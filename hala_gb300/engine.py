@@ -313,6 +313,30 @@ def solve_cg_info(engine, A, ilu, b, x, tol, max_iter=INT_MAX):
     return info
 
 
+def solve_cg_op(engine, A, ilu, trans, b, x, tol, max_iter=INT_MAX):
+    """CG on op(A) = A or A^T with the matching preconditioner (LU)^-1 or (LU)^-T; the adjoint
+    solve of the differentiable path.  Returns SolveInfo."""
+    info = SolveInfo()
+    check(_h.lib().hgb_cg_solve_op(engine.h, A.h, ilu.h if ilu else None, ch_(trans), _p(b), _p(x), float(tol),
+                                   int(max_iter), C.byref(info)), "solve_cg_op")
+    return info
+
+
+def solve_ir_pcg_op(engine, A64, A_inner, ilu_inner, trans, b, x, tol, inner_rtol=1e-4, max_inner=100000,
+                    max_outer=50):
+    info = SolveInfo()
+    check(_h.lib().hgb_ir_pcg_solve_op(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, ch_(trans),
+                                       _p(b), _p(x), float(tol), float(inner_rtol), int(max_inner), int(max_outer),
+                                       C.byref(info)), "solve_ir_pcg_op")
+    return info
+
+
+def pattern_grad(A, alpha, lam, u, grad):
+    """grad[p] = alpha * lam[row(p)] * u[col(p)] over A's pattern (dL/dA with alpha = -1)."""
+    check(_h.lib().hgb_csr_pattern_grad(A.h, float(alpha), _p(lam), _p(u), _p(grad)), "pattern_grad")
+    return grad
+
+
 def solve_gmres(engine, stop, restart, pntr, indx, vals, b, x, ilu=None, matrix=None):
     """solve_gmres / solve_gmres_ilu(gpu_engine, ...), hex/solvers/hala_solvers_gmres.hpp:127-267."""
     s = _stop(stop)

@@ -123,6 +123,9 @@ int hgb_csr_create(hgb_ctx *ctx, int n_rows, int n_cols, int nnz, const int *pnt
 int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double beta, void *y);
 /* y = A x and *dot_out (device) = <x, y> in one pass (the fused SpMV + BLAS-1 epilogue) */
 int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out_device);
+/* grad[p] = alpha * lam[i] * u[indx[p]] for every stored entry p of row i: dL/dA restricted to
+ * A's pattern for L(u(A)) with adjoint lam (alpha = -1).  Vectors in A's precision (F64/F32). */
+int hgb_csr_pattern_grad(hgb_csr *A, double alpha, const void *lam, const void *u, void *grad);
 int hgb_csr_destroy(hgb_csr *A);
 
 /* ------------------------------------------------------------ pattern analysis --------- */
@@ -169,6 +172,10 @@ int hgb_tri_destroy(hgb_tri *tri);
  * Precision follows A (F64: x,b double; F32/BF16: float). */
 int hgb_cg_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, const void *b, void *x, double tol,
                  int max_iter, hgb_solve_info *info);
+/* Same on op(A) = A^T ('T') or A ('N'): the transposed product goes through the matrix's cached
+ * transpose and the preconditioner applies (LU)^-T.  The adjoint solve A^T lambda = g. */
+int hgb_cg_solve_op(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, char trans, const void *b, void *x,
+                    double tol, int max_iter, hgb_solve_info *info);
 /* Mixed precision iterative refinement: FP64 outer residual, update and stopping test on A64
  * (F64); inner ILU(0)-PCG on A_inner (F32 or BF16 values, FP32 vectors and accumulation) with
  * M_inner (store F32 or BF16, FP64 pivots), each inner solve to ||r|| < inner_rtol * ||r0||.
@@ -176,6 +183,11 @@ int hgb_cg_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, const void *b, void *x, d
 int hgb_ir_pcg_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner,
                      const double *b, double *x, double tol, double inner_rtol, int max_inner,
                      int max_outer, hgb_solve_info *info);
+/* hgb_ir_pcg_solve on op(A) (trans 'N' or 'T'; 'T' needs an F32 inner matrix): the adjoint of
+ * the mixed-precision forward solve. */
+int hgb_ir_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, char trans,
+                        const double *b, double *x, double tol, double inner_rtol, int max_inner,
+                        int max_outer, hgb_solve_info *info);
 /* solve_gmres / solve_gmres_ilu over gpu_engine (hex/solvers/hala_solvers_gmres.hpp:127-267):
  * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations on
  * the host in the reference's order.  max_iter bounds the restarts, tol is absolute on the

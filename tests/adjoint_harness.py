@@ -1,0 +1,100 @@
+"""Test harness for the differentiable solve (variable-coefficient 2D diffusion).
+
+-div(k grad u) = f on an n x n grid of unit cells (5-point finite volumes, face conductivity the
+harmonic mean of the two cells, Dirichlet faces 2 k_cell), k = exp(theta).  Loss
+L = ||u(theta) - u_target||^2.  The solve is a torch.autograd.Function: forward = mixed precision
+ILU(0)-PCG (FP32 inner, FP64 refinement) through the C ABI; backward = the hand-written adjoint:
+A^T lam = dL/du by the same solver on the transposed operator, dL/df = lam and
+dL/dA_ij = -lam_i u_j on A's pattern (hgb_csr_pattern_grad).  dL/dtheta follows by autograd
+through the assembly below.
+"""
+import numpy as np
+import torch
+
+from hala_gb300 import engine as E
+from hala_gb300 import problems as P
+
+
+class Stencil:
+    """Pattern of the 5-point operator and the mask that maps (row, offset) -> CSR position."""
+
+    def __init__(self, n, device):
+        self.n = n
+        k1 = np.ones(n * n)
+        p, i, _ = P.vardiff2d(n, k1)
+        self.pntr, self.indx = p, i
+        N = n * n
+        x = np.arange(N) % n
+        y = np.arange(N) // n
+        # offsets in column order: south, west, diagonal, east, north (problems._stencil_csr)
+        valid = np.stack([y > 0, x > 0, np.ones(N, bool), x < n - 1, y < n - 1], 1)
+        self.valid = torch.from_numpy(valid.reshape(-1)).to(device)
+        self.gp = torch.from_numpy(p).to(device)
+        self.gi = torch.from_numpy(i).to(device)
+
+
+def assemble(st, theta):
+    """CSR values of the operator for conductivity exp(theta) (differentiable in theta)."""
+    n = st.n
+    k = torch.exp(theta).reshape(n, n)                       # [y][x]
+    kx = torch.empty(n, n + 1, dtype=k.dtype, device=k.device)
+    kx[:, 1:-1] = 2 * k[:, :-1] * k[:, 1:] / (k[:, :-1] + k[:, 1:])
+    kx[:, 0] = 2 * k[:, 0]
+    kx[:, -1] = 2 * k[:, -1]
+    ky = torch.empty(n + 1, n, dtype=k.dtype, device=k.device)
+    ky[1:-1, :] = 2 * k[:-1, :] * k[1:, :] / (k[:-1, :] + k[1:, :])
+    ky[0, :] = 2 * k[0, :]
+    ky[-1, :] = 2 * k[-1, :]
+    west, east = kx[:, :-1].reshape(-1), kx[:, 1:].reshape(-1)
+    south, north = ky[:-1, :].reshape(-1), ky[1:, :].reshape(-1)
+    diag = west + east + south + north
+    full = torch.stack([-south, -west, diag, -east, -north], 1).reshape(-1)
+    return full[st.valid]
+
+
+class Solver:
+    def __init__(self, eng, st, tol=1e-12, inner_rtol=1e-5):
+        self.eng, self.st, self.tol, self.inner_rtol = eng, st, tol, inner_rtol
+        self.last = None
+
+    def _setup(self, vals):
+        st = self.st
+        n = st.n * st.n
+        v64 = vals.detach().contiguous()
+        v32 = v64.float()
+        A64 = E.make_sparse_matrix(self.eng, n, st.gp, st.gi, v64)
+        A32 = E.make_sparse_matrix(self.eng, n, st.gp, st.gi, v32)
+        M = E.make_ilu(self.eng, st.gp, st.gi, v64, store=torch.float32)
+        return (A64, A32, M, v64, v32)
+
+    def solve(self, vals, rhs, trans="N", ops=None):
+        ops = ops or self._setup(vals)
+        A64, A32, M = ops[:3]
+        x = torch.zeros_like(rhs)
+        tol = self.tol * float(torch.linalg.vector_norm(rhs))
+        E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, tol, inner_rtol=self.inner_rtol)
+        return x, ops
+
+
+class DiffSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, vals, f, solver):
+        u, ops = solver.solve(vals, f)
+        ctx.solver, ctx.ops = solver, ops
+        ctx.save_for_backward(u)
+        return u
+
+    @staticmethod
+    def backward(ctx, gu):
+        (u,) = ctx.saved_tensors
+        solver, ops = ctx.solver, ctx.ops
+        lam, _ = solver.solve(None, gu.contiguous(), trans="T", ops=ops)
+        gvals = torch.empty_like(ops[3])
+        E.pattern_grad(ops[0], -1.0, lam, u, gvals)
+        return gvals, lam, None
+
+
+def loss(solver, st, theta, f, u_target):
+    vals = assemble(st, theta)
+    u = DiffSolve.apply(vals, f, solver)
+    return torch.sum((u - u_target) ** 2)

@@ -1,0 +1,95 @@
+"""Differentiable solve on variable-coefficient 2D diffusion (512 x 512): the adjoint gradient
+dL/dtheta against central finite differences (h = 1e-6, 64 random directions) and against the
+gradient built from FP64 oracle solves; plus the transposed solvers against their 'N' forms."""
+import numpy as np
+import pytest
+import torch
+
+from hala_gb300 import engine as E
+from hala_gb300 import problems as P
+from oracle import oracle as O
+from tests import adjoint_harness as H
+
+pytestmark = pytest.mark.gpu
+dev = torch.device("cuda")
+N = 512
+
+
+@pytest.fixture(scope="module")
+def setup(eng):
+    st = H.Stencil(N, dev)
+    theta = torch.from_numpy(P.grf2d(N, length=16.0, sigma=1.0, seed=1)).to(dev)
+    theta2 = torch.from_numpy(P.grf2d(N, length=16.0, sigma=1.0, seed=2)).to(dev)
+    f = torch.ones(N * N, dtype=torch.float64, device=dev)
+    solver = H.Solver(eng, st, tol=1e-13)
+    with torch.no_grad():
+        u_target, _ = solver.solve(H.assemble(st, theta2), f)
+    return st, theta, f, u_target, solver
+
+
+def test_forward_solve_accuracy(setup):
+    st, theta, f, u_target, solver = setup
+    vals = H.assemble(st, theta).detach()
+    u, _ = solver.solve(vals, f)
+    p, i = st.pntr, st.indx
+    r = f.cpu().numpy() - P.csr_matvec(p, i, vals.cpu().numpy(), u.cpu().numpy())
+    assert np.linalg.norm(r) <= 1e-13 * np.linalg.norm(f.cpu().numpy()) * 1.5
+
+
+def test_gradient_vs_central_differences(setup):
+    st, theta, f, u_target, solver = setup
+    th = theta.clone().requires_grad_(True)
+    L = H.loss(solver, st, th, f, u_target)
+    (g,) = torch.autograd.grad(L, th)
+    rng = np.random.default_rng(11)
+    h = 1e-6
+    errs = []
+    with torch.no_grad():
+        for _ in range(64):
+            d = torch.from_numpy(rng.standard_normal(N * N)).to(dev)
+            d /= torch.linalg.vector_norm(d)
+            lp = H.loss(solver, st, theta + h * d, f, u_target)
+            lm = H.loss(solver, st, theta - h * d, f, u_target)
+            fd = float((lp - lm) / (2 * h))
+            ad = float(torch.dot(g, d))
+            errs.append(abs(fd - ad) / max(abs(ad), 1e-30 * float(L)))
+    assert np.median(errs) < 1e-3 and max(errs) < 5e-2, (np.median(errs), max(errs))
+
+
+def test_gradient_vs_fp64_oracle(setup):
+    st, theta, f, u_target, solver = setup
+    th = theta.clone().requires_grad_(True)
+    L = H.loss(solver, st, th, f, u_target)
+    (g,) = torch.autograd.grad(L, th)
+    # FP64 oracle: u = A^-1 f, lam = A^-T 2(u - u_t) (A symmetric), dL/dvals = -lam_i u_j
+    vals = H.assemble(st, theta).detach().cpu().numpy()
+    p, i = st.pntr, st.indx
+    fo, do, _ = O.ilu_factor(p, i, vals)
+    fn = f.cpu().numpy()
+    u, _, _ = O.cg(p, i, vals, fn, tol=1e-13 * np.linalg.norm(fn), diag=do, ilu=fo)
+    gu = 2 * (u - u_target.cpu().numpy())
+    lam, _, _ = O.cg(p, i, vals, gu, tol=1e-13 * np.linalg.norm(gu), diag=do, ilu=fo)
+    rows = np.repeat(np.arange(len(p) - 1), np.diff(p))
+    gvals = torch.from_numpy(-lam[rows] * u[i]).to(dev)
+    th2 = theta.clone().requires_grad_(True)
+    (g64,) = torch.autograd.grad(H.assemble(st, th2), th2, grad_outputs=gvals)
+    rel = float(torch.linalg.vector_norm(g - g64) / torch.linalg.vector_norm(g64))
+    assert rel < 1e-5, rel
+
+
+def test_transposed_cg_matches_forward(eng, rng):
+    p, i, v = P.aniso3d(20)
+    n = len(p) - 1
+    b = rng.standard_normal(n)
+    gp, gi, gv = (torch.from_numpy(a).to(dev) for a in (p, i, v))
+    A = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    M = E.make_ilu(eng, gp, gi, gv)
+    gb = torch.from_numpy(b).to(dev)
+    tol = 1e-11 * np.linalg.norm(b)
+    xn = torch.zeros(n, dtype=torch.float64, device=dev)
+    xt = torch.zeros(n, dtype=torch.float64, device=dev)
+    inf_n = E.solve_cg_op(eng, A, M, "N", gb, xn, tol)
+    inf_t = E.solve_cg_op(eng, A, M, "T", gb, xt, tol)
+    # A symmetric: A^T = A and (LU)^T = LU up to rounding, so both solves agree
+    assert abs(inf_n.iterations - inf_t.iterations) <= 2
+    assert float(torch.linalg.vector_norm(xn - xt) / torch.linalg.vector_norm(xn)) < 1e-9
