@@ -23,7 +23,7 @@
 
 namespace hgb {
 
-constexpr int kBsStages = 8;
+constexpr int kBsStages = 4;
 constexpr int kBsConsumers = 128;          // consumer threads (4 warps); + 1 producer warp
 constexpr int kBsCapRows = 128;            // rows per chunk (level piece)
 constexpr int kBsCapEnt = 1024;            // entries per chunk (padded to 8)
@@ -43,6 +43,7 @@ struct BsArgs {
     const void *dvals;       // V or double (pivots)
     int dv_double;           // dvals are FP64 pivots
     int R;                   // rows per block (smem slice)
+    int n, lower;            // block b holds rows [row_lo, row_lo + cnt) in both directions
     int mode, unit;
     int *ticket;
     int *err;
@@ -104,6 +105,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                 }
             }
         } else {
+            // the block's right-hand side into its shared solution slice (slot = row - row_lo);
+            // a row reads its own slot before overwriting it, dependencies read finished slots
+            const int cnt_rows = min(A.R, A.n - b * A.R);
+            const int row_lo = A.lower ? b * A.R : A.n - b * A.R - cnt_rows;
+#pragma unroll 4
+            for (int i = tid; i < cnt_rows; i += kBsConsumers) xs[i] = in[row_lo + i];
+            named_bar(1, kBsConsumers);
             for (int c = c0; c < c1; c++) {
                 const unsigned u = u0 + (c - c0);
                 const int s = u % kBsStages;
@@ -116,7 +124,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                 const unsigned char *dv = st + kBsCapRows * 16 + kBsCapEnt * (4 + sizeof(V));
                 for (int t = tid; t < ch.y; t += kBsConsumers) {
                     const int4 r = rec[t];
-                    const X xin = in[r.x];
+                    const X xin = xs[r.w];
                     X acc = (A.mode == 0) ? xin : X(0);
                     for (int k0 = 0; k0 < r.z; k0 += 8) {
                         const int cnt = min(8, r.z - k0);
@@ -245,6 +253,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
     for (int b = 0; b < nblk; b++) {
         const int p0 = b * R, p1 = std::min(n, p0 + R);
+        const int row_lo = lower ? p0 : n - p1;     // the block's rows are [row_lo, row_lo + p1 - p0)
         int maxlev = 0;
         for (int pos = p0; pos < p1; pos++) {
             const int row = row_of(pos);
@@ -279,11 +288,11 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     const int a = lower ? pntr[row] : diag[row] + 1;
                     const int e = lower ? diag[row] : pntr[row + 1];
                     if (ne + (e - a) > kBsCapEnt) break;
-                    recs.push_back(make_int4(row, ne, e - a, pos - p0));
+                    recs.push_back(make_int4(row, ne, e - a, row - row_lo));
                     for (int q = 0; q < e - a; q++) {
                         const int p = rev ? e - 1 - q : a + q;
                         const int pj = pos_of(indx[p]);
-                        codes.push_back(pj >= p0 ? pj - p0 : -(indx[p] + 1));
+                        codes.push_back(pj >= p0 ? indx[p] - row_lo : -(indx[p] + 1));
                         ent_map.push_back(p);
                     }
                     dv_map.push_back(diag[row]);
@@ -302,6 +311,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         blk_chunk.push_back((int)chunks.size());
     }
     S.n = n;
+    S.lower = lower;
     S.nblk = nblk;
     S.R = R;
     S.nchunks = (int)chunks.size();
@@ -367,6 +377,8 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     A.dvals = S.dvals;
     A.dv_double = S.dv_double;
     A.R = S.R;
+    A.n = S.n;
+    A.lower = S.lower;
     A.mode = mode;
     A.unit = unit;
     A.ticket = S.ticket;

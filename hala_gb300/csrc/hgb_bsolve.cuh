@@ -6,7 +6,7 @@
 namespace hgb {
 
 struct BlockSolve {
-    int n = 0, nblk = 0, nchunks = 0, nrec = 0, nent = 0, R = 0;
+    int n = 0, lower = 1, nblk = 0, nchunks = 0, nrec = 0, nent = 0, R = 0;
     int vsize = 0, dv_double = 0;
     int *blk_chunk = nullptr;   // [nblk+1]
     int4 *chunks = nullptr;     // [nchunks] {rec_off, nrows, ent_off, nent}
@@ -19,8 +19,8 @@ struct BlockSolve {
     void release();
 };
 
-// rows per block: the block's solution slice lives in shared memory
-inline int bsolve_rows(int xsize) { return xsize == 8 ? 8192 : 16384; }
+// rows per block: the block's solution slice (128 KB) lives in shared memory
+inline int bsolve_rows(int xsize) { return xsize == 8 ? 16384 : 32768; }
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
                    int rev, int R, BlockSolve &S);
