@@ -28,9 +28,10 @@ constexpr int kBsConsumers = 128;          // consumer threads (4 warps); + 1 pr
 constexpr int kBsCapRows = 128;            // rows per chunk (level piece)
 constexpr int kBsCapEnt = 1024;            // entries per chunk (padded to 8)
 
+// stage layout: [records | codes | values | diagonal values | 16-byte chunk descriptor]
 template <typename V>
 __host__ __device__ constexpr size_t bs_stage_bytes(size_t dvb) {
-    return (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * 4 + (size_t)kBsCapEnt * sizeof(V) + (size_t)kBsCapRows * dvb;
+    return (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * 4 + (size_t)kBsCapEnt * sizeof(V) + (size_t)kBsCapRows * dvb + 16;
 }
 
 struct BsArgs {
@@ -84,24 +85,36 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
         if (b >= A.nblk) break;
         const int c0 = __ldg(A.blk_chunk + b), c1 = __ldg(A.blk_chunk + b + 1);
         if (producer) {
-            if (tid == kBsConsumers) {
-                for (int c = c0; c < c1; c++) {
-                    const unsigned u = u0 + (c - c0);
-                    const int s = u % kBsStages;
-                    if (u >= kBsStages) mbar_wait(&empty[s], ((u / kBsStages) - 1) & 1, A.err);
-                    const int4 ch = __ldg(A.chunks + c);
-                    unsigned char *st = ring + s * sb;
-                    const uint32_t br = (uint32_t)ch.y * 16, be = (uint32_t)ch.w;
-                    const uint32_t bd = (uint32_t)(((ch.y + 7) & ~7) * dvb);
-                    // every chunk has >= 1 row, so the transaction count is never zero
-                    mbar_arrive_tx(&full[s], br + be * 4 + be * (uint32_t)sizeof(V) + bd);
-                    bulk_g2s(st, A.recs + ch.x, br, &full[s]);
-                    if (be) {
-                        bulk_g2s(st + kBsCapRows * 16, A.codes + ch.z, be * 4, &full[s]);
-                        bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * 4, (const V *)A.vals + ch.z, be * sizeof(V), &full[s]);
+            // descriptors of the next 32 chunks come in one warp-wide load; lane 0 issues the copies
+            const int lane = tid & 31;
+            for (int cb = c0; cb < c1; cb += 32) {
+                int4 mine = make_int4(0, 0, 0, 0);
+                if (cb + lane < c1) mine = __ldg(A.chunks + cb + lane);
+                const int cnt = min(32, c1 - cb);
+                for (int k = 0; k < cnt; k++) {
+                    int4 ch;
+                    ch.x = __shfl_sync(0xffffffffu, mine.x, k);
+                    ch.y = __shfl_sync(0xffffffffu, mine.y, k);
+                    ch.z = __shfl_sync(0xffffffffu, mine.z, k);
+                    ch.w = __shfl_sync(0xffffffffu, mine.w, k);
+                    if (lane == 0) {
+                        const unsigned u = u0 + (cb + k - c0);
+                        const int s = u % kBsStages;
+                        if (u >= kBsStages) mbar_wait(&empty[s], ((u / kBsStages) - 1) & 1, A.err);
+                        unsigned char *st = ring + s * sb;
+                        *(int4 *)(st + sb - 16) = ch;     // published by the arrive below
+                        const uint32_t br = (uint32_t)ch.y * 16, be = (uint32_t)ch.w;
+                        const uint32_t bd = (uint32_t)(((ch.y + 7) & ~7) * dvb);
+                        // every chunk has >= 1 row, so the transaction count is never zero
+                        mbar_arrive_tx(&full[s], br + be * 4 + be * (uint32_t)sizeof(V) + bd);
+                        bulk_g2s(st, A.recs + ch.x, br, &full[s]);
+                        if (be) {
+                            bulk_g2s(st + kBsCapRows * 16, A.codes + ch.z, be * 4, &full[s]);
+                            bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * 4, (const V *)A.vals + ch.z, be * sizeof(V), &full[s]);
+                        }
+                        bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * (4 + sizeof(V)),
+                                 (const unsigned char *)A.dvals + (size_t)ch.x * dvb, bd, &full[s]);
                     }
-                    bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * (4 + sizeof(V)),
-                             (const unsigned char *)A.dvals + (size_t)ch.x * dvb, bd, &full[s]);
                 }
             }
         } else {
@@ -116,8 +129,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                 const unsigned u = u0 + (c - c0);
                 const int s = u % kBsStages;
                 mbar_wait(&full[s], (u / kBsStages) & 1, A.err);
-                const int4 ch = __ldg(A.chunks + c);
                 const unsigned char *st = ring + s * sb;
+                const int4 ch = *(const int4 *)(st + sb - 16);
                 const int4 *rec = (const int4 *)st;
                 const int *code = (const int *)(st + kBsCapRows * 16);
                 const V *val = (const V *)(st + kBsCapRows * 16 + kBsCapEnt * 4);

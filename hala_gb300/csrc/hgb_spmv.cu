@@ -11,13 +11,15 @@
 
 namespace hgb {
 
-constexpr int kSpmvRows = 256;              // rows (threads) per tile
-constexpr int kSpmvSmem = 72 * 1024;        // dynamic smem per CTA: 3 CTAs per SM
+constexpr int kSpmvRows = 256;              // rows per tile = consumer threads (8 warps)
+constexpr int kSpmvStages = 4;              // TMA ring depth
+constexpr int kSpmvStageBytes = 27 * 1024;  // vals + indx of one tile
+constexpr int kSpmvSmem = kSpmvStages * kSpmvStageBytes;   // 108 KB: 2 CTAs per SM
 
 template <typename V>
 __host__ __device__ constexpr int spmv_cap() {
-    // entries per stage: two stages of (vals + indx) fit in kSpmvSmem with 8 entries of slack
-    return (kSpmvSmem / (2 * (int)(sizeof(V) + sizeof(int)))) / 16 * 16 - 16;
+    // entries per stage, with 16 entries of slack for the 16-byte rounding of the staged range
+    return (kSpmvStageBytes / (int)(sizeof(V) + sizeof(int))) / 16 * 16 - 16;
 }
 
 template <typename V>
@@ -28,38 +30,25 @@ struct TileGeom {
 };
 
 template <typename V>
-__device__ __forceinline__ TileGeom<V> tile_geom(const int *pntr, int n_rows, int tile, bool tma) {
+__device__ __forceinline__ TileGeom<V> tile_geom_se(int s, int e, bool tma) {
     constexpr int VA = 16 / sizeof(V);
     TileGeom<V> g;
-    int r0 = tile * kSpmvRows;
-    int r1 = min(r0 + kSpmvRows, n_rows);
-    g.s = __ldg(pntr + r0);
-    g.e = __ldg(pntr + r1);
-    bool staged = tma && (g.e - g.s) <= spmv_cap<V>();
-    g.sv = g.s & ~(VA - 1);
-    g.ev = staged ? (g.e & ~(VA - 1)) : g.sv;
-    g.si = g.s & ~3;
-    g.ei = staged ? (g.e & ~3) : g.si;
+    g.s = s;
+    g.e = e;
+    bool staged = tma && (e - s) <= spmv_cap<V>();
+    g.sv = s & ~(VA - 1);
+    g.ev = staged ? (e & ~(VA - 1)) : g.sv;
+    g.si = s & ~3;
+    g.ei = staged ? (e & ~3) : g.si;
     return g;
 }
 
-template <typename V>
-__device__ __forceinline__ void issue_tile(const TileGeom<V> &g, const V *vals, const int *indx, V *sv,
-                                           int *si, uint64_t *bar) {
-    uint32_t bv = (uint32_t)(g.ev - g.sv) * sizeof(V);
-    uint32_t bi = (uint32_t)(g.ei - g.si) * sizeof(int);
-    if (bv + bi == 0) {
-        mbar_arrive(bar);
-        return;
-    }
-    mbar_arrive_tx(bar, bv + bi);
-    if (bv) bulk_g2s(sv, vals + g.sv, bv, bar);
-    if (bi) bulk_g2s(si, indx + g.si, bi, bar);
-}
-
-// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (rows of A index x: square A).
+// Warp-specialized SpMV: warp 8 streams tile data into a kSpmvStages-deep shared ring with TMA
+// bulk copies (boundaries of the next 32 tiles fetched by its 32 lanes at once); warps 0-7 take
+// one row each per tile, issue up to 8 x-gathers at a time and sum in column order.
+// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A).
 template <typename V, bool FUSE_DOT>
-__global__ void __launch_bounds__(kSpmvRows)
+__global__ void __launch_bounds__(kSpmvRows + 32, 2)
 spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *__restrict__ indx,
               const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
               typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, int tma, double *partials,
@@ -68,69 +57,98 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
     if (skip && *skip) return;   // converged solver iteration replayed from a graph
     constexpr int CAP = spmv_cap<V>() + 16;
     extern __shared__ __align__(128) unsigned char smem[];
-    V *const sv0 = (V *)smem;
-    int *const si0 = (int *)(smem + 2 * CAP * sizeof(V));
-    __shared__ __align__(8) uint64_t bars[2];
-
+    __shared__ __align__(8) uint64_t full[kSpmvStages], empty[kSpmvStages];
     const int tid = threadIdx.x;
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int k = 0; k < kSpmvStages; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], 1);
+        }
         fence_mbar_init();
     }
     __syncthreads();
     const bool use_tma = tma != 0;
-    int tile = blockIdx.x;
-    if (tid == 0) {
-        if (tile < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, tile, use_tma), vals, indx, sv0, si0, &bars[0]);
-        int t1 = tile + gridDim.x;
-        if (t1 < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, t1, use_tma), vals, indx, sv0 + CAP, si0 + CAP, &bars[1]);
-    }
+    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     double dsum[1] = {0.0};
-    for (int k = 0; tile < ntiles; tile += gridDim.x, k++) {
-        const int st = k & 1;
-        TileGeom<V> g = tile_geom<V>(pntr, n_rows, tile, use_tma);
-        const int r = tile * kSpmvRows + tid;
-        int ps = 0, pe = 0;
-        if (r < n_rows) {
-            ps = __ldg(pntr + r);
-            pe = __ldg(pntr + r + 1);
-        }
-        mbar_wait(&bars[st], (uint32_t)((k >> 1) & 1), err);
-        if (r < n_rows) {
-            const V *svs = sv0 + st * CAP;
-            const int *sis = si0 + st * CAP;
-            X acc = X(0);
-            // up to 8 entries at a time: all x gathers in flight together, then the sum in
-            // column order (the reference's sequential order, so the result keeps its bits)
-            for (int j0 = ps; j0 < pe; j0 += 8) {
-                X xv[8], vv[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    const int j = j0 + k;
-                    if (j < pe) {
-                        V v = (j < g.ev) ? svs[j - g.sv] : __ldg(vals + j);
-                        int c = (j < g.ei) ? sis[j - g.si] : __ldg(indx + j);
-                        vv[k] = Val<V>::get(v);
-                        xv[k] = __ldg(x + c);
+    if (tid >= kSpmvRows) {
+        // producer warp
+        const int lane = tid & 31;
+        for (int base = 0; base < my_tiles; base += 32) {
+            int s = 0, e = 0;
+            const int mine = base + lane;
+            if (mine < my_tiles) {
+                const int tile = blockIdx.x + mine * gridDim.x;
+                s = __ldg(pntr + tile * kSpmvRows);
+                e = __ldg(pntr + min(tile * kSpmvRows + kSpmvRows, n_rows));
+            }
+            const int cnt = min(32, my_tiles - base);
+            for (int k = 0; k < cnt; k++) {
+                const int sk = __shfl_sync(0xffffffffu, s, k), ek = __shfl_sync(0xffffffffu, e, k);
+                if (lane == 0) {
+                    const int j = base + k;
+                    const int st = j % kSpmvStages;
+                    if (j >= kSpmvStages) mbar_wait(&empty[st], ((j / kSpmvStages) - 1) & 1, err);
+                    TileGeom<V> g = tile_geom_se<V>(sk, ek, use_tma);
+                    V *sv = (V *)(smem + st * kSpmvStageBytes);
+                    int *si = (int *)(smem + st * kSpmvStageBytes + CAP * sizeof(V));
+                    uint32_t bv = (uint32_t)(g.ev - g.sv) * sizeof(V);
+                    uint32_t bi = (uint32_t)(g.ei - g.si) * sizeof(int);
+                    if (bv + bi == 0) {
+                        mbar_arrive(&full[st]);
+                    } else {
+                        mbar_arrive_tx(&full[st], bv + bi);
+                        if (bv) bulk_g2s(sv, vals + g.sv, bv, &full[st]);
+                        if (bi) bulk_g2s(si, indx + g.si, bi, &full[st]);
                     }
                 }
-#pragma unroll
-                for (int k = 0; k < 8; k++)
-                    if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
             }
-            X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
-            y[r] = out;
-            if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
         }
-        __syncthreads();   // every thread is done with stage st
-        if (tid == 0) {
-            int t2 = tile + 2 * gridDim.x;
-            if (t2 < ntiles) issue_tile(tile_geom<V>(pntr, n_rows, t2, use_tma), vals, indx, sv0 + st * CAP, si0 + st * CAP, &bars[st]);
+    } else {
+        for (int j = 0; j < my_tiles; j++) {
+            const int tile = blockIdx.x + j * gridDim.x;
+            const int st = j % kSpmvStages;
+            const int r = tile * kSpmvRows + tid;
+            const int r1 = min(tile * kSpmvRows + kSpmvRows, n_rows);
+            const int ts = __ldg(pntr + tile * kSpmvRows), te = __ldg(pntr + r1);
+            int ps = 0, pe = 0;
+            if (r < n_rows) {
+                ps = __ldg(pntr + r);
+                pe = __ldg(pntr + r + 1);
+            }
+            const TileGeom<V> g = tile_geom_se<V>(ts, te, use_tma);
+            mbar_wait(&full[st], (uint32_t)((j / kSpmvStages) & 1), err);
+            if (r < n_rows) {
+                const V *svs = (const V *)(smem + st * kSpmvStageBytes);
+                const int *sis = (const int *)(smem + st * kSpmvStageBytes + CAP * sizeof(V));
+                X acc = X(0);
+                // up to 8 entries at a time: all x gathers in flight together, then the sum in
+                // column order (the reference's sequential order, so the result keeps its bits)
+                for (int j0 = ps; j0 < pe; j0 += 8) {
+                    X xv[8], vv[8];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const int jj = j0 + k;
+                        if (jj < pe) {
+                            V v = (jj < g.ev) ? svs[jj - g.sv] : __ldg(vals + jj);
+                            int c = (jj < g.ei) ? sis[jj - g.si] : __ldg(indx + jj);
+                            vv[k] = Val<V>::get(v);
+                            xv[k] = __ldg(x + c);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+                }
+                X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
+                y[r] = out;
+                if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
+            }
+            named_bar_sync(1, kSpmvRows);   // every consumer is done with stage st
+            if (tid == 0) mbar_arrive(&empty[st]);
         }
     }
     if (FUSE_DOT) {
-        grid_sum<1>(dsum, partials, counter, [&](double (&s)[1]) { *dot_out = s[0]; });
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
     }
 }
 
@@ -326,14 +344,14 @@ int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, cons
                   typename Val<V>::X *y, double *dot_out, const int *skip) {
     if (n_rows <= 0) return HGB_OK;
     int ntiles = (n_rows + kSpmvRows - 1) / kSpmvRows;
-    int grid = std::min(ntiles, c->num_sms * 3);
+    int grid = std::min(ntiles, c->num_sms * 2);
     int tma = (aligned16(vals) && aligned16(indx)) ? 1 : 0;
     if (dot_out) {
         grid = std::min(grid, kMaxReduceBlocks);
-        spmv_n_kernel<V, true><<<grid, kSpmvRows, kSpmvSmem, c->stream>>>(
+        spmv_n_kernel<V, true><<<grid, kSpmvRows + 32, kSpmvSmem, c->stream>>>(
             n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, c->partials, c->counter, dot_out, c->err, skip);
     } else {
-        spmv_n_kernel<V, false><<<grid, kSpmvRows, kSpmvSmem, c->stream>>>(
+        spmv_n_kernel<V, false><<<grid, kSpmvRows + 32, kSpmvSmem, c->stream>>>(
             n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, nullptr, nullptr, nullptr, c->err, skip);
     }
     return launch_check("spmv_n_kernel");

@@ -322,7 +322,7 @@ def solve_cg_op(engine, A, ilu, trans, b, x, tol, max_iter=INT_MAX):
     return info
 
 
-def solve_ir_pcg_op(engine, A64, A_inner, ilu_inner, trans, b, x, tol, inner_rtol=1e-4, max_inner=100000,
+def solve_ir_pcg_op(engine, A64, A_inner, ilu_inner, trans, b, x, tol, inner_rtol=1e-4, max_inner=5000,
                     max_outer=50):
     info = SolveInfo()
     check(_h.lib().hgb_ir_pcg_solve_op(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, ch_(trans),
@@ -352,7 +352,7 @@ def solve_gmres_ilu(engine, stop, restart, pntr, indx, vals, b, x, ilu=None, pol
     return solve_gmres(engine, stop, restart, pntr, indx, vals, b, x, ilu=ilu)
 
 
-def solve_ir_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, inner_rtol=1e-4, max_inner=100000, max_outer=50):
+def solve_ir_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, inner_rtol=1e-4, max_inner=5000, max_outer=50):
     """Mixed-precision ILU(0)-PCG: FP32/BF16 inner solves, FP64 refinement (no reference
     counterpart).  Returns SolveInfo."""
     info = SolveInfo()
@@ -381,7 +381,7 @@ def solve_cg_mixed(engine, stop, pntr_h, indx_h, vals_h, ilu, b_h, x_h):
 
 
 def solve_ir_pcg_mixed(engine, tol, pntr_h, indx_h, vals_h, ilu_inner, b_h, x_h, inner_rtol=1e-4,
-                       max_inner=100000, max_outer=50):
+                       max_inner=5000, max_outer=50):
     """Host-buffer mixed-precision refinement (hgb_mixed_ir_pcg_solve).  Returns SolveInfo."""
     info = SolveInfo()
     n = pntr_h.size - 1
