@@ -24,14 +24,17 @@
 namespace hgb {
 
 constexpr int kBsStages = 4;
-constexpr int kBsConsumers = 128;          // consumer threads (4 warps); + 1 producer warp
+constexpr int kBsConsumers = 128;          // consumer threads (4 warps)
+constexpr int kBsThreads = kBsConsumers + 32 + 32 * kBsStages;   // + TMA warp + one prefetch warp per stage
 constexpr int kBsCapRows = 128;            // rows per chunk (level piece)
-constexpr int kBsCapEnt = 1024;            // entries per chunk (padded to 8)
+constexpr int kBsCapEnt = 512;             // entries per chunk (padded to 8)
 
-// stage layout: [records | codes | values | diagonal values | 16-byte chunk descriptor]
-template <typename V>
+// stage layout: [records | codes | values | diagonal values | prefetched remote values |
+//                16-byte chunk descriptor]
+template <typename V, typename X>
 __host__ __device__ constexpr size_t bs_stage_bytes(size_t dvb) {
-    return (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * 4 + (size_t)kBsCapEnt * sizeof(V) + (size_t)kBsCapRows * dvb + 16;
+    return (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * 4 + (size_t)kBsCapEnt * sizeof(V) + (size_t)kBsCapRows * dvb +
+           (size_t)kBsCapEnt * sizeof(X) + 16;
 }
 
 struct BsArgs {
@@ -56,21 +59,24 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
 }
 
 template <typename V, typename X>
-__global__ void __launch_bounds__(kBsConsumers + 32, 1)
+__global__ void __launch_bounds__(kBsThreads, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
     const size_t dvb = A.dv_double ? sizeof(double) : sizeof(V);
-    const size_t sb = bs_stage_bytes<V>(dvb);
+    const size_t sb = bs_stage_bytes<V, X>(dvb);
+    const size_t rv_off = (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * (4 + sizeof(V)) + (size_t)kBsCapRows * dvb;
     X *xs = (X *)smem;
     unsigned char *ring = smem + (size_t)A.R * sizeof(X);
-    __shared__ __align__(8) uint64_t full[kBsStages], empty[kBsStages];
+    __shared__ __align__(8) uint64_t full[kBsStages], ready[kBsStages], empty[kBsStages];
     __shared__ int blk_sh;
     const int tid = threadIdx.x;
-    const bool producer = tid >= kBsConsumers;
+    const bool producer = (tid >= kBsConsumers) && (tid < kBsConsumers + 32);
+    const bool prefetcher = tid >= kBsConsumers + 32;
     if (tid == 0) {
         for (int s = 0; s < kBsStages; s++) {
             mbar_init(&full[s], 1);
+            mbar_init(&ready[s], 1);
             mbar_init(&empty[s], 1);
         }
         fence_mbar_init();
@@ -117,6 +123,37 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                     }
                 }
             }
+        } else if (prefetcher) {
+            // warp w owns ring stage w: once the stage's chunk has landed, load the chunk's
+            // dependencies on earlier blocks from L2 (16 loads in flight per lane) into the
+            // stage, then release it to the consumers.  Values still pending are re-polled there.
+            const int w = (tid - kBsConsumers - 32) >> 5, lane = tid & 31;
+            for (int c = c0; c < c1; c++) {
+                const unsigned u = u0 + (c - c0);
+                if ((int)(u % kBsStages) != w) continue;
+                mbar_wait(&full[w], (u / kBsStages) & 1, A.err);
+                unsigned char *st = ring + w * sb;
+                const int4 ch = *(const int4 *)(st + sb - 16);
+                const int *code = (const int *)(st + kBsCapRows * 16);
+                X *rv = (X *)(st + rv_off);
+                X v[kBsCapEnt / 32];
+#pragma unroll
+                for (int q = 0; q < kBsCapEnt / 32; q++) {
+                    const int e = lane + 32 * q;
+                    if (e < ch.w) {
+                        const int cd = code[e];
+                        if (cd < 0) v[q] = ld_relaxed(out + (-cd - 1));
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kBsCapEnt / 32; q++) {
+                    const int e = lane + 32 * q;
+                    if (e < ch.w && code[e] < 0) rv[e] = v[q];
+                }
+                __threadfence_block();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ready[w]);
+            }
         } else {
             // the block's right-hand side into its shared solution slice (slot = row - row_lo);
             // a row reads its own slot before overwriting it, dependencies read finished slots
@@ -128,9 +165,10 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
             for (int c = c0; c < c1; c++) {
                 const unsigned u = u0 + (c - c0);
                 const int s = u % kBsStages;
-                mbar_wait(&full[s], (u / kBsStages) & 1, A.err);
+                mbar_wait(&ready[s], (u / kBsStages) & 1, A.err);
                 const unsigned char *st = ring + s * sb;
                 const int4 ch = *(const int4 *)(st + sb - 16);
+                const X *rv = (const X *)(st + rv_off);
                 const int4 *rec = (const int4 *)st;
                 const int *code = (const int *)(st + kBsCapRows * 16);
                 const V *val = (const V *)(st + kBsCapRows * 16 + kBsCapEnt * 4);
@@ -153,8 +191,9 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                                     xv[k] = xs[cd];
                                     jj[k] = 0;
                                 } else {
+                                    xv[k] = rv[r.y + k0 + k];      // prefetched; pending -> re-poll
                                     jj[k] = -cd - 1;
-                                    remote |= 1u << k;
+                                    if (Pending<X>::is(xv[k])) remote |= 1u << k;
                                 }
                             }
                         if (remote) {
@@ -398,7 +437,7 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     A.err = c->err;
     A.skip = skip;
     const size_t dvb = S.dv_double ? sizeof(double) : sizeof(V);
-    const size_t smem = (size_t)S.R * sizeof(X) + kBsStages * bs_stage_bytes<V>(dvb);
+    const size_t smem = (size_t)S.R * sizeof(X) + kBsStages * bs_stage_bytes<V, X>(dvb);
     static bool attr[2][3] = {};
     const int xi = sizeof(X) == 8 ? 0 : 1, vi = sizeof(V) == 8 ? 0 : (sizeof(V) == 4 ? 1 : 2);
     if (!attr[xi][vi]) {
@@ -407,7 +446,7 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     }
     if (smem > 220 * 1024) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory", smem);
     const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-    bsolve_kernel<V, X><<<grid, kBsConsumers + 32, smem, c->stream>>>(A, alpha, in, out, pend_a, pend_b);
+    bsolve_kernel<V, X><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend_a, pend_b);
     return launch_check("bsolve_kernel");
 }
 

@@ -13,13 +13,14 @@ namespace hgb {
 
 constexpr int kSpmvRows = 256;              // rows per tile = consumer threads (8 warps)
 constexpr int kSpmvStages = 4;              // TMA ring depth
-constexpr int kSpmvStageBytes = 27 * 1024;  // vals + indx of one tile
+constexpr int kSpmvStageBytes = 27 * 1024;  // one tile: row pointers, header, vals, indx
+constexpr int kSpmvHdr = kSpmvRows * 4 + 16;  // pntr[r0, r0+256) and {s, e, k} of the tile
 constexpr int kSpmvSmem = kSpmvStages * kSpmvStageBytes;   // 108 KB: 2 CTAs per SM
 
 template <typename V>
 __host__ __device__ constexpr int spmv_cap() {
     // entries per stage, with 16 entries of slack for the 16-byte rounding of the staged range
-    return (kSpmvStageBytes / (int)(sizeof(V) + sizeof(int))) / 16 * 16 - 16;
+    return ((kSpmvStageBytes - kSpmvHdr) / (int)(sizeof(V) + sizeof(int))) / 16 * 16 - 16;
 }
 
 template <typename V>
@@ -88,15 +89,27 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
                     const int j = base + k;
                     const int st = j % kSpmvStages;
                     if (j >= kSpmvStages) mbar_wait(&empty[st], ((j / kSpmvStages) - 1) & 1, err);
+                    const int tile = blockIdx.x + j * gridDim.x;
+                    const int r0 = tile * kSpmvRows, r1 = min(r0 + kSpmvRows, n_rows);
+                    // row pointers [r0, r0 + kp) by bulk copy (kp a multiple of 4 so the size is a
+                    // multiple of 16 bytes and no copy reads past pntr[n_rows]); the rest from global
+                    const int kp = use_tma ? ((r1 - r0 + 1) & ~3) : 0;
+                    unsigned char *stg = smem + st * kSpmvStageBytes;
+                    int *hdr = (int *)(stg + kSpmvRows * 4);
+                    hdr[0] = sk;
+                    hdr[1] = ek;
+                    hdr[2] = kp;
                     TileGeom<V> g = tile_geom_se<V>(sk, ek, use_tma);
-                    V *sv = (V *)(smem + st * kSpmvStageBytes);
-                    int *si = (int *)(smem + st * kSpmvStageBytes + CAP * sizeof(V));
+                    V *sv = (V *)(stg + kSpmvHdr);
+                    int *si = (int *)(stg + kSpmvHdr + CAP * sizeof(V));
+                    uint32_t bp = (uint32_t)kp * 4;
                     uint32_t bv = (uint32_t)(g.ev - g.sv) * sizeof(V);
                     uint32_t bi = (uint32_t)(g.ei - g.si) * sizeof(int);
-                    if (bv + bi == 0) {
+                    if (bp + bv + bi == 0) {
                         mbar_arrive(&full[st]);
                     } else {
-                        mbar_arrive_tx(&full[st], bv + bi);
+                        mbar_arrive_tx(&full[st], bp + bv + bi);
+                        if (bp) bulk_g2s(stg, pntr + r0, bp, &full[st]);
                         if (bv) bulk_g2s(sv, vals + g.sv, bv, &full[st]);
                         if (bi) bulk_g2s(si, indx + g.si, bi, &full[st]);
                     }
@@ -108,18 +121,17 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
             const int tile = blockIdx.x + j * gridDim.x;
             const int st = j % kSpmvStages;
             const int r = tile * kSpmvRows + tid;
-            const int r1 = min(tile * kSpmvRows + kSpmvRows, n_rows);
-            const int ts = __ldg(pntr + tile * kSpmvRows), te = __ldg(pntr + r1);
-            int ps = 0, pe = 0;
-            if (r < n_rows) {
-                ps = __ldg(pntr + r);
-                pe = __ldg(pntr + r + 1);
-            }
-            const TileGeom<V> g = tile_geom_se<V>(ts, te, use_tma);
             mbar_wait(&full[st], (uint32_t)((j / kSpmvStages) & 1), err);
+            const unsigned char *stg = smem + st * kSpmvStageBytes;
+            const int *sp = (const int *)stg;
+            const int *hdr = (const int *)(stg + kSpmvRows * 4);
+            const int kp = hdr[2];
+            const TileGeom<V> g = tile_geom_se<V>(hdr[0], hdr[1], use_tma);
             if (r < n_rows) {
-                const V *svs = (const V *)(smem + st * kSpmvStageBytes);
-                const int *sis = (const int *)(smem + st * kSpmvStageBytes + CAP * sizeof(V));
+                const int ps = (tid < kp) ? sp[tid] : __ldg(pntr + r);
+                const int pe = (tid + 1 < kp) ? sp[tid + 1] : ((tid + 1 == kSpmvRows) ? hdr[1] : __ldg(pntr + r + 1));
+                const V *svs = (const V *)(stg + kSpmvHdr);
+                const int *sis = (const int *)(stg + kSpmvHdr + CAP * sizeof(V));
                 X acc = X(0);
                 // up to 8 entries at a time: all x gathers in flight together, then the sum in
                 // column order (the reference's sequential order, so the result keeps its bits)
@@ -345,7 +357,7 @@ int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, cons
     if (n_rows <= 0) return HGB_OK;
     int ntiles = (n_rows + kSpmvRows - 1) / kSpmvRows;
     int grid = std::min(ntiles, c->num_sms * 2);
-    int tma = (aligned16(vals) && aligned16(indx)) ? 1 : 0;
+    int tma = (aligned16(vals) && aligned16(indx) && aligned16(pntr)) ? 1 : 0;
     if (dot_out) {
         grid = std::min(grid, kMaxReduceBlocks);
         spmv_n_kernel<V, true><<<grid, kSpmvRows + 32, kSpmvSmem, c->stream>>>(
