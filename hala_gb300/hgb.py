@@ -85,6 +85,7 @@ _SIGS = {
     "hgb_batch_cg_solve": ([vp, vp, vp, f64, f64, i32, i32, vp, vp], i32),
     "hgb_batch_autotune": ([vp, vp, vp, f64, C.c_char_p, vp], i32),
     "hgb_batch_destroy": ([vp], i32),
+    "hgb_dot_f64_noalloc": ([i32, vp, vp, vp, vp], i32),
     "hgb_selftest_wait_timeout": ([vp, i32], i32),
 }
 

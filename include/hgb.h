@@ -233,6 +233,18 @@ int hgb_batch_autotune(hgb_batch *batch, const double *b, double *x, double rtol
                        const char *cache_path, hgb_batch_config *best);
 int hgb_batch_destroy(hgb_batch *batch);
 
+/* ------------------------------------------------------- allocation-free reduction ---- */
+/* No counterpart in the reference.  *result_device = <x, y> for callers that may not allocate
+ * device memory where they need the reduction (an allocator owned by someone else, a stream
+ * callback, a host integration that cannot create an hgb_ctx, which allocates).  Needs no
+ * context: the partial sums live in a static device array (one per 2048 entries), so
+ * n <= 33,554,432; larger n returns HGB_ERR_ARG before any launch.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress) and clears its counter: make it before any stream
+ * capture.  Calls share the array, so calls whose kernels overlap on the GPU race.  Runs on the
+ * current device, on the given stream (cudaStream_t, may be NULL); does not synchronise. */
+int hgb_dot_f64_noalloc(int n, const double *x, const double *y, double *result_device,
+                        void *stream);
+
 /* ----------------------------------------------------------- fault-path self test ------ */
 /* Launches one bounded device wait on a value nothing ever publishes; returns HGB_ERR_TIMEOUT
  * after spin_limit polls while leaving the context usable.  Test hook for the timeout path. */
