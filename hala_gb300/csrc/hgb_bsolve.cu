@@ -230,7 +230,9 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                     }
                     if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
                     if (!A.unit) {
-                        if (A.dv_double) acc = (X)__ddiv_rn((double)acc, ((const double *)dv)[t]);
+                        // mixed stores: the FP64 pivot division as one FP64 multiply by the pivot's
+                        // FP64 reciprocal (the slow FP64 divide stays out of the sweep)
+                        if (A.dv_double) acc = (X)__dmul_rn((double)acc, ((const double *)dv)[t]);
                         else acc = div_rn(acc, Val<V>::get(((const V *)dv)[t]));
                     }
                     acc = Pending<X>::canon(acc);
@@ -268,7 +270,7 @@ __global__ void bs_gather_piv_kernel(long n, const int *__restrict__ rowmap, con
                                      double *__restrict__ dst) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         int r = rowmap[i];
-        dst[i] = (r >= 0) ? piv[r] : 1.0;
+        dst[i] = (r >= 0) ? 1.0 / piv[r] : 1.0;   // FP64 reciprocal of the FP64 pivot
     }
 }
 

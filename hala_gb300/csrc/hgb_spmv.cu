@@ -7,6 +7,8 @@
 #include "hgb_kernels.cuh"
 
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 namespace hgb {
@@ -162,6 +164,47 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
     if (FUSE_DOT) {
         grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
     }
+}
+
+// Full-occupancy variant without shared memory: one row per thread, grid-stride, the row's
+// vals/indx and x gathers (8 at a time) straight from global through L1.  Same arithmetic.
+template <typename V, bool FUSE_DOT>
+__global__ void __launch_bounds__(256)
+spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
+                   const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
+                   typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter,
+                   double *dot_out, const int *skip) {
+    using X = typename Val<V>::X;
+    if (skip && *skip) return;
+    double dsum[1] = {0.0};
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+        const int ps = __ldg(pntr + r), pe = __ldg(pntr + r + 1);
+        X acc = X(0);
+        for (int j0 = ps; j0 < pe; j0 += 8) {
+            X xv[8], vv[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (j0 + k < pe) {
+                    vv[k] = Val<V>::get(__ldg(vals + j0 + k));
+                    xv[k] = __ldg(x + __ldg(indx + j0 + k));
+                }
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+        }
+        X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
+        y[r] = out;
+        if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
+    }
+    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+}
+
+static int spmv_variant() {
+    static int v = [] {
+        const char *e = getenv("HGB_SPMV");
+        return (e && std::string(e) == "direct") ? 1 : 0;
+    }();
+    return v;
 }
 
 // transposed product by atomic scatter (stateless path): y[c] += (alpha * x[i]) * v_ic
@@ -355,6 +398,16 @@ int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, cons
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
                   typename Val<V>::X *y, double *dot_out, const int *skip) {
     if (n_rows <= 0) return HGB_OK;
+    if (spmv_variant() == 1) {
+        int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
+        if (dot_out)
+            spmv_direct_kernel<V, true><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, c->partials,
+                                                                 c->counter, dot_out, skip);
+        else
+            spmv_direct_kernel<V, false><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr,
+                                                                  nullptr, nullptr, skip);
+        return launch_check("spmv_direct_kernel");
+    }
     int ntiles = (n_rows + kSpmvRows - 1) / kSpmvRows;
     int grid = std::min(ntiles, c->num_sms * 2);
     int tma = (aligned16(vals) && aligned16(indx) && aligned16(pntr)) ? 1 : 0;

@@ -13,6 +13,7 @@ import torch
 
 from hala_gb300 import engine as E
 from hala_gb300 import problems as P
+from hala_gb300.hgb import HGB_ERR_NOT_CONVERGED, HgbError
 
 
 class Stencil:
@@ -69,13 +70,23 @@ class Solver:
         M = E.make_ilu(self.eng, st.gp, st.gi, v64, store=torch.float32)
         return (A64, A32, M, v64, v32)
 
-    def solve(self, vals, rhs, trans="N", ops=None):
+    def solve(self, vals, rhs, trans="N", ops=None, sweeps=None):
+        """sweeps=None: refine to tol; sweeps=k: exactly k refinement sweeps (no tolerance), which
+        drives the error to the FP64 floor kappa*eps (used by the finite-difference check)."""
         ops = ops or self._setup(vals)
         A64, A32, M = ops[:3]
         x = torch.zeros_like(rhs)
-        tol = self.tol * float(torch.linalg.vector_norm(rhs))
-        E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, tol, inner_rtol=self.inner_rtol,
-                          max_inner=self.max_inner, max_outer=200)
+        if sweeps is None:
+            tol = self.tol * float(torch.linalg.vector_norm(rhs))
+            E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, tol, inner_rtol=self.inner_rtol,
+                              max_inner=self.max_inner, max_outer=200)
+        else:
+            try:
+                E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, 0.0, inner_rtol=self.inner_rtol,
+                                  max_inner=self.max_inner, max_outer=sweeps)
+            except HgbError as e:     # a zero tolerance is never met: the sweeps ran out, x is final
+                if e.status != HGB_ERR_NOT_CONVERGED:
+                    raise
         return x, ops
 
 
@@ -101,3 +112,10 @@ def loss(solver, st, theta, f, u_target):
     vals = assemble(st, theta)
     u = DiffSolve.apply(vals, f, solver)
     return torch.sum((u - u_target) ** 2)
+
+
+def loss_converged(solver, st, theta, f, u_target, sweeps=12):
+    """L(theta) from a solve run for a fixed number of sweeps past convergence (no autograd)."""
+    with torch.no_grad():
+        u, _ = solver.solve(assemble(st, theta), f, sweeps=sweeps)
+        return torch.sum((u - u_target) ** 2)

@@ -49,13 +49,13 @@ def test_gradient_vs_central_differences(setup):
         for _ in range(64):
             d = torch.from_numpy(rng.standard_normal(N * N)).to(dev)
             d /= torch.linalg.vector_norm(d)
-            lp = H.loss(solver, st, theta + h * d, f, u_target)
-            lm = H.loss(solver, st, theta - h * d, f, u_target)
+            lp = H.loss_converged(solver, st, theta + h * d, f, u_target)
+            lm = H.loss_converged(solver, st, theta - h * d, f, u_target)
             fd = float((lp - lm) / (2 * h))
             ad = float(torch.dot(g, d))
             errs.append(abs(fd - ad) / max(abs(ad), 1e-30 * float(L)))
-    # finite differences of solves converged to the FP64 residual floor carry ~1e-3 noise; the
-    # exact check of the adjoint is test_gradient_vs_fp64_oracle
+    # the FD losses come from solves refined to the FP64 floor (error ~ kappa * eps); the exact
+    # check of the adjoint is test_gradient_vs_fp64_oracle
     errs = np.array(errs)
     assert np.median(errs) < 1e-2 and np.quantile(errs, 0.9) < 5e-2, (np.median(errs), np.quantile(errs, 0.9))
 
