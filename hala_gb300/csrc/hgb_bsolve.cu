@@ -1,255 +1,256 @@
 // Block-local level-scheduled sparse triangular solve for sm_103a.
 //
-// Rows are cut, in solve order, into contiguous blocks of R rows; one persistent CTA solves one
-// block at a time (blocks handed out by an atomic ticket in solve order, so a CTA only waits on
-// blocks already taken by running CTAs).  Inside a block the rows are grouped by LOCAL level
-// (levels over the dependencies that stay inside the block): a dependency inside the block is
-// read from the block's solution slice in shared memory, a dependency on an earlier block is
-// read from global memory, where a not-yet-produced entry holds a signalling-NaN pattern (the
-// value is its own ready flag, bounded poll).  A named barrier separates local levels, so most
-// dependency hops cost a shared-memory round trip instead of an L2 round trip between SMs.
+// Rows are cut, in solve order, into contiguous blocks of at most R rows and kBsStepCap steps.
+// One persistent CTA of 128 threads solves one block at a time; blocks are handed out by an
+// atomic ticket in solve order, so a CTA only waits on blocks already taken by running CTAs.
+// Inside a block the rows are grouped by LOCAL level (levels over the dependencies that stay
+// inside the block) and each level is cut into steps of at most 128 rows, one row per thread.
+// A dependency inside the block is read from the block's solution slice in shared memory. A
+// dependency on an earlier block is read from global memory, where a not-yet-produced entry
+// holds a signalling-NaN pattern: the value is its own ready flag (bounded poll). A barrier after
+// the last step of each level publishes the level in shared memory.
 //
-// The per-level data is repacked at analysis time into contiguous chunks (row records, entry
-// codes, entry values, diagonal values), streamed into a shared-memory ring by a producer warp
-// with TMA bulk copies (cp.async.bulk + mbarrier full/empty pairs) while the consumer warps
-// compute.  Entries keep the reference's accumulation order within each row, so results are
-// bit-identical to the sequential loops of apply_ilu_array / sparse_trsv_array.
+// Each row is stored as a packet of 16-byte pieces: three dependency codes and the row's slot,
+// then the values and the diagonal terms. Packets are laid out per step, so thread t of a step
+// finds its packet at (the step's first packet + t). Every thread streams its own packets into a
+// private ring of D steps in shared memory with cp.async, one commit group per step, so the ring
+// needs no handshake between warps: a thread waits only for its own copies. The first dependency
+// of a row on an earlier block is loaded H steps before its use, which hides the L2 round trip
+// between the SMs that solve consecutive blocks. Entries keep the reference's accumulation order
+// within each row, so results are bit-identical to the sequential loops of apply_ilu_array /
+// sparse_trsv_array (sparse/hala_sparse_utils.hpp).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
 #include "hgb_bsolve.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 namespace hgb {
 
-constexpr int kBsStages = 4;
-constexpr int kBsConsumers = 128;          // consumer threads (4 warps)
-constexpr int kBsThreads = kBsConsumers + 32 + 32 * kBsStages;   // + TMA warp + one prefetch warp per stage
-constexpr int kBsCapRows = 128;            // rows per chunk (level piece)
-constexpr int kBsCapEnt = 512;             // entries per chunk (padded to 8)
+constexpr int kBsThreads = 128;   // one row per thread per step
+constexpr int kBsStepCap = 512;   // steps per block: the block's descriptors sit in shared memory
+constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
-// stage layout: [records | codes | values | diagonal values | prefetched remote values |
-//                16-byte chunk descriptor]
+// value pieces per packet (NV), ring depth in steps (D), look-ahead of the remote loads (H)
+template <typename V> struct BsCfg;
+template <> struct BsCfg<double> { static constexpr int NV = 3, D = 10, H = 4; };
+template <> struct BsCfg<float> { static constexpr int NV = 1, D = 18, H = 6; };
+template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 18, H = 6; };
+
+inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
+
+// shared memory: [ring D x (1 + NV) x 128 pieces | step descriptors | solution slice]
 template <typename V, typename X>
-__host__ __device__ constexpr size_t bs_stage_bytes(size_t dvb) {
-    return (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * 4 + (size_t)kBsCapEnt * sizeof(V) + (size_t)kBsCapRows * dvb +
-           (size_t)kBsCapEnt * sizeof(X) + 16;
+constexpr size_t bs_smem_bytes(int R) {
+    return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)kBsStepCap * 16 +
+           ((size_t)R + 16 / sizeof(X)) * sizeof(X);
+}
+
+// One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
+//   FP64 {v0, v1} {v2, RN(1/d)} {d, 0};  FP32 {v0, v1, v2, dv};  BF16 {v0 | v1 << 16, v2, dv, 0}
+// dv is the FP32 diagonal (divided by) or the FP32 reciprocal of an FP64 pivot (multiplied by).
+template <typename V> struct BsRow;
+template <> struct BsRow<double> {
+    double v[3], d, dinv;
+    __device__ __forceinline__ void load(const int4 *p) {
+        const double2 a = *(const double2 *)p, b = *(const double2 *)(p + kBsThreads),
+                      c = *(const double2 *)(p + 2 * kBsThreads);
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = b.x;
+        dinv = b.y;
+        d = c.x;
+    }
+};
+template <> struct BsRow<float> {
+    float v[3], d;
+    __device__ __forceinline__ void load(const int4 *p) {
+        const float4 a = *(const float4 *)p;
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = a.z;
+        d = a.w;
+    }
+};
+template <> struct BsRow<uint16_t> {
+    float v[3], d;
+    __device__ __forceinline__ void load(const int4 *p) {
+        const int4 a = *p;
+        v[0] = __uint_as_float((unsigned)a.x << 16);
+        v[1] = __uint_as_float((unsigned)a.x & 0xFFFF0000u);
+        v[2] = __uint_as_float((unsigned)a.y << 16);
+        d = __int_as_float(a.z);
+    }
+};
+
+// a / d correctly rounded, from the stored y = RN(1/d): q0 = RN(a y), r = a - d q0 (exact with
+// FMA), q = RN(q0 + r y) equals RN(a / d) (Markstein, IBM J. Res. Dev. 34(1), 1990) when no step
+// overflows or underflows.  Operands with |exponent| >= 500, zeros, infinities and NaNs take the
+// division instead.
+__device__ __forceinline__ double bs_divide(double a, const BsRow<double> &r, int) {
+    const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
+    const unsigned ed = ((unsigned)__double2hiint(r.d) >> 20) & 0x7FFu;
+    if (ea - 523u < 1000u && ed - 523u < 1000u) {
+        const double q0 = __dmul_rn(a, r.dinv);
+        const double rem = __fma_rn(-r.d, q0, a);
+        return __fma_rn(rem, r.dinv, q0);
+    }
+    return __ddiv_rn(a, r.d);
+}
+template <typename V>
+__device__ __forceinline__ float bs_divide(float a, const BsRow<V> &r, int recip) {
+    return recip ? __fmul_rn(a, r.d) : __fdiv_rn(a, r.d);
 }
 
 struct BsArgs {
     int nblk;
-    const int *blk_chunk;    // [nblk+1] chunk range of each block
-    const int4 *chunks;      // {rec_off, nrows, ent_off, nent (padded)}
-    const int4 *recs;        // {row, entry offset in chunk, ndeps, smem slot}
-    const int *codes;        // >= 0: smem slot of a local dependency; < 0: -(global index + 1)
-    const void *vals;        // V
-    const void *dvals;       // V or double (pivots)
-    int dv_double;           // dvals are FP64 pivots
-    int R;                   // rows per block (smem slice)
-    int n, lower;            // block b holds rows [row_lo, row_lo + cnt) in both directions
-    int mode, unit;
+    const int4 *blk;      // {first step, end step, row_lo, rows}
+    const int4 *desc;     // {first packet, rows, first overflow entry, overflow width | barrier << 16}
+    const int4 *pk0;      // {code0, code1, code2, slot | ndeps << 16}; code >= 0: slot, < 0: -(row + 1)
+    const int4 *pkv;      // value pieces, piece p of packet i at pkv[p * npk + i]
+    long npk;
+    const int *ovf_codes;   // dependency k >= 3 of row t of a step: [first + (k - 3) * rows + t]
+    const void *ovf_vals;
+    int mode, unit, recip;
     int *ticket;
     int *err;
     const int *skip;
 };
 
-__device__ __forceinline__ void named_bar(int id, int nthreads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
-
 template <typename V, typename X>
 __global__ void __launch_bounds__(kBsThreads, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
+    constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, H = BsCfg<V>::H, NP = 1 + NV;
+    static_assert(H >= 1 && D - 1 - H >= 1, "ring too shallow for the look-ahead");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
-    const size_t dvb = A.dv_double ? sizeof(double) : sizeof(V);
-    const size_t sb = bs_stage_bytes<V, X>(dvb);
-    const size_t rv_off = (size_t)kBsCapRows * 16 + (size_t)kBsCapEnt * (4 + sizeof(V)) + (size_t)kBsCapRows * dvb;
-    X *xs = (X *)smem;
-    unsigned char *ring = smem + (size_t)A.R * sizeof(X);
-    __shared__ __align__(8) uint64_t full[kBsStages], ready[kBsStages], empty[kBsStages];
+    int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
+    int4 *sdesc = ring + D * NP * kBsThreads;           // [kBsStepCap]
+    X *xsbuf = (X *)(sdesc + kBsStepCap);               // [R + 16 / sizeof(X)]
     __shared__ int blk_sh;
-    const int tid = threadIdx.x;
-    const bool producer = (tid >= kBsConsumers) && (tid < kBsConsumers + 32);
-    const bool prefetcher = tid >= kBsConsumers + 32;
-    if (tid == 0) {
-        for (int s = 0; s < kBsStages; s++) {
-            mbar_init(&full[s], 1);
-            mbar_init(&ready[s], 1);
-            mbar_init(&empty[s], 1);
-        }
-        fence_mbar_init();
-    }
-    __syncthreads();
-    unsigned u0 = 0;   // chunks this CTA has streamed so far (stage / phase bookkeeping)
+    const int t = threadIdx.x;
     for (;;) {
-        if (tid == 0) blk_sh = atomicAdd(A.ticket, 1);
+        __syncthreads();   // every thread is done with the previous block
+        if (t == 0) blk_sh = atomicAdd(A.ticket, 1);
         __syncthreads();
         const int b = blk_sh;
-        __syncthreads();
         if (b >= A.nblk) break;
-        const int c0 = __ldg(A.blk_chunk + b), c1 = __ldg(A.blk_chunk + b + 1);
-        if (producer) {
-            // descriptors of the next 32 chunks come in one warp-wide load; lane 0 issues the copies
-            const int lane = tid & 31;
-            for (int cb = c0; cb < c1; cb += 32) {
-                int4 mine = make_int4(0, 0, 0, 0);
-                if (cb + lane < c1) mine = __ldg(A.chunks + cb + lane);
-                const int cnt = min(32, c1 - cb);
-                for (int k = 0; k < cnt; k++) {
-                    int4 ch;
-                    ch.x = __shfl_sync(0xffffffffu, mine.x, k);
-                    ch.y = __shfl_sync(0xffffffffu, mine.y, k);
-                    ch.z = __shfl_sync(0xffffffffu, mine.z, k);
-                    ch.w = __shfl_sync(0xffffffffu, mine.w, k);
-                    if (lane == 0) {
-                        const unsigned u = u0 + (cb + k - c0);
-                        const int s = u % kBsStages;
-                        if (u >= kBsStages) mbar_wait(&empty[s], ((u / kBsStages) - 1) & 1, A.err);
-                        unsigned char *st = ring + s * sb;
-                        *(int4 *)(st + sb - 16) = ch;     // published by the arrive below
-                        const uint32_t br = (uint32_t)ch.y * 16, be = (uint32_t)ch.w;
-                        const uint32_t bd = (uint32_t)(((ch.y + 7) & ~7) * dvb);
-                        // every chunk has >= 1 row, so the transaction count is never zero
-                        mbar_arrive_tx(&full[s], br + be * 4 + be * (uint32_t)sizeof(V) + bd);
-                        bulk_g2s(st, A.recs + ch.x, br, &full[s]);
-                        if (be) {
-                            bulk_g2s(st + kBsCapRows * 16, A.codes + ch.z, be * 4, &full[s]);
-                            bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * 4, (const V *)A.vals + ch.z, be * sizeof(V), &full[s]);
-                        }
-                        bulk_g2s(st + kBsCapRows * 16 + kBsCapEnt * (4 + sizeof(V)),
-                                 (const unsigned char *)A.dvals + (size_t)ch.x * dvb, bd, &full[s]);
-                    }
+        const int4 bi = __ldg(A.blk + b);
+        const int ns = bi.y - bi.x, row_lo = bi.z, cnt = bi.w;
+
+        // the block's step descriptors and its right-hand side slice, in one commit group
+        for (int i = t; i < ns; i += kBsThreads) cp_async16(sdesc + i, A.desc + bi.x + i);
+        constexpr int E = 16 / (int)sizeof(X);
+        const X *src = in + row_lo;
+        const int mis = (int)(((size_t)src & 15) / sizeof(X));
+        X *xs = xsbuf + mis;   // xs[i] and src[i] sit at the same offset modulo 16 bytes
+        const int head = min(cnt, (E - mis) % E);
+        const int body = (cnt - head) / E;
+        for (int i = t; i < body; i += kBsThreads) cp_async16(xs + head + i * E, src + head + i * E);
+        for (int i = head + body * E + t; i < cnt; i += kBsThreads) xs[i] = src[i];
+        if (t < head) xs[t] = src[t];
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncthreads();
+
+        // thread t's packet of step s into ring slot s % D (an empty group past the last step)
+        auto issue = [&](int s) {
+            if (s < ns) {
+                const int4 d = sdesc[s];
+                if (t < d.y) {
+                    int4 *slot = ring + (s % D) * NP * kBsThreads + t;
+                    cp_async16(slot, A.pk0 + d.x + t);
+#pragma unroll
+                    for (int p = 0; p < NV; p++)
+                        cp_async16(slot + (1 + p) * kBsThreads, A.pkv + (long)p * A.npk + d.x + t);
                 }
             }
-        } else if (prefetcher) {
-            // warp w owns ring stage w: once the stage's chunk has landed, load the chunk's
-            // dependencies on earlier blocks from L2 (16 loads in flight per lane) into the
-            // stage, then release it to the consumers.  Values still pending are re-polled there.
-            const int w = (tid - kBsConsumers - 32) >> 5, lane = tid & 31;
-            for (int c = c0; c < c1; c++) {
-                const unsigned u = u0 + (c - c0);
-                if ((int)(u % kBsStages) != w) continue;
-                mbar_wait(&full[w], (u / kBsStages) & 1, A.err);
-                unsigned char *st = ring + w * sb;
-                const int4 ch = *(const int4 *)(st + sb - 16);
-                const int *code = (const int *)(st + kBsCapRows * 16);
-                X *rv = (X *)(st + rv_off);
-                X v[kBsCapEnt / 32];
-#pragma unroll
-                for (int q = 0; q < kBsCapEnt / 32; q++) {
-                    const int e = lane + 32 * q;
-                    if (e < ch.w) {
-                        const int cd = code[e];
-                        if (cd < 0) v[q] = ld_relaxed(out + (-cd - 1));
-                    }
+            cp_async_commit();
+        };
+        // load the first remote dependency of thread t's row of step s (landed in the ring)
+        auto lookahead = [&](int s) -> X {
+            X v = X(0);
+            if (s < ns) {
+                const int4 d = sdesc[s];
+                if (t < d.y) {
+                    const int4 p0 = ring[(s % D) * NP * kBsThreads + t];
+                    const int nd = (int)((unsigned)p0.w >> 16);
+                    const int j = (nd > 0 && p0.x < 0) ? p0.x : (nd > 1 && p0.y < 0) ? p0.y : (nd > 2 && p0.z < 0) ? p0.z : 0;
+                    if (j < 0) v = ld_relaxed(out + (-j - 1));
                 }
-#pragma unroll
-                for (int q = 0; q < kBsCapEnt / 32; q++) {
-                    const int e = lane + 32 * q;
-                    if (e < ch.w && code[e] < 0) rv[e] = v[q];
-                }
-                __threadfence_block();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&ready[w]);
             }
-        } else {
-            // the block's right-hand side into its shared solution slice (slot = row - row_lo);
-            // a row reads its own slot before overwriting it, dependencies read finished slots
-            const int cnt_rows = min(A.R, A.n - b * A.R);
-            const int row_lo = A.lower ? b * A.R : A.n - b * A.R - cnt_rows;
-#pragma unroll 4
-            for (int i = tid; i < cnt_rows; i += kBsConsumers) xs[i] = in[row_lo + i];
-            named_bar(1, kBsConsumers);
-            for (int c = c0; c < c1; c++) {
-                const unsigned u = u0 + (c - c0);
-                const int s = u % kBsStages;
-                mbar_wait(&ready[s], (u / kBsStages) & 1, A.err);
-                const unsigned char *st = ring + s * sb;
-                const int4 ch = *(const int4 *)(st + sb - 16);
-                const X *rv = (const X *)(st + rv_off);
-                const int4 *rec = (const int4 *)st;
-                const int *code = (const int *)(st + kBsCapRows * 16);
-                const V *val = (const V *)(st + kBsCapRows * 16 + kBsCapEnt * 4);
-                const unsigned char *dv = st + kBsCapRows * 16 + kBsCapEnt * (4 + sizeof(V));
-                for (int t = tid; t < ch.y; t += kBsConsumers) {
-                    const int4 r = rec[t];
-                    const X xin = xs[r.w];
-                    X acc = (A.mode == 0) ? xin : X(0);
-                    for (int k0 = 0; k0 < r.z; k0 += 8) {
-                        const int cnt = min(8, r.z - k0);
-                        int jj[8];
-                        X vv[8], xv[8];
-                        unsigned remote = 0;
+            return v;
+        };
+        auto solve_row = [&](int s, X rv) {
+            const int4 d = sdesc[s];
+            if (t >= d.y) return;
+            const int4 *slot = ring + (s % D) * NP * kBsThreads + t;
+            const int4 p0 = slot[0];
+            BsRow<V> rw;
+            rw.load(slot + kBsThreads);
+            const int sl = p0.w & 0xFFFF, nd = (int)((unsigned)p0.w >> 16);
+            const int code[kBsInline] = {p0.x, p0.y, p0.z};
+            const X xin = xs[sl];
+            X acc = (A.mode == 0) ? xin : X(0);
+            bool first = true;
 #pragma unroll
-                        for (int k = 0; k < 8; k++)
-                            if (k < cnt) {
-                                const int cd = code[r.y + k0 + k];
-                                vv[k] = Val<V>::get(val[r.y + k0 + k]);
-                                if (cd >= 0) {
-                                    xv[k] = xs[cd];
-                                    jj[k] = 0;
-                                } else {
-                                    xv[k] = rv[r.y + k0 + k];      // prefetched; pending -> re-poll
-                                    jj[k] = -cd - 1;
-                                    if (Pending<X>::is(xv[k])) remote |= 1u << k;
-                                }
-                            }
-                        if (remote) {
-                            // poll the remote dependencies together (one L2 round trip when ready)
-                            int spins = 0;
-#pragma unroll
-                            for (int k = 0; k < 8; k++)
-                                if (remote & (1u << k)) {
-                                    xv[k] = ld_relaxed(out + jj[k]);
-                                    if (!Pending<X>::is(xv[k])) remote &= ~(1u << k);
-                                }
-                            while (remote) {
-                                if (++spins > kSpinLimit) {
-                                    atomicOr(A.err, DEV_ERR_TIMEOUT);
-#pragma unroll
-                                    for (int k = 0; k < 8; k++)
-                                        if (remote & (1u << k)) xv[k] = Pending<X>::canon(Pending<X>::value());
-                                    break;
-                                }
-#pragma unroll
-                                for (int k = 0; k < 8; k++)
-                                    if (remote & (1u << k)) {
-                                        xv[k] = ld_relaxed(out + jj[k]);
-                                        if (!Pending<X>::is(xv[k])) remote &= ~(1u << k);
-                                    }
-                            }
-                        }
-#pragma unroll
-                        for (int k = 0; k < 8; k++)
-                            if (k < cnt) {
-                                if (A.mode == 0) acc = sub_rn(acc, mul_rn(vv[k], xv[k]));
-                                else acc = add_rn(acc, mul_rn(vv[k], xv[k]));
-                            }
+            for (int k = 0; k < kBsInline; k++) {
+                if (k < nd) {
+                    const int cd = code[k];
+                    X xv;
+                    if (cd >= 0) {
+                        xv = xs[cd];
+                    } else {
+                        xv = first ? rv : Pending<X>::value();
+                        first = false;
+                        if (Pending<X>::is(xv)) xv = wait_value(out + (-cd - 1), A.err);
                     }
-                    if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
-                    if (!A.unit) {
-                        // mixed stores: the FP64 pivot division as one FP64 multiply by the pivot's
-                        // FP64 reciprocal (the slow FP64 divide stays out of the sweep)
-                        if (A.dv_double) acc = (X)__dmul_rn((double)acc, ((const double *)dv)[t]);
-                        else acc = div_rn(acc, Val<V>::get(((const V *)dv)[t]));
-                    }
-                    acc = Pending<X>::canon(acc);
-                    xs[r.w] = acc;
-                    st_relaxed(out + r.x, acc);
-                    if (pend_a) pend_a[r.x] = Pending<X>::value();
-                    if (pend_b) pend_b[r.x] = Pending<X>::value();
+                    const X vk = (X)rw.v[k];
+                    acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xv)) : add_rn(acc, mul_rn(vk, xv));
                 }
-                named_bar(1, kBsConsumers);     // this level is complete in shared memory
-                if (tid == 0) mbar_arrive(&empty[s]);
+            }
+            for (int k = kBsInline; k < nd; k++) {
+                const long e = (long)d.z + (long)(k - kBsInline) * d.y + t;
+                const int cd = __ldg(A.ovf_codes + e);
+                const X vk = Val<V>::get(__ldg((const V *)A.ovf_vals + e));
+                const X xv = (cd >= 0) ? xs[cd] : wait_value(out + (-cd - 1), A.err);
+                acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xv)) : add_rn(acc, mul_rn(vk, xv));
+            }
+            if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
+            if (!A.unit) acc = bs_divide(acc, rw, A.recip);
+            acc = Pending<X>::canon(acc);
+            xs[sl] = acc;
+            const int row = row_lo + sl;
+            st_relaxed(out + row, acc);
+            if (pend_a) pend_a[row] = Pending<X>::value();
+            if (pend_b) pend_b[row] = Pending<X>::value();
+        };
+
+        // ring prologue: steps 0 .. D-2 in flight, the first H of them landed
+        for (int s = 0; s < D - 1; s++) issue(s);
+        cp_async_wait<D - 1 - H>();
+        X rv[H];
+#pragma unroll
+        for (int u = 0; u < H; u++) rv[u] = lookahead(u);
+        for (int sb = 0; sb < ns; sb += H) {
+#pragma unroll
+            for (int u = 0; u < H; u++) {
+                const int s = sb + u;
+                if (s < ns) {
+                    issue(s + D - 1);
+                    cp_async_wait<D - 1 - H>();   // steps <= s + H have landed
+                    solve_row(s, rv[u]);
+                    rv[u] = lookahead(s + H);
+                    if (sdesc[s].w >> 16) __syncthreads();   // last step of a level
+                }
             }
         }
-        u0 += (unsigned)(c1 - c0);
-        __syncthreads();
+        cp_async_wait<0>();
     }
-    // drain: the producer issued nothing beyond the consumed chunks; last CTA resets the ticket
-    if (tid == 0) {
+    // the last CTA to leave resets the ticket for the next launch
+    if (t == 0) {
         __threadfence();
         if (atomicAdd(A.ticket + 1, 1) == (int)gridDim.x - 1) {
             A.ticket[0] = 0;
@@ -258,162 +259,227 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
     }
 }
 
+// value pieces of the packets (layout in BsRow)
+template <typename V>
+__global__ void bs_pack_kernel(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
+                               const int *__restrict__ dv_row, const V *__restrict__ src,
+                               const double *__restrict__ piv, int4 *__restrict__ pkv);
+
+template <>
+__global__ void bs_pack_kernel<double>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
+                                       const int *__restrict__ dv_row, const double *__restrict__ src,
+                                       const double *__restrict__ piv, int4 *__restrict__ pkv) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
+        double v[3];
+        for (int k = 0; k < 3; k++) {
+            const int m = map3[3 * i + k];
+            v[k] = m >= 0 ? src[m] : 0.0;
+        }
+        const int dm = dv_map[i], r = dv_row[i];
+        const double d = piv ? piv[r] : (dm >= 0 ? src[dm] : 1.0);
+        ((double2 *)pkv)[i] = make_double2(v[0], v[1]);
+        ((double2 *)(pkv + npk))[i] = make_double2(v[2], 1.0 / d);   // correctly rounded reciprocal
+        ((double2 *)(pkv + 2 * npk))[i] = make_double2(d, 0.0);
+    }
+}
+
+template <>
+__global__ void bs_pack_kernel<float>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
+                                      const int *__restrict__ dv_row, const float *__restrict__ src,
+                                      const double *__restrict__ piv, int4 *__restrict__ pkv) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
+        float v[3];
+        for (int k = 0; k < 3; k++) {
+            const int m = map3[3 * i + k];
+            v[k] = m >= 0 ? src[m] : 0.0f;
+        }
+        const int dm = dv_map[i], r = dv_row[i];
+        const float dv = piv ? (float)(1.0 / piv[r]) : (dm >= 0 ? src[dm] : 1.0f);
+        ((float4 *)pkv)[i] = make_float4(v[0], v[1], v[2], dv);
+    }
+}
+
+template <>
+__global__ void bs_pack_kernel<uint16_t>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
+                                         const int *__restrict__ dv_row, const uint16_t *__restrict__ src,
+                                         const double *__restrict__ piv, int4 *__restrict__ pkv) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
+        unsigned v[3];
+        for (int k = 0; k < 3; k++) {
+            const int m = map3[3 * i + k];
+            v[k] = m >= 0 ? src[m] : 0u;
+        }
+        const int dm = dv_map[i], r = dv_row[i];
+        const float dv = piv ? (float)(1.0 / piv[r]) : (dm >= 0 ? __uint_as_float((unsigned)src[dm] << 16) : 1.0f);
+        pkv[i] = make_int4((int)(v[0] | (v[1] << 16)), (int)v[2], __float_as_int(dv), 0);
+    }
+}
+
 template <typename V>
 __global__ void bs_gather_kernel(long n, const int *__restrict__ map, const V *__restrict__ src, V *__restrict__ dst) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        int m = map[i];
+        const int m = map[i];
         dst[i] = (m >= 0) ? src[m] : V(0);
     }
 }
 
-__global__ void bs_gather_piv_kernel(long n, const int *__restrict__ rowmap, const double *__restrict__ piv,
-                                     double *__restrict__ dst) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        int r = rowmap[i];
-        dst[i] = (r >= 0) ? 1.0 / piv[r] : 1.0;   // FP64 reciprocal of the FP64 pivot
-    }
-}
-
 void BlockSolve::release() {
-    cudaFree(blk_chunk);
-    cudaFree(chunks);
-    cudaFree(recs);
-    cudaFree(codes);
-    cudaFree(vals);
-    cudaFree(dvals);
-    cudaFree(ticket);
-    cudaFree(ent_map);
+    cudaFree(blk);
+    cudaFree(desc);
+    cudaFree(pk0);
+    cudaFree(pkv);
+    cudaFree(ovf_codes);
+    cudaFree(ovf_vals);
+    cudaFree(map3);
     cudaFree(dv_map);
     cudaFree(dv_row);
+    cudaFree(ovf_map);
+    cudaFree(ticket);
     *this = BlockSolve();
 }
 
-// Host-side analysis: blocks, local levels, chunks and the packed arrays (structure only; the
-// values are gathered on the device through ent_map / dv_map).
+template <typename T>
+static int upload(T **dst, const std::vector<T> &src) {
+    HGB_CUDA(cudaMalloc(dst, sizeof(T) * std::max<size_t>(src.size(), 1)));
+    if (!src.empty()) HGB_CUDA(cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
+    return HGB_OK;
+}
+
+// Host-side analysis: blocks, local levels, steps and the packets (structure only; the values are
+// gathered on the device through map3 / dv_map / dv_row / ovf_map).
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
                    int rev, int R, BlockSolve &S) {
-    std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(n);
+    std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(std::max(n, 1));
     HGB_CUDA(cudaMemcpyAsync(pntr.data(), pntr_d, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(indx.data(), indx_d, sizeof(int) * nnz, cudaMemcpyDeviceToHost, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(diag.data(), diag_d, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (nnz > 0)
+        HGB_CUDA(cudaMemcpyAsync(indx.data(), indx_d, sizeof(int) * nnz, cudaMemcpyDeviceToHost, c->stream));
+    if (n > 0) HGB_CUDA(cudaMemcpyAsync(diag.data(), diag_d, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     HGB_CUDA(cudaStreamSynchronize(c->stream));
-    const int nblk = (n + R - 1) / R;
-    std::vector<int> blk_chunk(1, 0);
-    std::vector<int4> chunks;
-    std::vector<int4> recs;
-    std::vector<int> codes, ent_map, dv_map, dv_row;
-    std::vector<int> lev(R), cnt, order;
+    std::vector<int4> blk, desc, pk0;
+    std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map;
+    std::vector<int> lev(R), cnt, start, cur, order;
     auto row_of = [&](int pos) { return lower ? pos : n - 1 - pos; };
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
-    for (int b = 0; b < nblk; b++) {
-        const int p0 = b * R, p1 = std::min(n, p0 + R);
-        const int row_lo = lower ? p0 : n - p1;     // the block's rows are [row_lo, row_lo + p1 - p0)
-        int maxlev = 0;
-        for (int pos = p0; pos < p1; pos++) {
-            const int row = row_of(pos);
-            const int a = lower ? pntr[row] : diag[row] + 1;
-            const int e = lower ? diag[row] : pntr[row + 1];
-            if (e - a > kBsCapEnt) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row, e - a);
+    auto deps = [&](int row, int &a, int &e) {
+        a = lower ? pntr[row] : diag[row] + 1;
+        e = lower ? diag[row] : pntr[row + 1];
+    };
+    for (int p0 = 0; p0 < n;) {
+        // grow the block in solve order while it fits R rows and kBsStepCap steps
+        cnt.clear();
+        int steps = 0, p1 = p0;
+        while (p1 < n && p1 - p0 < R) {
+            int a, e;
+            deps(row_of(p1), a, e);
+            if (e - a > 0xFFFF) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row_of(p1), e - a);
             int lv = 0;
             for (int q = a; q < e; q++) {
                 const int pj = pos_of(indx[q]);
                 if (pj >= p0) lv = std::max(lv, lev[pj - p0] + 1);
             }
-            lev[pos - p0] = lv;
-            maxlev = std::max(maxlev, lv);
+            if ((int)cnt.size() <= lv) cnt.resize(lv + 1, 0);
+            const int add = (cnt[lv] % kBsThreads == 0) ? 1 : 0;
+            if (steps + add > kBsStepCap) break;
+            steps += add;
+            cnt[lv]++;
+            lev[p1 - p0] = lv;
+            p1++;
         }
-        cnt.assign(maxlev + 2, 0);
-        for (int pos = p0; pos < p1; pos++) cnt[lev[pos - p0] + 1]++;
-        for (int l = 0; l <= maxlev; l++) cnt[l + 1] += cnt[l];
-        order.assign(p1 - p0, 0);
-        {
-            std::vector<int> cur(cnt.begin(), cnt.end() - 1);
-            for (int pos = p0; pos < p1; pos++) order[cur[lev[pos - p0]]++] = pos;
-        }
-        for (int l = 0; l <= maxlev; l++) {
-            int k = cnt[l];
-            while (k < cnt[l + 1]) {
-                // one chunk: rows of level l while they fit the stage
-                const int rec0 = (int)recs.size(), ent0 = (int)codes.size();
-                int nr = 0, ne = 0;
-                while (k < cnt[l + 1] && nr < kBsCapRows) {
-                    const int pos = order[k];
-                    const int row = row_of(pos);
-                    const int a = lower ? pntr[row] : diag[row] + 1;
-                    const int e = lower ? diag[row] : pntr[row + 1];
-                    if (ne + (e - a) > kBsCapEnt) break;
-                    recs.push_back(make_int4(row, ne, e - a, row - row_lo));
-                    for (int q = 0; q < e - a; q++) {
+        const int rows = p1 - p0, row_lo = lower ? p0 : n - p1, nl = (int)cnt.size();
+        start.assign(nl + 1, 0);
+        for (int l = 0; l < nl; l++) start[l + 1] = start[l] + cnt[l];
+        cur.assign(start.begin(), start.end() - 1);
+        order.assign(rows, 0);
+        for (int pos = p0; pos < p1; pos++) order[cur[lev[pos - p0]]++] = pos;
+        const int s_first = (int)desc.size();
+        for (int l = 0; l < nl; l++) {
+            for (int k = start[l]; k < start[l + 1]; k += kBsThreads) {
+                const int nr = std::min(kBsThreads, start[l + 1] - k);
+                int kx = 0;
+                for (int i = 0; i < nr; i++) {
+                    int a, e;
+                    deps(row_of(order[k + i]), a, e);
+                    kx = std::max(kx, e - a - kBsInline);
+                }
+                const size_t ob = ovf_codes.size();
+                if (ob + (size_t)kx * nr > (size_t)INT_MAX || pk0.size() + nr > (size_t)INT_MAX)
+                    return fail(HGB_ERR_UNSUPPORTED, "block solve: packed arrays exceed 2^31 entries");
+                const int bar = (k + nr == start[l + 1]) ? 1 : 0;
+                desc.push_back(make_int4((int)pk0.size(), nr, (int)ob, kx | (bar << 16)));
+                ovf_codes.resize(ob + (size_t)kx * nr, 0);
+                ovf_map.resize(ob + (size_t)kx * nr, -1);
+                for (int i = 0; i < nr; i++) {
+                    const int row = row_of(order[k + i]);
+                    int a, e;
+                    deps(row, a, e);
+                    const int nd = e - a;
+                    int cd[kBsInline] = {0, 0, 0}, mp[kBsInline] = {-1, -1, -1};
+                    for (int q = 0; q < nd; q++) {
                         const int p = rev ? e - 1 - q : a + q;
-                        const int pj = pos_of(indx[p]);
-                        codes.push_back(pj >= p0 ? indx[p] - row_lo : -(indx[p] + 1));
-                        ent_map.push_back(p);
+                        const int col = indx[p];
+                        const int code = pos_of(col) >= p0 ? col - row_lo : -(col + 1);
+                        if (q < kBsInline) {
+                            cd[q] = code;
+                            mp[q] = p;
+                        } else {
+                            ovf_codes[ob + (size_t)(q - kBsInline) * nr + i] = code;
+                            ovf_map[ob + (size_t)(q - kBsInline) * nr + i] = p;
+                        }
                     }
+                    pk0.push_back(make_int4(cd[0], cd[1], cd[2], (int)((unsigned)(row - row_lo) | ((unsigned)nd << 16))));
+                    for (int q = 0; q < kBsInline; q++) map3.push_back(mp[q]);
                     dv_map.push_back(diag[row]);
                     dv_row.push_back(row);
-                    ne += e - a;
-                    nr++;
-                    k++;
                 }
-                // pad entries and diagonal values to 16-byte multiples for the bulk copies
-                while (codes.size() % 8) { codes.push_back(0); ent_map.push_back(-1); }
-                while (dv_map.size() % 8) { dv_map.push_back(-1); dv_row.push_back(-1); }
-                while (recs.size() % 8) recs.push_back(make_int4(0, 0, 0, 0));
-                chunks.push_back(make_int4(rec0, nr, ent0, (int)codes.size() - ent0));
             }
         }
-        blk_chunk.push_back((int)chunks.size());
+        blk.push_back(make_int4(s_first, (int)desc.size(), row_lo, rows));
+        p0 = p1;
     }
+    S.release();
     S.n = n;
-    S.lower = lower;
-    S.nblk = nblk;
+    S.nblk = (int)blk.size();
+    S.nsteps = (int)desc.size();
     S.R = R;
-    S.nchunks = (int)chunks.size();
-    S.nrec = (int)recs.size();
-    S.nent = (int)codes.size();
-    HGB_CUDA(cudaMalloc(&S.blk_chunk, sizeof(int) * blk_chunk.size()));
-    HGB_CUDA(cudaMalloc(&S.chunks, sizeof(int4) * chunks.size()));
-    HGB_CUDA(cudaMalloc(&S.recs, sizeof(int4) * recs.size()));
-    HGB_CUDA(cudaMalloc(&S.codes, sizeof(int) * std::max<size_t>(codes.size(), 8)));
-    HGB_CUDA(cudaMalloc(&S.ent_map, sizeof(int) * std::max<size_t>(ent_map.size(), 8)));
-    HGB_CUDA(cudaMalloc(&S.dv_map, sizeof(int) * dv_map.size()));
-    HGB_CUDA(cudaMalloc(&S.dv_row, sizeof(int) * dv_row.size()));
+    S.npk = (long)pk0.size();
+    S.novf = (long)ovf_codes.size();
+    HGB_TRY(upload(&S.blk, blk));
+    HGB_TRY(upload(&S.desc, desc));
+    HGB_TRY(upload(&S.pk0, pk0));
+    HGB_TRY(upload(&S.map3, map3));
+    HGB_TRY(upload(&S.dv_map, dv_map));
+    HGB_TRY(upload(&S.dv_row, dv_row));
+    HGB_TRY(upload(&S.ovf_codes, ovf_codes));
+    HGB_TRY(upload(&S.ovf_map, ovf_map));
     HGB_CUDA(cudaMalloc(&S.ticket, sizeof(int) * 2));
-    HGB_CUDA(cudaMemcpy(S.blk_chunk, blk_chunk.data(), sizeof(int) * blk_chunk.size(), cudaMemcpyHostToDevice));
-    HGB_CUDA(cudaMemcpy(S.chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice));
-    HGB_CUDA(cudaMemcpy(S.recs, recs.data(), sizeof(int4) * recs.size(), cudaMemcpyHostToDevice));
-    if (!codes.empty()) {
-        HGB_CUDA(cudaMemcpy(S.codes, codes.data(), sizeof(int) * codes.size(), cudaMemcpyHostToDevice));
-        HGB_CUDA(cudaMemcpy(S.ent_map, ent_map.data(), sizeof(int) * ent_map.size(), cudaMemcpyHostToDevice));
-    }
-    HGB_CUDA(cudaMemcpy(S.dv_map, dv_map.data(), sizeof(int) * dv_map.size(), cudaMemcpyHostToDevice));
-    HGB_CUDA(cudaMemcpy(S.dv_row, dv_row.data(), sizeof(int) * dv_row.size(), cudaMemcpyHostToDevice));
     HGB_CUDA(cudaMemset(S.ticket, 0, sizeof(int) * 2));
     return HGB_OK;
 }
 
-// Gather the values (store precision vsize) and diagonal values (or FP64 pivots) into packed order.
+// Gather the values (store precision vsize) and the diagonal terms into the packets.  With piv
+// (FP64 pivots of a lower-precision store) the packets carry the pivots' reciprocals.
 int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, const double *piv) {
-    cudaFree(S.vals);
-    cudaFree(S.dvals);
-    S.vals = S.dvals = nullptr;
+    cudaFree(S.pkv);
+    cudaFree(S.ovf_vals);
+    S.pkv = nullptr;
+    S.ovf_vals = nullptr;
     S.vsize = vsize;
-    S.dv_double = piv != nullptr;
-    HGB_CUDA(cudaMalloc(&S.vals, (size_t)vsize * std::max(S.nent, 8)));
-    HGB_CUDA(cudaMalloc(&S.dvals, (size_t)(piv ? 8 : vsize) * std::max(S.nrec, 8)));
-    int g = std::max(1, std::min((S.nent + 255) / 256, c->num_sms * 8));
-    int gr = std::max(1, std::min((S.nrec + 255) / 256, c->num_sms * 8));
+    S.dv_recip = (piv != nullptr && vsize != 8) ? 1 : 0;
+    HGB_CUDA(cudaMalloc(&S.pkv, sizeof(int4) * (size_t)bs_nv(vsize) * std::max<long>(S.npk, 1)));
+    HGB_CUDA(cudaMalloc(&S.ovf_vals, (size_t)vsize * std::max<long>(S.novf, 1)));
+    const int g = (int)std::max<long>(1, std::min<long>((S.npk + 255) / 256, c->num_sms * 8));
+    const int go = (int)std::max<long>(1, std::min<long>((S.novf + 255) / 256, c->num_sms * 8));
     if (vsize == 8) {
-        bs_gather_kernel<double><<<g, 256, 0, c->stream>>>(S.nent, S.ent_map, (const double *)svals, (double *)S.vals);
-        bs_gather_kernel<double><<<gr, 256, 0, c->stream>>>(S.nrec, S.dv_map, (const double *)svals, (double *)S.dvals);
+        bs_pack_kernel<double><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const double *)svals, piv, S.pkv);
+        if (S.novf) bs_gather_kernel<double><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const double *)svals, (double *)S.ovf_vals);
     } else if (vsize == 4) {
-        bs_gather_kernel<float><<<g, 256, 0, c->stream>>>(S.nent, S.ent_map, (const float *)svals, (float *)S.vals);
-        if (!piv) bs_gather_kernel<float><<<gr, 256, 0, c->stream>>>(S.nrec, S.dv_map, (const float *)svals, (float *)S.dvals);
+        bs_pack_kernel<float><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const float *)svals, piv, S.pkv);
+        if (S.novf) bs_gather_kernel<float><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const float *)svals, (float *)S.ovf_vals);
     } else {
-        bs_gather_kernel<uint16_t><<<g, 256, 0, c->stream>>>(S.nent, S.ent_map, (const uint16_t *)svals, (uint16_t *)S.vals);
-        if (!piv) bs_gather_kernel<uint16_t><<<gr, 256, 0, c->stream>>>(S.nrec, S.dv_map, (const uint16_t *)svals, (uint16_t *)S.dvals);
+        bs_pack_kernel<uint16_t><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const uint16_t *)svals, piv, S.pkv);
+        if (S.novf)
+            bs_gather_kernel<uint16_t><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const uint16_t *)svals, (uint16_t *)S.ovf_vals);
     }
-    if (piv) bs_gather_piv_kernel<<<gr, 256, 0, c->stream>>>(S.nrec, S.dv_row, piv, (double *)S.dvals);
     return launch_check("bsolve_load_values");
 }
 
@@ -421,32 +487,32 @@ template <typename V, typename X>
 int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend_a,
                   X *pend_b, const int *skip) {
     if (S.n == 0) return HGB_OK;
+    if (S.vsize != (int)sizeof(V) || !S.pkv) return fail(HGB_ERR_ARG, "bsolve: values not loaded for this store");
     BsArgs A;
     A.nblk = S.nblk;
-    A.blk_chunk = S.blk_chunk;
-    A.chunks = S.chunks;
-    A.recs = S.recs;
-    A.codes = S.codes;
-    A.vals = S.vals;
-    A.dvals = S.dvals;
-    A.dv_double = S.dv_double;
-    A.R = S.R;
-    A.n = S.n;
-    A.lower = S.lower;
+    A.blk = S.blk;
+    A.desc = S.desc;
+    A.pk0 = S.pk0;
+    A.pkv = S.pkv;
+    A.npk = S.npk;
+    A.ovf_codes = S.ovf_codes;
+    A.ovf_vals = S.ovf_vals;
     A.mode = mode;
     A.unit = unit;
+    A.recip = S.dv_recip;
     A.ticket = S.ticket;
     A.err = c->err;
     A.skip = skip;
-    const size_t dvb = S.dv_double ? sizeof(double) : sizeof(V);
-    const size_t smem = (size_t)S.R * sizeof(X) + kBsStages * bs_stage_bytes<V, X>(dvb);
-    static bool attr[2][3] = {};
-    const int xi = sizeof(X) == 8 ? 0 : 1, vi = sizeof(V) == 8 ? 0 : (sizeof(V) == 4 ? 1 : 2);
-    if (!attr[xi][vi]) {
-        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr[xi][vi] = true;
+    const size_t smem = bs_smem_bytes<V, X>(S.R);
+    static int attr_dev[3] = {-1, -1, -1};   // device on which the attribute was set, per store type
+    const int vi = sizeof(V) == 8 ? 0 : (sizeof(V) == 4 ? 1 : 2);
+    if (attr_dev[vi] != c->device) {
+        int mx = 0;
+        HGB_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        if (smem > (size_t)mx) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem, mx);
+        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_dev[vi] = c->device;
     }
-    if (smem > 220 * 1024) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory", smem);
     const int grid = std::max(1, std::min(S.nblk, c->num_sms));
     bsolve_kernel<V, X><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend_a, pend_b);
     return launch_check("bsolve_kernel");

@@ -6,15 +6,16 @@
 namespace hgb {
 
 struct BlockSolve {
-    int n = 0, lower = 1, nblk = 0, nchunks = 0, nrec = 0, nent = 0, R = 0;
-    int vsize = 0, dv_double = 0;
-    int *blk_chunk = nullptr;   // [nblk+1]
-    int4 *chunks = nullptr;     // [nchunks] {rec_off, nrows, ent_off, nent}
-    int4 *recs = nullptr;       // [nrec] {row, entry offset in chunk, ndeps, smem slot}
-    int *codes = nullptr;       // [nent]
-    void *vals = nullptr;       // [nent] store precision
-    void *dvals = nullptr;      // [nrec] store precision or FP64 pivots
-    int *ent_map = nullptr, *dv_map = nullptr, *dv_row = nullptr;   // value gather maps
+    int n = 0, nblk = 0, nsteps = 0, R = 0;
+    long npk = 0, novf = 0;
+    int vsize = 0, dv_recip = 0;
+    int4 *blk = nullptr;        // [nblk] {first step, end step, row_lo, rows}
+    int4 *desc = nullptr;       // [nsteps] {first packet, rows, first overflow entry, overflow width | barrier << 16}
+    int4 *pk0 = nullptr;        // [npk] {code0, code1, code2, slot | ndeps << 16}
+    int4 *pkv = nullptr;        // [NV * npk] value pieces (store precision, diagonal terms)
+    int *ovf_codes = nullptr;   // [novf] dependencies beyond the third, column-major per step
+    void *ovf_vals = nullptr;
+    int *map3 = nullptr, *dv_map = nullptr, *dv_row = nullptr, *ovf_map = nullptr;   // value gather maps
     int *ticket = nullptr;
     void release();
 };

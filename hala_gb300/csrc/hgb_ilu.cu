@@ -323,7 +323,8 @@ __device__ __forceinline__ void wait_values(const X *out, const int (&jj)[8], X 
         }
     int spins = 0;
     while (pending) {
-        if (++spins > kSpinLimit) {
+        ++spins;
+        if (spins > kSpinLimit || ((spins & 4095) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT))) {
             atomicOr(err, DEV_ERR_TIMEOUT);
 #pragma unroll
             for (int k = 0; k < 8; k++)

@@ -173,13 +173,16 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 constexpr int kSpinLimit = 1 << 22;
 
 // Wait until *p no longer holds the pending pattern; bounded.  On timeout the error word gets
-// DEV_ERR_TIMEOUT and NaN is returned so that dependents terminate too.
+// DEV_ERR_TIMEOUT and NaN is returned so that dependents terminate too.  A wait also gives up as
+// soon as another wait has timed out (checked every 4096 polls), so a launch whose inputs can
+// never arrive ends after one poll budget instead of one budget per waiting row.
 template <typename T>
 __device__ __forceinline__ T wait_value(const T *p, int *err, int limit = kSpinLimit) {
     T v = ld_relaxed(p);
     int spins = 0;
     while (Pending<T>::is(v)) {
-        if (++spins > limit) {
+        ++spins;
+        if (spins > limit || ((spins & 4095) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT))) {
             atomicOr(err, DEV_ERR_TIMEOUT);
             return Pending<T>::canon(Pending<T>::value());
         }

@@ -198,6 +198,22 @@ def csr_matvec(pntr, indx, vals, x):
     return out
 
 
+def random_csr_sparse(n, per_row, rng):
+    """Random square pattern with about per_row uniformly placed entries per row plus the diagonal
+    (sorted columns, diagonally dominant), built without a dense mask."""
+    rows = np.repeat(np.arange(n, dtype=np.int64), per_row)
+    cols = rng.integers(0, n, size=n * per_row)
+    key = np.unique(np.concatenate([rows * n + cols, np.arange(n, dtype=np.int64) * (n + 1)]))
+    r, c = key // n, key % n
+    v = rng.uniform(-1, 1, size=len(r))
+    rowsum = np.bincount(r, np.abs(v), n)
+    d = r == c
+    v[d] = rowsum[r[d]] + 1.0
+    pntr = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(r, minlength=n), out=pntr[1:])
+    return pntr.astype(np.int32), c.astype(np.int32), v
+
+
 def random_csr(n, density, rng, with_diag=True, dominant=True, ncols=None):
     """Random sparse matrix with sorted columns; optional full diagonal (diagonally dominant)."""
     ncols = n if ncols is None else ncols

@@ -141,15 +141,21 @@ static double dnorm(int n, const double *x) {
     return sqrt(s);
 }
 
-/* FP32 ILU(0) apply with FP64 pivots: off-diagonal updates in float, x_i / u_ii in double */
+/* FP32 ILU(0) apply with FP64 pivots: off-diagonal updates in float; x_i times the pivot's
+ * reciprocal, formed in double and rounded to float once. */
 static void ilu_apply_mixed(int n, const int *pntr, const int *indx, const int *diag,
                             const float *ilu32, const double *piv, float *x) {
     for (int i = 1; i < n; i++)
         for (int j = pntr[i]; j < diag[i]; j++) x[i] -= ilu32[j] * x[indx[j]];
     for (int i = n - 1; i >= 0; i--) {
         for (int j = diag[i] + 1; j < pntr[i + 1]; j++) x[i] -= ilu32[j] * x[indx[j]];
-        x[i] = (float)((double)x[i] / piv[i]);
+        x[i] = x[i] * (float)(1.0 / piv[i]);
     }
+}
+
+void or_ilu_apply_mixed(int n, const int *pntr, const int *indx, const int *diag, const float *ilu32,
+                        const double *piv, float *x) {
+    ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, x);
 }
 
 /* Iterative refinement (outer FP64, inner FP32 ILU(0)-PCG following solve_cg_core's order;

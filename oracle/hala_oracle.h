@@ -83,6 +83,12 @@ OR_DECLARE(float, f)
  * inner ILU(0)-PCG in FP32 on (vals32, ilu32 with FP64 pivots piv) to relative tolerance
  * inner_rtol, x += d in FP64.  Stops when ||b - A x|| < tol.  Returns total inner iterations;
  * *outer_out gets the outer count. */
+/* FP32 ILU(0) apply of an FP32 factor with FP64 pivots (the inner preconditioner of
+ * or_ir_pcg): off-diagonal updates in float in the order of apply_ilu_array, then x_i times
+ * (float)(1.0 / piv_i). */
+void or_ilu_apply_mixed(int n, const int *pntr, const int *indx, const int *diag, const float *ilu32,
+                        const double *piv, float *x);
+
 int or_ir_pcg(int n, const int *pntr, const int *indx, const double *vals, const float *vals32,
               const int *diag, const float *ilu32, const double *piv, const double *b, double *x,
               double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out);

@@ -39,6 +39,7 @@ def _load():
     lib.or_levels.argtypes = [i, _i32p, _i32p, _i32p, c, _i32p]
     lib.or_levels.restype = i
     lib.or_ilu_factor_pivot_d.argtypes = [i, _i32p, _i32p, _i32p, _f64p]
+    lib.or_ilu_apply_mixed.argtypes = [i, _i32p, _i32p, _i32p, _f32p, _f64p, _f32p]
     lib.or_spmv_bf16f32.argtypes = [c, i, i, C.c_float, _i32p, _i32p, _u16p, _f32p, C.c_float, _f32p]
     for s, fp, ft in (("d", _f64p, C.c_double), ("f", _f32p, C.c_float)):
         getattr(lib, f"or_spmv_{s}").argtypes = [c, i, i, ft, _i32p, _i32p, fp, fp, ft, fp]
@@ -162,6 +163,14 @@ def ilu_apply(pntr, indx, diag, ilu, x, trans="N"):
     y = np.array(x, ilu.dtype, copy=True)
     fn = "or_ilu_apply_" if trans in ("N", "n") else "or_ilu_apply_t_"
     getattr(lib(), fn + _sfx(ilu.dtype))(n, pntr, indx, diag, ilu, y)
+    return y
+
+
+def ilu_apply_mixed(pntr, indx, diag, ilu32, piv, x):
+    """FP32 factor with FP64 pivots (the inner preconditioner of ir_pcg)."""
+    y = np.array(x, np.float32, copy=True)
+    lib().or_ilu_apply_mixed(len(pntr) - 1, pntr, indx, diag, np.ascontiguousarray(ilu32, np.float32),
+                             np.ascontiguousarray(piv, np.float64), y)
     return y
 
 
