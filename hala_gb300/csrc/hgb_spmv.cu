@@ -199,10 +199,101 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
     if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
 }
 
+// Warp-tiled SpMV: each warp takes 32 consecutive rows, copies the tile's whole vals / indx range
+// into its own shared-memory buffer with 16-byte cp.async (coalesced, no cross-warp handshake),
+// then every lane sums its row from shared memory, gathering x from global memory kGW entries at
+// a time.  Tiles with more than kWarpCap entries read their rows directly.
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+constexpr int kWarpCap = 256;
+constexpr int kWarpBlock = 256;   // 8 warps per CTA
+constexpr int kGW = 4;            // x gathers in flight per lane
+
+template <typename V, bool FUSE_DOT>
+__global__ void __launch_bounds__(kWarpBlock)
+spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
+                 typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, typename Val<V>::X beta,
+                 typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter, double *dot_out,
+                 const int *skip) {
+    using X = typename Val<V>::X;
+    constexpr int EV = 16 / (int)sizeof(V);   // values per 16-byte unit
+    if (skip && *skip) return;
+    __shared__ __align__(16) V s_vals[kWarpBlock / 32][kWarpCap + 2 * EV];
+    __shared__ __align__(16) int s_idx[kWarpBlock / 32][kWarpCap + 8];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nnz = __ldg(pntr + n_rows);
+    const long nwarps = (long)gridDim.x * (kWarpBlock / 32);
+    V *sv = s_vals[wib];
+    int *si = s_idx[wib];
+    double dsum[1] = {0.0};
+    for (long tile = (long)blockIdx.x * (kWarpBlock / 32) + wib; tile * 32 < n_rows; tile += nwarps) {
+        const int r0 = (int)(tile * 32), row = r0 + lane;
+        const int nr = min(32, n_rows - r0);
+        const int ps = __ldg(pntr + min(row, n_rows)), pe = __ldg(pntr + min(row + 1, n_rows));
+        const int base = __shfl_sync(0xffffffffu, ps, 0);
+        const int end = __shfl_sync(0xffffffffu, pe, nr - 1);
+        X acc = X(0);
+        if (end - base <= kWarpCap) {
+            const int av = base & ~(EV - 1), ai = base & ~3;
+            for (int g = av + lane * EV; g < end; g += 32 * EV) {
+                if (g + EV <= nnz) cp_async16(sv + (g - av), vals + g);
+                else
+                    for (int k = 0; k < EV && g + k < end; k++) sv[g - av + k] = vals[g + k];
+            }
+            for (int g = ai + lane * 4; g < end; g += 32 * 4) {
+                if (g + 4 <= nnz) cp_async16(si + (g - ai), indx + g);
+                else
+                    for (int k = 0; k < 4 && g + k < end; k++) si[g - ai + k] = indx[g + k];
+            }
+            cp_async_commit();
+            cp_async_wait<0>();
+            __syncwarp();
+            if (row < n_rows) {
+                for (int j0 = ps; j0 < pe; j0 += kGW) {
+                    X xv[kGW], vv[kGW];
+#pragma unroll
+                    for (int k = 0; k < kGW; k++)
+                        if (j0 + k < pe) {
+                            vv[k] = Val<V>::get(sv[j0 + k - av]);
+                            xv[k] = __ldg(x + si[j0 + k - ai]);
+                        }
+#pragma unroll
+                    for (int k = 0; k < kGW; k++)
+                        if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+                }
+            }
+            __syncwarp();   // the buffers are refilled by the next tile
+        } else if (row < n_rows) {
+            for (int j0 = ps; j0 < pe; j0 += kGW) {
+                X xv[kGW], vv[kGW];
+#pragma unroll
+                for (int k = 0; k < kGW; k++)
+                    if (j0 + k < pe) {
+                        vv[k] = Val<V>::get(__ldg(vals + j0 + k));
+                        xv[k] = __ldg(x + __ldg(indx + j0 + k));
+                    }
+#pragma unroll
+                for (int k = 0; k < kGW; k++)
+                    if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+            }
+        }
+        if (row < n_rows) {
+            const X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[row]));
+            y[row] = out;
+            if (FUSE_DOT) dsum[0] += (double)__ldg(x + row) * (double)out;
+        }
+    }
+    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+}
+
+// SpMV variant: warp-tiled (default), "direct" (thread per row, no staging) or "tma" (CTA-wide
+// bulk-copy ring), selected by HGB_SPMV for comparisons
 static int spmv_variant() {
     static int v = [] {
         const char *e = getenv("HGB_SPMV");
-        return (e && std::string(e) == "direct") ? 1 : 0;
+        if (e && std::string(e) == "direct") return 1;
+        if (e && std::string(e) == "tma") return 2;
+        return 0;
     }();
     return v;
 }
@@ -391,14 +482,33 @@ void Transpose::release() {
     pntr = row = map = nullptr;
 }
 
-static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 template <typename V>
 int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
                   typename Val<V>::X *y, double *dot_out, const int *skip) {
     if (n_rows <= 0) return HGB_OK;
-    if (spmv_variant() == 1) {
+    const int variant = spmv_variant();
+    if (variant == 0 && aligned16(vals) && aligned16(indx)) {
+        // persistent grid: the resident CTAs of every SM (occupancy queried once per kernel)
+        static int occ[2] = {0, 0};
+        int &o = occ[dot_out ? 1 : 0];
+        if (!o) {
+            if (dot_out) HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmv_warp_kernel<V, true>, kWarpBlock, 0));
+            else HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmv_warp_kernel<V, false>, kWarpBlock, 0));
+            o = std::max(o, 1);
+        }
+        const long tiles = ((long)n_rows + 31) / 32;
+        const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, std::min(c->num_sms * o, kMaxReduceBlocks)));
+        if (dot_out)
+            spmv_warp_kernel<V, true><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
+                                                                     c->partials, c->counter, dot_out, skip);
+        else
+            spmv_warp_kernel<V, false><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
+                                                                      nullptr, nullptr, nullptr, skip);
+        return launch_check("spmv_warp_kernel");
+    }
+    if (variant != 2) {
         int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
         if (dot_out)
             spmv_direct_kernel<V, true><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, c->partials,
