@@ -30,7 +30,7 @@
 namespace hgb {
 
 constexpr int kBsThreads = 128;   // one row per thread per step
-constexpr int kBsStepCap = 512;   // steps per block: the block's descriptors sit in shared memory
+constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
 // value pieces per packet (NV), ring depth in steps (D), look-ahead of the remote loads (H)

@@ -44,8 +44,12 @@ def test_forward_solve_accuracy(setup):
     vals = H.assemble(st, theta).detach()
     u, _ = solver.solve(vals, f)
     p, i = st.pntr, st.indx
-    r = f.cpu().numpy() - P.csr_matvec(p, i, vals.cpu().numpy(), u.cpu().numpy())
-    assert np.linalg.norm(r) <= 3e-11 * np.linalg.norm(f.cpu().numpy()) * 1.5
+    vn, un = vals.cpu().numpy(), u.cpu().numpy()
+    r = f.cpu().numpy() - P.csr_matvec(p, i, vn, un)
+    # the solver stops on its own FP64 residual; recomputing it here adds rounding of the order
+    # eps * || |A| |u| ||
+    floor = np.finfo(np.float64).eps * np.linalg.norm(P.csr_matvec(p, i, np.abs(vn), np.abs(un)))
+    assert np.linalg.norm(r) <= 3e-11 * np.linalg.norm(f.cpu().numpy()) + 4 * floor
 
 
 def test_gradient_vs_central_differences(setup_fd):
