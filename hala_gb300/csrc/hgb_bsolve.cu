@@ -33,11 +33,20 @@ constexpr int kBsThreads = 128;   // one row per thread per step
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
-// value pieces per packet (NV), ring depth in steps (D), look-ahead of the remote loads (H)
+// value pieces per packet (NV), ring depth in steps (D, a power of two), look-ahead of the
+// remote loads in steps (H)
 template <typename V> struct BsCfg;
-template <> struct BsCfg<double> { static constexpr int NV = 3, D = 10, H = 4; };
-template <> struct BsCfg<float> { static constexpr int NV = 1, D = 18, H = 6; };
-template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 18, H = 6; };
+template <> struct BsCfg<double> { static constexpr int NV = 3, D = 8, H = 2; };
+template <> struct BsCfg<float> { static constexpr int NV = 1, D = 16, H = 2; };
+template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 16, H = 2; };
+
+// the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
+// dependencies (kBsIdle: no row for this thread in this step), bit 31 set on the last step of a
+// level (a barrier follows)
+constexpr int kBsIdle = 0xFFFF;
+__host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
+    return (int)((unsigned)slot | ((unsigned)nd << 15) | ((unsigned)bar << 31));
+}
 
 inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
 
@@ -88,11 +97,12 @@ template <> struct BsRow<uint16_t> {
 // a / d correctly rounded, from the stored y = RN(1/d): q0 = RN(a y), r = a - d q0 (exact with
 // FMA), q = RN(q0 + r y) equals RN(a / d) (Markstein, IBM J. Res. Dev. 34(1), 1990) when no step
 // overflows or underflows.  Operands with |exponent| >= 500, zeros, infinities and NaNs take the
-// division instead.
+// division instead; for such a d the packet stores y = 0.  The guards are integer tests (the FP64
+// pipe of sm_103 is slow).
+__host__ __device__ constexpr bool bs_markstein_range(unsigned biased_exp) { return biased_exp - 523u < 1000u; }
 __device__ __forceinline__ double bs_divide(double a, const BsRow<double> &r, int) {
     const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
-    const unsigned ed = ((unsigned)__double2hiint(r.d) >> 20) & 0x7FFu;
-    if (ea - 523u < 1000u && ed - 523u < 1000u) {
+    if (bs_markstein_range(ea) && __double_as_longlong(r.dinv) != 0) {
         const double q0 = __dmul_rn(a, r.dinv);
         const double rem = __fma_rn(-r.d, q0, a);
         return __fma_rn(rem, r.dinv, q0);
@@ -121,9 +131,9 @@ struct BsArgs {
 
 template <typename V, typename X>
 __global__ void __launch_bounds__(kBsThreads, 1)
-bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
+bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, H = BsCfg<V>::H, NP = 1 + NV;
-    static_assert(H >= 1 && D - 1 - H >= 1, "ring too shallow for the look-ahead");
+    static_assert((D & (D - 1)) == 0 && H >= 1 && D - 1 - H >= 1, "ring shape");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
@@ -131,6 +141,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
     X *xsbuf = (X *)(sdesc + kBsStepCap);               // [R + 16 / sizeof(X)]
     __shared__ int blk_sh;
     const int t = threadIdx.x;
+    int4 *myring = ring + t;                            // this thread's piece 0 of ring slot 0
     for (;;) {
         __syncthreads();   // every thread is done with the previous block
         if (t == 0) blk_sh = atomicAdd(A.ticket, 1);
@@ -154,78 +165,87 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
         cp_async_commit();
         cp_async_wait<0>();
         __syncthreads();
+        X *outb = out + row_lo;
+        X *pendb = pend ? pend + row_lo : nullptr;
 
-        // thread t's packet of step s into ring slot s % D (an empty group past the last step)
+        // thread t's packet of step s into its ring slot s % D (an empty group past the last step);
+        // without a row in step s it writes an idle word that carries the step's barrier flag
         auto issue = [&](int s) {
             if (s < ns) {
                 const int4 d = sdesc[s];
+                int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
                 if (t < d.y) {
-                    int4 *slot = ring + (s % D) * NP * kBsThreads + t;
                     cp_async16(slot, A.pk0 + d.x + t);
 #pragma unroll
                     for (int p = 0; p < NV; p++)
                         cp_async16(slot + (1 + p) * kBsThreads, A.pkv + (long)p * A.npk + d.x + t);
+                } else {
+                    slot->w = bs_word(0, kBsIdle, (d.w >> 16) & 1);
                 }
             }
             cp_async_commit();
         };
-        // load the first remote dependency of thread t's row of step s (landed in the ring)
+        // start the load of the first remote dependency of thread t's row of step s (landed)
         auto lookahead = [&](int s) -> X {
             X v = X(0);
             if (s < ns) {
-                const int4 d = sdesc[s];
-                if (t < d.y) {
-                    const int4 p0 = ring[(s % D) * NP * kBsThreads + t];
-                    const int nd = (int)((unsigned)p0.w >> 16);
+                const int4 p0 = myring[(s & (D - 1)) * (NP * kBsThreads)];
+                const int nd = (p0.w >> 15) & 0xFFFF;
+                if (nd != kBsIdle) {
                     const int j = (nd > 0 && p0.x < 0) ? p0.x : (nd > 1 && p0.y < 0) ? p0.y : (nd > 2 && p0.z < 0) ? p0.z : 0;
                     if (j < 0) v = ld_relaxed(out + (-j - 1));
                 }
             }
             return v;
         };
-        auto solve_row = [&](int s, X rv) {
-            const int4 d = sdesc[s];
-            if (t >= d.y) return;
-            const int4 *slot = ring + (s % D) * NP * kBsThreads + t;
+        auto step = [&](int s, X rv) {
+            const int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
             const int4 p0 = slot[0];
-            BsRow<V> rw;
-            rw.load(slot + kBsThreads);
-            const int sl = p0.w & 0xFFFF, nd = (int)((unsigned)p0.w >> 16);
-            const int code[kBsInline] = {p0.x, p0.y, p0.z};
-            const X xin = xs[sl];
-            X acc = (A.mode == 0) ? xin : X(0);
-            bool first = true;
+            const int w = p0.w, nd = (w >> 15) & 0xFFFF;
+            if (nd != kBsIdle) {
+                BsRow<V> rw;
+                rw.load(slot + kBsThreads);
+                const int sl = w & 0x7FFF;
+                const int code[kBsInline] = {p0.x, p0.y, p0.z};
+                const X xin = xs[sl];
+                // padded entries (k >= nd) contribute 0 * 0, which leaves the sum's bits unchanged
+                X xv[kBsInline], vv[kBsInline];
+                bool first = true;
 #pragma unroll
-            for (int k = 0; k < kBsInline; k++) {
-                if (k < nd) {
+                for (int k = 0; k < kBsInline; k++) {
+                    const bool live = k < nd;
                     const int cd = code[k];
-                    X xv;
-                    if (cd >= 0) {
-                        xv = xs[cd];
-                    } else {
-                        xv = first ? rv : Pending<X>::value();
+                    X xk = xs[max(cd, 0)];
+                    if (live && cd < 0) {
+                        xk = first ? rv : Pending<X>::value();
                         first = false;
-                        if (Pending<X>::is(xv)) xv = wait_value(out + (-cd - 1), A.err);
+                        if (Pending<X>::is(xk)) xk = wait_value(out + (-cd - 1), A.err);
                     }
-                    const X vk = (X)rw.v[k];
-                    acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xv)) : add_rn(acc, mul_rn(vk, xv));
+                    xv[k] = live ? xk : X(0);
+                    vv[k] = live ? (X)rw.v[k] : X(0);
                 }
+                X acc = (A.mode == 0) ? xin : X(0);
+#pragma unroll
+                for (int k = 0; k < kBsInline; k++)
+                    acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vv[k], xv[k])) : add_rn(acc, mul_rn(vv[k], xv[k]));
+                if (nd > kBsInline) {
+                    const int4 d = sdesc[s];
+                    for (int k = kBsInline; k < nd; k++) {
+                        const long e = (long)d.z + (long)(k - kBsInline) * d.y + t;
+                        const int cd = __ldg(A.ovf_codes + e);
+                        const X vk = Val<V>::get(__ldg((const V *)A.ovf_vals + e));
+                        const X xk = (cd >= 0) ? xs[cd] : wait_value(out + (-cd - 1), A.err);
+                        acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xk)) : add_rn(acc, mul_rn(vk, xk));
+                    }
+                }
+                if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
+                if (!A.unit) acc = bs_divide(acc, rw, A.recip);
+                acc = Pending<X>::canon(acc);
+                xs[sl] = acc;
+                st_relaxed(outb + sl, acc);
+                if (pendb) pendb[sl] = Pending<X>::value();
             }
-            for (int k = kBsInline; k < nd; k++) {
-                const long e = (long)d.z + (long)(k - kBsInline) * d.y + t;
-                const int cd = __ldg(A.ovf_codes + e);
-                const X vk = Val<V>::get(__ldg((const V *)A.ovf_vals + e));
-                const X xv = (cd >= 0) ? xs[cd] : wait_value(out + (-cd - 1), A.err);
-                acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xv)) : add_rn(acc, mul_rn(vk, xv));
-            }
-            if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
-            if (!A.unit) acc = bs_divide(acc, rw, A.recip);
-            acc = Pending<X>::canon(acc);
-            xs[sl] = acc;
-            const int row = row_lo + sl;
-            st_relaxed(out + row, acc);
-            if (pend_a) pend_a[row] = Pending<X>::value();
-            if (pend_b) pend_b[row] = Pending<X>::value();
+            if (w < 0) __syncthreads();   // last step of a level
         };
 
         // ring prologue: steps 0 .. D-2 in flight, the first H of them landed
@@ -241,9 +261,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend_a, X *pend_b) {
                 if (s < ns) {
                     issue(s + D - 1);
                     cp_async_wait<D - 1 - H>();   // steps <= s + H have landed
-                    solve_row(s, rv[u]);
+                    step(s, rv[u]);
                     rv[u] = lookahead(s + H);
-                    if (sdesc[s].w >> 16) __syncthreads();   // last step of a level
                 }
             }
         }
@@ -278,7 +297,8 @@ __global__ void bs_pack_kernel<double>(long npk, const int *__restrict__ map3, c
         const int dm = dv_map[i], r = dv_row[i];
         const double d = piv ? piv[r] : (dm >= 0 ? src[dm] : 1.0);
         ((double2 *)pkv)[i] = make_double2(v[0], v[1]);
-        ((double2 *)(pkv + npk))[i] = make_double2(v[2], 1.0 / d);   // correctly rounded reciprocal
+        const bool fast = bs_markstein_range(((unsigned)__double2hiint(d) >> 20) & 0x7FFu);
+        ((double2 *)(pkv + npk))[i] = make_double2(v[2], fast ? 1.0 / d : 0.0);   // correctly rounded reciprocal
         ((double2 *)(pkv + 2 * npk))[i] = make_double2(d, 0.0);
     }
 }
@@ -371,7 +391,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         while (p1 < n && p1 - p0 < R) {
             int a, e;
             deps(row_of(p1), a, e);
-            if (e - a > 0xFFFF) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row_of(p1), e - a);
+            if (e - a >= kBsIdle) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row_of(p1), e - a);
             int lv = 0;
             for (int q = a; q < e; q++) {
                 const int pj = pos_of(indx[q]);
@@ -426,7 +446,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                             ovf_map[ob + (size_t)(q - kBsInline) * nr + i] = p;
                         }
                     }
-                    pk0.push_back(make_int4(cd[0], cd[1], cd[2], (int)((unsigned)(row - row_lo) | ((unsigned)nd << 16))));
+                    pk0.push_back(make_int4(cd[0], cd[1], cd[2], bs_word(row - row_lo, nd, bar)));
                     for (int q = 0; q < kBsInline; q++) map3.push_back(mp[q]);
                     dv_map.push_back(diag[row]);
                     dv_row.push_back(row);
@@ -484,9 +504,10 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
 }
 
 template <typename V, typename X>
-int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend_a,
-                  X *pend_b, const int *skip) {
+int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,
+                  const int *skip) {
     if (S.n == 0) return HGB_OK;
+    if (S.R > 32768) return fail(HGB_ERR_ARG, "bsolve: %d rows per block exceed the 15-bit slot", S.R);
     if (S.vsize != (int)sizeof(V) || !S.pkv) return fail(HGB_ERR_ARG, "bsolve: values not loaded for this store");
     BsArgs A;
     A.nblk = S.nblk;
@@ -514,15 +535,15 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
         attr_dev[vi] = c->device;
     }
     const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-    bsolve_kernel<V, X><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend_a, pend_b);
+    bsolve_kernel<V, X><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend);
     return launch_check("bsolve_kernel");
 }
 
 template int bsolve_launch<double, double>(hgb_ctx *, const BlockSolve &, int, int, double, const double *, double *,
-                                           double *, double *, const int *);
+                                           double *, const int *);
 template int bsolve_launch<float, float>(hgb_ctx *, const BlockSolve &, int, int, float, const float *, float *, float *,
-                                         float *, const int *);
+                                         const int *);
 template int bsolve_launch<uint16_t, float>(hgb_ctx *, const BlockSolve &, int, int, float, const float *, float *,
-                                            float *, float *, const int *);
+                                            float *, const int *);
 
 }  // namespace hgb

@@ -27,7 +27,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                    int rev, int R, BlockSolve &S);
 int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, const double *piv);
 template <typename V, typename X>
-int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend_a,
-                  X *pend_b, const int *skip);
+int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,
+                  const int *skip);
 
 }  // namespace hgb

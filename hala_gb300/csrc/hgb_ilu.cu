@@ -541,8 +541,8 @@ static int ilu_apply_n(hgb_ilu *M, const void *x, void *r, const int *skip) {
     }
     if (M->use_bs) {
         // forward: unit lower, tmp <- L^-1 x (r reset to pending); backward: r <- U^-1 tmp
-        HGB_TRY(bsolve_launch<V, X>(c, M->BL, MODE_ILU, 1, X(1), (const X *)x, tmp, (X *)r, nullptr, skip));
-        HGB_TRY(bsolve_launch<V, X>(c, M->BU, MODE_ILU, 0, X(1), tmp, (X *)r, tmp, nullptr, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BL, MODE_ILU, 1, X(1), (const X *)x, tmp, (X *)r, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BU, MODE_ILU, 0, X(1), tmp, (X *)r, tmp, skip));
         return HGB_OK;
     }
     SolveArgs A{};
@@ -608,8 +608,8 @@ static int ilu_apply_t(hgb_ilu *M, const void *x, void *r, const int *skip) {
         M->tmp_epoch = c->error_epoch;
     }
     if (M->use_bsT) {
-        HGB_TRY(bsolve_launch<V, X>(c, M->BLT, MODE_TRSV, 0, X(1), (const X *)x, tmp, (X *)r, nullptr, skip));
-        HGB_TRY(bsolve_launch<V, X>(c, M->BUT, MODE_TRSV, 1, X(1), tmp, (X *)r, tmp, nullptr, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BLT, MODE_TRSV, 0, X(1), (const X *)x, tmp, (X *)r, skip));
+        HGB_TRY(bsolve_launch<V, X>(c, M->BUT, MODE_TRSV, 1, X(1), tmp, (X *)r, tmp, skip));
         return HGB_OK;
     }
     SolveArgs A{};
