@@ -50,11 +50,11 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
 
 inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
 
-// shared memory: [ring D x (1 + NV) x 128 pieces | step descriptors | solution slice]
+// shared memory: [ring D x (1 + NV) x 128 pieces | step descriptors | solution slice + zero slot]
 template <typename V, typename X>
 constexpr size_t bs_smem_bytes(int R) {
     return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)kBsStepCap * 16 +
-           ((size_t)R + 16 / sizeof(X)) * sizeof(X);
+           ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
 }
 
 // One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
@@ -100,7 +100,8 @@ template <> struct BsRow<uint16_t> {
 // division instead; for such a d the packet stores y = 0.  The guards are integer tests (the FP64
 // pipe of sm_103 is slow).
 __host__ __device__ constexpr bool bs_markstein_range(unsigned biased_exp) { return biased_exp - 523u < 1000u; }
-__device__ __forceinline__ double bs_divide(double a, const BsRow<double> &r, int) {
+template <bool RECIP>
+__device__ __forceinline__ double bs_divide(double a, const BsRow<double> &r) {
     const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
     if (bs_markstein_range(ea) && __double_as_longlong(r.dinv) != 0) {
         const double q0 = __dmul_rn(a, r.dinv);
@@ -109,9 +110,9 @@ __device__ __forceinline__ double bs_divide(double a, const BsRow<double> &r, in
     }
     return __ddiv_rn(a, r.d);
 }
-template <typename V>
-__device__ __forceinline__ float bs_divide(float a, const BsRow<V> &r, int recip) {
-    return recip ? __fmul_rn(a, r.d) : __fdiv_rn(a, r.d);
+template <bool RECIP, typename V>
+__device__ __forceinline__ float bs_divide(float a, const BsRow<V> &r) {
+    return RECIP ? __fmul_rn(a, r.d) : __fdiv_rn(a, r.d);
 }
 
 struct BsArgs {
@@ -123,13 +124,34 @@ struct BsArgs {
     long npk;
     const int *ovf_codes;   // dependency k >= 3 of row t of a step: [first + (k - 3) * rows + t]
     const void *ovf_vals;
-    int mode, unit, recip;
+    int R;                  // rows per block; slot R of the solution slice holds 0 (padding code)
     int *ticket;
     int *err;
     const int *skip;
 };
 
-template <typename V, typename X>
+// Asynchronous-copy issue and the polling load without a compiler memory clobber: the ring slots
+// they write are read only after cp_async_wait, which keeps its clobber, so the compiler may
+// schedule the step's arithmetic around them.
+__device__ __forceinline__ void bs_copy16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src));
+}
+__device__ __forceinline__ void bs_commit() { asm volatile("cp.async.commit_group;"); }
+__device__ __forceinline__ double bs_poll(const double *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
+    return __longlong_as_double((long long)v);
+}
+__device__ __forceinline__ float bs_poll(const float *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return __uint_as_float(v);
+}
+
+// MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
+// MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
+// UNIT: no division; RECIP: multiply by the stored FP32 reciprocal instead of dividing.
+template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
 __global__ void __launch_bounds__(kBsThreads, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, H = BsCfg<V>::H, NP = 1 + NV;
@@ -138,7 +160,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
     int4 *sdesc = ring + D * NP * kBsThreads;           // [kBsStepCap]
-    X *xsbuf = (X *)(sdesc + kBsStepCap);               // [R + 16 / sizeof(X)]
+    X *xsbuf = (X *)(sdesc + kBsStepCap);               // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh;
     const int t = threadIdx.x;
     int4 *myring = ring + t;                            // this thread's piece 0 of ring slot 0
@@ -152,95 +174,93 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         const int ns = bi.y - bi.x, row_lo = bi.z, cnt = bi.w;
 
         // the block's step descriptors and its right-hand side slice, in one commit group
-        for (int i = t; i < ns; i += kBsThreads) cp_async16(sdesc + i, A.desc + bi.x + i);
+        for (int i = t; i < ns; i += kBsThreads) bs_copy16(sdesc + i, A.desc + bi.x + i);
         constexpr int E = 16 / (int)sizeof(X);
         const X *src = in + row_lo;
         const int mis = (int)(((size_t)src & 15) / sizeof(X));
         X *xs = xsbuf + mis;   // xs[i] and src[i] sit at the same offset modulo 16 bytes
         const int head = min(cnt, (E - mis) % E);
         const int body = (cnt - head) / E;
-        for (int i = t; i < body; i += kBsThreads) cp_async16(xs + head + i * E, src + head + i * E);
+        for (int i = t; i < body; i += kBsThreads) bs_copy16(xs + head + i * E, src + head + i * E);
         for (int i = head + body * E + t; i < cnt; i += kBsThreads) xs[i] = src[i];
         if (t < head) xs[t] = src[t];
-        cp_async_commit();
+        if (t == 0) xs[A.R] = X(0);
+        bs_commit();
         cp_async_wait<0>();
         __syncthreads();
         X *outb = out + row_lo;
         X *pendb = pend ? pend + row_lo : nullptr;
 
         // thread t's packet of step s into its ring slot s % D (an empty group past the last step);
-        // without a row in step s it writes an idle word that carries the step's barrier flag
+        // without a row in step s it writes an idle packet (zero-slot codes, the barrier flag)
         auto issue = [&](int s) {
             if (s < ns) {
                 const int4 d = sdesc[s];
                 int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
                 if (t < d.y) {
-                    cp_async16(slot, A.pk0 + d.x + t);
+                    bs_copy16(slot, A.pk0 + d.x + t);
 #pragma unroll
                     for (int p = 0; p < NV; p++)
-                        cp_async16(slot + (1 + p) * kBsThreads, A.pkv + (long)p * A.npk + d.x + t);
+                        bs_copy16(slot + (1 + p) * kBsThreads, A.pkv + (long)p * A.npk + d.x + t);
                 } else {
-                    slot->w = bs_word(0, kBsIdle, (d.w >> 16) & 1);
+                    *slot = make_int4(A.R, A.R, A.R, bs_word(0, kBsIdle, (d.w >> 16) & 1));
                 }
             }
-            cp_async_commit();
+            bs_commit();
         };
-        // start the load of the first remote dependency of thread t's row of step s (landed)
+        // start the load of the first remote dependency of thread t's row of step s (landed);
+        // padding and idle codes are >= 0
         auto lookahead = [&](int s) -> X {
             X v = X(0);
             if (s < ns) {
                 const int4 p0 = myring[(s & (D - 1)) * (NP * kBsThreads)];
-                const int nd = (p0.w >> 15) & 0xFFFF;
-                if (nd != kBsIdle) {
-                    const int j = (nd > 0 && p0.x < 0) ? p0.x : (nd > 1 && p0.y < 0) ? p0.y : (nd > 2 && p0.z < 0) ? p0.z : 0;
-                    if (j < 0) v = ld_relaxed(out + (-j - 1));
-                }
+                const int j = p0.x < 0 ? p0.x : (p0.y < 0 ? p0.y : p0.z);
+                if (j < 0) v = bs_poll(out + (-j - 1));
             }
             return v;
         };
         auto step = [&](int s, X rv) {
             const int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
             const int4 p0 = slot[0];
-            const int w = p0.w, nd = (w >> 15) & 0xFFFF;
-            if (nd != kBsIdle) {
-                BsRow<V> rw;
-                rw.load(slot + kBsThreads);
-                const int sl = w & 0x7FFF;
-                const int code[kBsInline] = {p0.x, p0.y, p0.z};
-                const X xin = xs[sl];
-                // padded entries (k >= nd) contribute 0 * 0, which leaves the sum's bits unchanged
-                X xv[kBsInline], vv[kBsInline];
+            const int w = p0.w, nd = (w >> 15) & 0xFFFF, sl = w & 0x7FFF;
+            BsRow<V> rw;
+            rw.load(slot + kBsThreads);
+            const int code[kBsInline] = {p0.x, p0.y, p0.z};
+            const X xin = xs[sl];
+            // padding entries read the zero slot and the zero value: 0 * 0 leaves the sum unchanged
+            X xv[kBsInline];
+#pragma unroll
+            for (int k = 0; k < kBsInline; k++) xv[k] = xs[max(code[k], 0)];
+            if ((code[0] | code[1] | code[2]) < 0) {
+                // dependencies on earlier blocks: the first one was loaded ahead, the others are polled
                 bool first = true;
 #pragma unroll
-                for (int k = 0; k < kBsInline; k++) {
-                    const bool live = k < nd;
-                    const int cd = code[k];
-                    X xk = xs[max(cd, 0)];
-                    if (live && cd < 0) {
-                        xk = first ? rv : Pending<X>::value();
-                        first = false;
-                        if (Pending<X>::is(xk)) xk = wait_value(out + (-cd - 1), A.err);
-                    }
-                    xv[k] = live ? xk : X(0);
-                    vv[k] = live ? (X)rw.v[k] : X(0);
-                }
-                X acc = (A.mode == 0) ? xin : X(0);
-#pragma unroll
                 for (int k = 0; k < kBsInline; k++)
-                    acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vv[k], xv[k])) : add_rn(acc, mul_rn(vv[k], xv[k]));
-                if (nd > kBsInline) {
-                    const int4 d = sdesc[s];
-                    for (int k = kBsInline; k < nd; k++) {
-                        const long e = (long)d.z + (long)(k - kBsInline) * d.y + t;
-                        const int cd = __ldg(A.ovf_codes + e);
-                        const X vk = Val<V>::get(__ldg((const V *)A.ovf_vals + e));
-                        const X xk = (cd >= 0) ? xs[cd] : wait_value(out + (-cd - 1), A.err);
-                        acc = (A.mode == 0) ? sub_rn(acc, mul_rn(vk, xk)) : add_rn(acc, mul_rn(vk, xk));
+                    if (code[k] < 0) {
+                        X xk = first ? rv : Pending<X>::value();
+                        first = false;
+                        if (Pending<X>::is(xk)) xk = wait_value(out + (-code[k] - 1), A.err);
+                        xv[k] = xk;
                     }
+            }
+            X acc = (MODE == 0) ? xin : X(0);
+#pragma unroll
+            for (int k = 0; k < kBsInline; k++)
+                acc = (MODE == 0) ? sub_rn(acc, mul_rn((X)rw.v[k], xv[k])) : add_rn(acc, mul_rn((X)rw.v[k], xv[k]));
+            if (nd > kBsInline && nd != kBsIdle) {
+                const int4 d = sdesc[s];
+                for (int k = kBsInline; k < nd; k++) {
+                    const long e = (long)d.z + (long)(k - kBsInline) * d.y + t;
+                    const int cd = __ldg(A.ovf_codes + e);
+                    const X vk = Val<V>::get(__ldg((const V *)A.ovf_vals + e));
+                    const X xk = (cd >= 0) ? xs[cd] : wait_value(out + (-cd - 1), A.err);
+                    acc = (MODE == 0) ? sub_rn(acc, mul_rn(vk, xk)) : add_rn(acc, mul_rn(vk, xk));
                 }
-                if (A.mode == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
-                if (!A.unit) acc = bs_divide(acc, rw, A.recip);
-                acc = Pending<X>::canon(acc);
+            }
+            if (MODE == 1) acc = sub_rn(mul_rn(alpha, xin), acc);
+            if (!UNIT) acc = bs_divide<RECIP>(acc, rw);
+            acc = Pending<X>::canon(acc);
+            if (nd != kBsIdle) {
                 xs[sl] = acc;
                 st_relaxed(outb + sl, acc);
                 if (pendb) pendb[sl] = Pending<X>::value();
@@ -433,7 +453,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     int a, e;
                     deps(row, a, e);
                     const int nd = e - a;
-                    int cd[kBsInline] = {0, 0, 0}, mp[kBsInline] = {-1, -1, -1};
+                    int cd[kBsInline] = {R, R, R}, mp[kBsInline] = {-1, -1, -1};   // padding: the zero slot
                     for (int q = 0; q < nd; q++) {
                         const int p = rev ? e - 1 - q : a + q;
                         const int col = indx[p];
@@ -503,6 +523,23 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
     return launch_check("bsolve_load_values");
 }
 
+template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
+static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
+    const size_t smem = bs_smem_bytes<V, X>(S.R);
+    static int attr_dev = -1;   // device on which the kernel's shared-memory attribute was set
+    if (attr_dev != c->device) {
+        int mx = 0;
+        HGB_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        if (smem > (size_t)mx) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem, mx);
+        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        attr_dev = c->device;
+    }
+    const int grid = std::max(1, std::min(S.nblk, c->num_sms));
+    bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend);
+    return launch_check("bsolve_kernel");
+}
+
 template <typename V, typename X>
 int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,
                   const int *skip) {
@@ -518,25 +555,19 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     A.npk = S.npk;
     A.ovf_codes = S.ovf_codes;
     A.ovf_vals = S.ovf_vals;
-    A.mode = mode;
-    A.unit = unit;
-    A.recip = S.dv_recip;
+    A.R = S.R;
     A.ticket = S.ticket;
     A.err = c->err;
     A.skip = skip;
-    const size_t smem = bs_smem_bytes<V, X>(S.R);
-    static int attr_dev[3] = {-1, -1, -1};   // device on which the attribute was set, per store type
-    const int vi = sizeof(V) == 8 ? 0 : (sizeof(V) == 4 ? 1 : 2);
-    if (attr_dev[vi] != c->device) {
-        int mx = 0;
-        HGB_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-        if (smem > (size_t)mx) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem, mx);
-        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_dev[vi] = c->device;
+    const bool recip = S.dv_recip && sizeof(V) != 8;
+    if (mode == 0) {
+        if (unit) return bs_launch_one<V, X, 0, true, false>(c, S, A, alpha, in, out, pend);
+        return recip ? bs_launch_one<V, X, 0, false, (sizeof(V) != 8)>(c, S, A, alpha, in, out, pend)
+                     : bs_launch_one<V, X, 0, false, false>(c, S, A, alpha, in, out, pend);
     }
-    const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-    bsolve_kernel<V, X><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend);
-    return launch_check("bsolve_kernel");
+    if (unit) return bs_launch_one<V, X, 1, true, false>(c, S, A, alpha, in, out, pend);
+    return recip ? bs_launch_one<V, X, 1, false, (sizeof(V) != 8)>(c, S, A, alpha, in, out, pend)
+                 : bs_launch_one<V, X, 1, false, false>(c, S, A, alpha, in, out, pend);
 }
 
 template int bsolve_launch<double, double>(hgb_ctx *, const BlockSolve &, int, int, double, const double *, double *,

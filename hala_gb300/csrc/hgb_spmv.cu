@@ -199,10 +199,12 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
     if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
 }
 
-// Warp-tiled SpMV: each warp takes 32 consecutive rows, copies the tile's whole vals / indx range
-// into its own shared-memory buffer with 16-byte cp.async (coalesced, no cross-warp handshake),
-// then every lane sums its row from shared memory, gathering x from global memory kGW entries at
-// a time.  Tiles with more than kWarpCap entries read their rows directly.
+// Warp-tiled SpMV: each warp owns a contiguous run of 32-row tiles.  For every tile it copies the
+// tile's whole vals / indx range into its own shared-memory buffer with 16-byte cp.async
+// (coalesced, no cross-warp handshake); every lane then sums its row from shared memory, gathering
+// x from global memory kGW entries at a time.  The warp double-buffers: the copy of tile k+1 and
+// the row pointers of tile k+2 are in flight while tile k is summed.  Tiles of more than kWarpCap
+// entries read their rows directly.
 static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 constexpr int kWarpCap = 256;
@@ -217,72 +219,108 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
                  const int *skip) {
     using X = typename Val<V>::X;
     constexpr int EV = 16 / (int)sizeof(V);   // values per 16-byte unit
+    constexpr int SV = kWarpCap + 2 * EV, SI = kWarpCap + 8;
     if (skip && *skip) return;
-    __shared__ __align__(16) V s_vals[kWarpBlock / 32][kWarpCap + 2 * EV];
-    __shared__ __align__(16) int s_idx[kWarpBlock / 32][kWarpCap + 8];
+    __shared__ __align__(16) V s_vals[kWarpBlock / 32][2][SV];
+    __shared__ __align__(16) int s_idx[kWarpBlock / 32][2][SI];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nnz = __ldg(pntr + n_rows);
+    const long ntiles = ((long)n_rows + 31) / 32;
     const long nwarps = (long)gridDim.x * (kWarpBlock / 32);
-    V *sv = s_vals[wib];
-    int *si = s_idx[wib];
+    const long per = (ntiles + nwarps - 1) / nwarps;
+    const long tb = ((long)blockIdx.x * (kWarpBlock / 32) + wib) * per;
+    const long te = min(ntiles, tb + per);
     double dsum[1] = {0.0};
-    for (long tile = (long)blockIdx.x * (kWarpBlock / 32) + wib; tile * 32 < n_rows; tile += nwarps) {
-        const int r0 = (int)(tile * 32), row = r0 + lane;
-        const int nr = min(32, n_rows - r0);
-        const int ps = __ldg(pntr + min(row, n_rows)), pe = __ldg(pntr + min(row + 1, n_rows));
-        const int base = __shfl_sync(0xffffffffu, ps, 0);
-        const int end = __shfl_sync(0xffffffffu, pe, nr - 1);
-        X acc = X(0);
+
+    // lane's row pointers of tile k (loads only; nothing waits on them yet)
+    auto load_ptrs = [&](long k, int &ps, int &pe) {
+        const int row = (int)(k * 32) + lane;
+        ps = __ldg(pntr + min(row, n_rows));
+        pe = __ldg(pntr + min(row + 1, n_rows));
+    };
+    // the tile's entry range, and its copy into buffer buf when it fits
+    auto start_tile = [&](long k, int ps, int pe, int buf, int &base, int &end) {
+        const int nr = min(32, n_rows - (int)(k * 32));
+        base = __shfl_sync(0xffffffffu, ps, 0);
+        end = __shfl_sync(0xffffffffu, pe, nr - 1);
         if (end - base <= kWarpCap) {
+            V *sv = s_vals[wib][buf];
+            int *si = s_idx[wib][buf];
             const int av = base & ~(EV - 1), ai = base & ~3;
             for (int g = av + lane * EV; g < end; g += 32 * EV) {
                 if (g + EV <= nnz) cp_async16(sv + (g - av), vals + g);
                 else
-                    for (int k = 0; k < EV && g + k < end; k++) sv[g - av + k] = vals[g + k];
+                    for (int q = 0; q < EV && g + q < end; q++) sv[g - av + q] = vals[g + q];
             }
             for (int g = ai + lane * 4; g < end; g += 32 * 4) {
                 if (g + 4 <= nnz) cp_async16(si + (g - ai), indx + g);
                 else
-                    for (int k = 0; k < 4 && g + k < end; k++) si[g - ai + k] = indx[g + k];
-            }
-            cp_async_commit();
-            cp_async_wait<0>();
-            __syncwarp();
-            if (row < n_rows) {
-                for (int j0 = ps; j0 < pe; j0 += kGW) {
-                    X xv[kGW], vv[kGW];
-#pragma unroll
-                    for (int k = 0; k < kGW; k++)
-                        if (j0 + k < pe) {
-                            vv[k] = Val<V>::get(sv[j0 + k - av]);
-                            xv[k] = __ldg(x + si[j0 + k - ai]);
-                        }
-#pragma unroll
-                    for (int k = 0; k < kGW; k++)
-                        if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
-                }
-            }
-            __syncwarp();   // the buffers are refilled by the next tile
-        } else if (row < n_rows) {
-            for (int j0 = ps; j0 < pe; j0 += kGW) {
-                X xv[kGW], vv[kGW];
-#pragma unroll
-                for (int k = 0; k < kGW; k++)
-                    if (j0 + k < pe) {
-                        vv[k] = Val<V>::get(__ldg(vals + j0 + k));
-                        xv[k] = __ldg(x + __ldg(indx + j0 + k));
-                    }
-#pragma unroll
-                for (int k = 0; k < kGW; k++)
-                    if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
+                    for (int q = 0; q < 4 && g + q < end; q++) si[g - ai + q] = indx[g + q];
             }
         }
-        if (row < n_rows) {
-            const X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[row]));
-            y[row] = out;
-            if (FUSE_DOT) dsum[0] += (double)__ldg(x + row) * (double)out;
+        cp_async_commit();
+    };
+
+    if (tb < te) {
+        int ps0, pe0, ps1 = 0, pe1 = 0, base0, end0;
+        load_ptrs(tb, ps0, pe0);
+        start_tile(tb, ps0, pe0, 0, base0, end0);
+        if (tb + 1 < te) load_ptrs(tb + 1, ps1, pe1);
+        for (long k = tb; k < te; k++) {
+            const int buf = (int)((k - tb) & 1);
+            int base1 = 0, end1 = 0, ps2 = 0, pe2 = 0;
+            if (k + 1 < te) start_tile(k + 1, ps1, pe1, buf ^ 1, base1, end1);
+            else cp_async_commit();
+            if (k + 2 < te) load_ptrs(k + 2, ps2, pe2);
+            cp_async_wait<1>();   // tile k has landed
+            __syncwarp();
+            const int row = (int)(k * 32) + lane;
+            X acc = X(0);
+            if (row < n_rows) {
+                if (end0 - base0 <= kWarpCap) {
+                    const V *sv = s_vals[wib][buf];
+                    const int *si = s_idx[wib][buf];
+                    const int ov = base0 & ~(EV - 1), oi = base0 & ~3;
+                    for (int j0 = ps0; j0 < pe0; j0 += kGW) {
+                        X xv[kGW], vv[kGW];
+#pragma unroll
+                        for (int q = 0; q < kGW; q++)
+                            if (j0 + q < pe0) {
+                                vv[q] = Val<V>::get(sv[j0 + q - ov]);
+                                xv[q] = __ldg(x + si[j0 + q - oi]);
+                            }
+#pragma unroll
+                        for (int q = 0; q < kGW; q++)
+                            if (j0 + q < pe0) acc = add_rn(acc, mul_rn(vv[q], xv[q]));
+                    }
+                } else {
+                    for (int j0 = ps0; j0 < pe0; j0 += kGW) {
+                        X xv[kGW], vv[kGW];
+#pragma unroll
+                        for (int q = 0; q < kGW; q++)
+                            if (j0 + q < pe0) {
+                                vv[q] = Val<V>::get(__ldg(vals + j0 + q));
+                                xv[q] = __ldg(x + __ldg(indx + j0 + q));
+                            }
+#pragma unroll
+                        for (int q = 0; q < kGW; q++)
+                            if (j0 + q < pe0) acc = add_rn(acc, mul_rn(vv[q], xv[q]));
+                    }
+                }
+                const X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[row]));
+                y[row] = out;
+                if (FUSE_DOT) dsum[0] += (double)__ldg(x + row) * (double)out;
+            }
+            __syncwarp();   // buffer buf is refilled by tile k+2
+            ps0 = ps1;
+            pe0 = pe1;
+            base0 = base1;
+            end0 = end1;
+            ps1 = ps2;
+            pe1 = pe2;
         }
     }
+    cp_async_wait<0>();
     if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
 }
 
