@@ -1,24 +1,24 @@
 // Block-local level-scheduled sparse triangular solve for sm_103a.
 //
 // Rows are cut, in solve order, into contiguous blocks of at most R rows and kBsStepCap steps.
-// One persistent CTA of 128 threads solves one block at a time; blocks are handed out by an
-// atomic ticket in solve order, so a CTA only waits on blocks already taken by running CTAs.
-// Inside a block the rows are grouped by LOCAL level (levels over the dependencies that stay
-// inside the block) and each level is cut into steps of at most 128 rows, one row per thread.
-// A dependency inside the block is read from the block's solution slice in shared memory. A
-// dependency on an earlier block is read from global memory, where a not-yet-produced entry
-// holds a signalling-NaN pattern: the value is its own ready flag (bounded poll). A barrier after
-// the last step of each level publishes the level in shared memory.
+// One persistent CTA solves one block at a time; blocks are handed out by an atomic ticket in
+// solve order, so a CTA only waits on blocks already taken by running CTAs.  Inside a block the
+// rows are grouped by LOCAL level (levels over the dependencies that stay inside the block) and
+// each level is cut into steps of at most 128 rows.  A dependency inside the block is read from
+// the block's solution slice in shared memory.  A dependency on an earlier block is read from
+// global memory, where a not-yet-produced entry holds a signalling-NaN pattern: the value is its
+// own ready flag (bounded polls).
 //
-// Each row is stored as a packet of 16-byte pieces: three dependency codes and the row's slot,
-// then the values and the diagonal terms. Packets are laid out per step, so thread t of a step
-// finds its packet at (the step's first packet + t). Every thread streams its own packets into a
-// private ring of D steps in shared memory with cp.async, one commit group per step, so the ring
-// needs no handshake between warps: a thread waits only for its own copies. The first dependency
-// of a row on an earlier block is loaded H steps before its use, which hides the L2 round trip
-// between the SMs that solve consecutive blocks. Entries keep the reference's accumulation order
-// within each row, so results are bit-identical to the sequential loops of apply_ilu_array /
-// sparse_trsv_array (sparse/hala_sparse_utils.hpp).
+// The CTA has two roles.  128 solver threads take one row each per step.  Every solver thread
+// streams its own row packets (three dependency codes and the row's slot, then the values and
+// diagonal terms, 16-byte pieces) D steps ahead into a private shared-memory ring with cp.async,
+// one commit group per step, so no handshake between warps sits on that path; a named barrier
+// ends each level.  Four fetcher warps poll the first dependency on an earlier block of every row
+// in the coming steps from L2 (many loads in flight, re-polled until produced) and deposit each
+// value in a shared-memory ring as soon as it is ready.  A solver thread therefore waits on
+// shared memory, not on an L2 round trip, when it needs a value from the block before.  Entries
+// keep the reference's accumulation order within each row, so results are bit-identical to the
+// sequential loops of apply_ilu_array / sparse_trsv_array (sparse/hala_sparse_utils.hpp).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
 #include "hgb_bsolve.cuh"
@@ -29,16 +29,19 @@
 
 namespace hgb {
 
-constexpr int kBsThreads = 128;   // one row per thread per step
+constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
+constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
+constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
+constexpr int kBsBatch = 4;       // steps per fetcher-warp batch
+constexpr int kBsF = 32;          // steps in the remote-value ring (>= 2 * kBsFetchWarps * kBsBatch)
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
-// value pieces per packet (NV), ring depth in steps (D, a power of two), look-ahead of the
-// remote loads in steps (H)
+// value pieces per packet (NV) and packet-ring depth in steps (D, a power of two)
 template <typename V> struct BsCfg;
-template <> struct BsCfg<double> { static constexpr int NV = 3, D = 8, H = 2; };
-template <> struct BsCfg<float> { static constexpr int NV = 1, D = 16, H = 2; };
-template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 16, H = 2; };
+template <> struct BsCfg<double> { static constexpr int NV = 3, D = 4; };
+template <> struct BsCfg<float> { static constexpr int NV = 1, D = 8; };
+template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 8; };
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
 // dependencies (kBsIdle: no row for this thread in this step), bit 31 set on the last step of a
@@ -50,11 +53,12 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
 
 inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
 
-// shared memory: [ring D x (1 + NV) x 128 pieces | step descriptors | solution slice + zero slot]
+// shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
+//                 remote-value ring kBsF x 128 | solution slice + zero slot]
 template <typename V, typename X>
 constexpr size_t bs_smem_bytes(int R) {
     return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)kBsStepCap * 16 +
-           ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
+           (size_t)kBsF * kBsThreads * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
 }
 
 // One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
@@ -121,6 +125,7 @@ struct BsArgs {
     const int4 *desc;     // {first packet, rows, first overflow entry, overflow width | barrier << 16}
     const int4 *pk0;      // {code0, code1, code2, slot | ndeps << 16}; code >= 0: slot, < 0: -(row + 1)
     const int4 *pkv;      // value pieces, piece p of packet i at pkv[p * npk + i]
+    const int *rj;        // per packet: global row of its first dependency on an earlier block, or -1
     long npk;
     const int *ovf_codes;   // dependency k >= 3 of row t of a step: [first + (k - 3) * rows + t]
     const void *ovf_vals;
@@ -130,43 +135,41 @@ struct BsArgs {
     const int *skip;
 };
 
-// Asynchronous-copy issue and the polling load without a compiler memory clobber: the ring slots
-// they write are read only after cp_async_wait, which keeps its clobber, so the compiler may
-// schedule the step's arithmetic around them.
+// Asynchronous-copy issue without a compiler memory clobber: the ring slots it writes are read
+// only after cp_async_wait, which keeps its clobber, so the compiler may schedule the step's
+// arithmetic around it.
 __device__ __forceinline__ void bs_copy16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src));
 }
 __device__ __forceinline__ void bs_commit() { asm volatile("cp.async.commit_group;"); }
-__device__ __forceinline__ double bs_poll(const double *p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p));
-    return __longlong_as_double((long long)v);
-}
-__device__ __forceinline__ float bs_poll(const float *p) {
-    unsigned v;
-    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p));
-    return __uint_as_float(v);
-}
-
 // MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
 // UNIT: no division; RECIP: multiply by the stored FP32 reciprocal instead of dividing.
 template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
-__global__ void __launch_bounds__(kBsThreads, 1)
+__global__ void __launch_bounds__(kBsCta, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
-    constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, H = BsCfg<V>::H, NP = 1 + NV;
-    static_assert((D & (D - 1)) == 0 && H >= 1 && D - 1 - H >= 1, "ring shape");
+    constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, NP = 1 + NV;
+    static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
+    static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps * kBsBatch, "remote ring shape");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
     int4 *sdesc = ring + D * NP * kBsThreads;           // [kBsStepCap]
-    X *xsbuf = (X *)(sdesc + kBsStepCap);               // [R + 16 / sizeof(X) + 1]
-    __shared__ int blk_sh;
+    X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][kBsThreads] remote values
+    X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
+    __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
+    __shared__ int slot_step[kBsF];                     // step whose remote values rbuf slot holds
     const int t = threadIdx.x;
-    int4 *myring = ring + t;                            // this thread's piece 0 of ring slot 0
+    const bool solver = t < kBsThreads;
+    int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
+    volatile int *vdone = &done_step;
+    volatile int *vslot = slot_step;
+    volatile X *vrbuf = rbuf;
     for (;;) {
         __syncthreads();   // every thread is done with the previous block
         if (t == 0) blk_sh = atomicAdd(A.ticket, 1);
+        if (t < kBsF) slot_step[t] = -1;
+        if (t == 0) done_step = -1;
         __syncthreads();
         const int b = blk_sh;
         if (b >= A.nblk) break;
@@ -174,23 +177,93 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         const int ns = bi.y - bi.x, row_lo = bi.z, cnt = bi.w;
 
         // the block's step descriptors and its right-hand side slice, in one commit group
-        for (int i = t; i < ns; i += kBsThreads) bs_copy16(sdesc + i, A.desc + bi.x + i);
+        for (int i = t; i < ns; i += kBsCta) bs_copy16(sdesc + i, A.desc + bi.x + i);
         constexpr int E = 16 / (int)sizeof(X);
         const X *src = in + row_lo;
         const int mis = (int)(((size_t)src & 15) / sizeof(X));
         X *xs = xsbuf + mis;   // xs[i] and src[i] sit at the same offset modulo 16 bytes
         const int head = min(cnt, (E - mis) % E);
         const int body = (cnt - head) / E;
-        for (int i = t; i < body; i += kBsThreads) bs_copy16(xs + head + i * E, src + head + i * E);
-        for (int i = head + body * E + t; i < cnt; i += kBsThreads) xs[i] = src[i];
+        for (int i = t; i < body; i += kBsCta) bs_copy16(xs + head + i * E, src + head + i * E);
+        for (int i = head + body * E + t; i < cnt; i += kBsCta) xs[i] = src[i];
         if (t < head) xs[t] = src[t];
         if (t == 0) xs[A.R] = X(0);
         bs_commit();
         cp_async_wait<0>();
         __syncthreads();
+
+        if (!solver) {
+            // ---- fetcher warps: warp w takes the batches of kBsBatch steps numbered w, w+4, ...
+            const int w = (t - kBsThreads) >> 5, l = t & 31;
+            for (int s0 = w * kBsBatch; s0 < ns; s0 += kBsFetchWarps * kBsBatch) {
+                const int k1 = min(kBsBatch, ns - s0);
+                // the ring slots of these steps were last used kBsF steps earlier
+                const int need = s0 + k1 - 1 - kBsF;
+                int spins = 0;
+                while (*vdone < need) {
+                    if (++spins > kSpinLimit || ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT))) {
+                        atomicOr(A.err, DEV_ERR_TIMEOUT);
+                        break;
+                    }
+                }
+                int jj[kBsBatch][4];
+#pragma unroll
+                for (int k = 0; k < kBsBatch; k++) {
+                    const int4 d = (k < k1) ? sdesc[s0 + k] : make_int4(0, 0, 0, 0);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int r = l + 32 * q;
+                        jj[k][q] = (k < k1 && r < d.y) ? __ldg(A.rj + d.x + r) : -1;
+                        if (k < k1) vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + r] = Pending<X>::value();
+                    }
+                }
+                __syncwarp();
+                __threadfence_block();
+                if (l < k1) vslot[(s0 + l) & (kBsF - 1)] = s0 + l;   // slots reset: publish their step
+                // poll until every remote value of the batch has been deposited
+                unsigned todo = 0;
+#pragma unroll
+                for (int k = 0; k < kBsBatch; k++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (jj[k][q] >= 0) todo |= 1u << (4 * k + q);
+                spins = 0;
+                while (todo) {
+                    X v[kBsBatch][4];
+#pragma unroll
+                    for (int k = 0; k < kBsBatch; k++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (todo & (1u << (4 * k + q))) v[k][q] = ld_relaxed(out + jj[k][q]);
+#pragma unroll
+                    for (int k = 0; k < kBsBatch; k++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if ((todo & (1u << (4 * k + q))) && !Pending<X>::is(v[k][q])) {
+                                vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] = v[k][q];
+                                todo &= ~(1u << (4 * k + q));
+                            }
+                    if (todo && (++spins > kSpinLimit ||
+                                 ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT)))) {
+                        // give up: deposit NaN so that the solver threads terminate too
+                        atomicOr(A.err, DEV_ERR_TIMEOUT);
+#pragma unroll
+                        for (int k = 0; k < kBsBatch; k++)
+#pragma unroll
+                            for (int q = 0; q < 4; q++)
+                                if (todo & (1u << (4 * k + q)))
+                                    vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] =
+                                        Pending<X>::canon(Pending<X>::value());
+                        todo = 0;
+                    }
+                }
+            }
+            continue;   // to the block-end barrier
+        }
+
+        // ---- solver threads
         X *outb = out + row_lo;
         X *pendb = pend ? pend + row_lo : nullptr;
-
         // thread t's packet of step s into its ring slot s % D (an empty group past the last step);
         // without a row in step s it writes an idle packet (zero-slot codes, the barrier flag)
         auto issue = [&](int s) {
@@ -208,18 +281,25 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
             bs_commit();
         };
-        // start the load of the first remote dependency of thread t's row of step s (landed);
-        // padding and idle codes are >= 0
-        auto lookahead = [&](int s) -> X {
-            X v = X(0);
-            if (s < ns) {
-                const int4 p0 = myring[(s & (D - 1)) * (NP * kBsThreads)];
-                const int j = p0.x < 0 ? p0.x : (p0.y < 0 ? p0.y : p0.z);
-                if (j < 0) v = bs_poll(out + (-j - 1));
+        // the first remote dependency of this thread's row of step s, from the fetchers' ring
+        auto remote_first = [&](int s, int cd) -> X {
+            const int slot = s & (kBsF - 1);
+            int spins = 0;
+            X v = Pending<X>::value();
+            for (;;) {
+                if (vslot[slot] == s) {
+                    __threadfence_block();   // the slot's reset is ordered before its step number
+                    v = vrbuf[slot * kBsThreads + t];
+                    if (!Pending<X>::is(v)) return v;
+                }
+                if (++spins > kSpinLimit || ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT)))
+                    return wait_value(out + (-cd - 1), A.err);   // read it directly (bounded)
             }
-            return v;
         };
-        auto step = [&](int s, X rv) {
+        for (int s = 0; s < D - 1; s++) issue(s);
+        for (int s = 0; s < ns; s++) {
+            issue(s + D - 1);
+            cp_async_wait<D - 1>();   // step s has landed
             const int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
             const int4 p0 = slot[0];
             const int w = p0.w, nd = (w >> 15) & 0xFFFF, sl = w & 0x7FFF;
@@ -232,15 +312,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 #pragma unroll
             for (int k = 0; k < kBsInline; k++) xv[k] = xs[max(code[k], 0)];
             if ((code[0] | code[1] | code[2]) < 0) {
-                // dependencies on earlier blocks: the first one was loaded ahead, the others are polled
+                // dependencies on earlier blocks: the first from the fetchers, any other one polled
                 bool first = true;
 #pragma unroll
                 for (int k = 0; k < kBsInline; k++)
                     if (code[k] < 0) {
-                        X xk = first ? rv : Pending<X>::value();
+                        xv[k] = first ? remote_first(s, code[k]) : wait_value(out + (-code[k] - 1), A.err);
                         first = false;
-                        if (Pending<X>::is(xk)) xk = wait_value(out + (-code[k] - 1), A.err);
-                        xv[k] = xk;
                     }
             }
             X acc = (MODE == 0) ? xin : X(0);
@@ -265,24 +343,11 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 st_relaxed(outb + sl, acc);
                 if (pendb) pendb[sl] = Pending<X>::value();
             }
-            if (w < 0) __syncthreads();   // last step of a level
-        };
-
-        // ring prologue: steps 0 .. D-2 in flight, the first H of them landed
-        for (int s = 0; s < D - 1; s++) issue(s);
-        cp_async_wait<D - 1 - H>();
-        X rv[H];
-#pragma unroll
-        for (int u = 0; u < H; u++) rv[u] = lookahead(u);
-        for (int sb = 0; sb < ns; sb += H) {
-#pragma unroll
-            for (int u = 0; u < H; u++) {
-                const int s = sb + u;
-                if (s < ns) {
-                    issue(s + D - 1);
-                    cp_async_wait<D - 1 - H>();   // steps <= s + H have landed
-                    step(s, rv[u]);
-                    rv[u] = lookahead(s + H);
+            if (w < 0) {   // last step of a level: publish it to the solver threads and the fetchers
+                named_bar_sync(1, kBsThreads);
+                if (t == 0) {
+                    __threadfence_block();
+                    *vdone = s;
                 }
             }
         }
@@ -367,6 +432,7 @@ void BlockSolve::release() {
     cudaFree(blk);
     cudaFree(desc);
     cudaFree(pk0);
+    cudaFree(rj);
     cudaFree(pkv);
     cudaFree(ovf_codes);
     cudaFree(ovf_vals);
@@ -396,7 +462,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     if (n > 0) HGB_CUDA(cudaMemcpyAsync(diag.data(), diag_d, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
     HGB_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<int4> blk, desc, pk0;
-    std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map;
+    std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj;
     std::vector<int> lev(R), cnt, start, cur, order;
     auto row_of = [&](int pos) { return lower ? pos : n - 1 - pos; };
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
@@ -467,6 +533,10 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                         }
                     }
                     pk0.push_back(make_int4(cd[0], cd[1], cd[2], bs_word(row - row_lo, nd, bar)));
+                    int first_remote = -1;
+                    for (int q = kBsInline - 1; q >= 0; q--)
+                        if (cd[q] < 0) first_remote = -cd[q] - 1;
+                    rj.push_back(first_remote);
                     for (int q = 0; q < kBsInline; q++) map3.push_back(mp[q]);
                     dv_map.push_back(diag[row]);
                     dv_row.push_back(row);
@@ -486,6 +556,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     HGB_TRY(upload(&S.blk, blk));
     HGB_TRY(upload(&S.desc, desc));
     HGB_TRY(upload(&S.pk0, pk0));
+    HGB_TRY(upload(&S.rj, rj));
     HGB_TRY(upload(&S.map3, map3));
     HGB_TRY(upload(&S.dv_map, dv_map));
     HGB_TRY(upload(&S.dv_row, dv_row));
@@ -536,7 +607,7 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
         attr_dev = c->device;
     }
     const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-    bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsThreads, smem, c->stream>>>(A, alpha, in, out, pend);
+    bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsCta, smem, c->stream>>>(A, alpha, in, out, pend);
     return launch_check("bsolve_kernel");
 }
 
@@ -552,6 +623,7 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     A.desc = S.desc;
     A.pk0 = S.pk0;
     A.pkv = S.pkv;
+    A.rj = S.rj;
     A.npk = S.npk;
     A.ovf_codes = S.ovf_codes;
     A.ovf_vals = S.ovf_vals;
