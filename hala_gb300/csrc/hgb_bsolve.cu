@@ -142,6 +142,21 @@ __device__ __forceinline__ void bs_copy16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src));
 }
 __device__ __forceinline__ void bs_commit() { asm volatile("cp.async.commit_group;"); }
+// Step numbers published between the roles: acquire / release at CTA scope on shared memory.
+__device__ __forceinline__ int bs_ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void bs_st_release(int *p, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+// a timed-out wait anywhere in the launch ends this one too (checked every 256 polls)
+__device__ __forceinline__ bool bs_give_up(int spins, int *err) {
+    return spins > kSpinLimit || ((spins & 255) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT));
+}
+constexpr int kBsSpinLimitSleeping = 1 << 22;   // polls with a 128 ns sleep: about half a second
+
 // MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
 // UNIT: no division; RECIP: multiply by the stored FP32 reciprocal instead of dividing.
@@ -162,8 +177,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     const int t = threadIdx.x;
     const bool solver = t < kBsThreads;
     int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
-    volatile int *vdone = &done_step;
-    volatile int *vslot = slot_step;
     volatile X *vrbuf = rbuf;
     for (;;) {
         __syncthreads();   // every thread is done with the previous block
@@ -200,11 +213,12 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 // the ring slots of these steps were last used kBsF steps earlier
                 const int need = s0 + k1 - 1 - kBsF;
                 int spins = 0;
-                while (*vdone < need) {
-                    if (++spins > kSpinLimit || ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT))) {
+                while (bs_ld_acquire(&done_step) < need) {   // sleeping: the solver threads share the LSU
+                    if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
                         atomicOr(A.err, DEV_ERR_TIMEOUT);
                         break;
                     }
+                    __nanosleep(128);
                 }
                 int jj[kBsBatch][4];
 #pragma unroll
@@ -219,7 +233,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 }
                 __syncwarp();
                 __threadfence_block();
-                if (l < k1) vslot[(s0 + l) & (kBsF - 1)] = s0 + l;   // slots reset: publish their step
+                if (l < k1) bs_st_release(&slot_step[(s0 + l) & (kBsF - 1)], s0 + l);   // slots reset: publish
                 // poll until every remote value of the batch has been deposited
                 unsigned todo = 0;
 #pragma unroll
@@ -229,6 +243,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                         if (jj[k][q] >= 0) todo |= 1u << (4 * k + q);
                 spins = 0;
                 while (todo) {
+                    const unsigned before = todo;
                     X v[kBsBatch][4];
 #pragma unroll
                     for (int k = 0; k < kBsBatch; k++)
@@ -243,8 +258,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                                 vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] = v[k][q];
                                 todo &= ~(1u << (4 * k + q));
                             }
-                    if (todo && (++spins > kSpinLimit ||
-                                 ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT)))) {
+                    if (todo == before) __nanosleep(64);   // nothing produced yet: back off a little
+                    if (todo && (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping)) {
                         // give up: deposit NaN so that the solver threads terminate too
                         atomicOr(A.err, DEV_ERR_TIMEOUT);
 #pragma unroll
@@ -287,13 +302,11 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             int spins = 0;
             X v = Pending<X>::value();
             for (;;) {
-                if (vslot[slot] == s) {
-                    __threadfence_block();   // the slot's reset is ordered before its step number
+                if (bs_ld_acquire(&slot_step[slot]) == s) {   // the slot's reset precedes its step number
                     v = vrbuf[slot * kBsThreads + t];
                     if (!Pending<X>::is(v)) return v;
                 }
-                if (++spins > kSpinLimit || ((spins & 4095) == 0 && (*(volatile int *)A.err & DEV_ERR_TIMEOUT)))
-                    return wait_value(out + (-cd - 1), A.err);   // read it directly (bounded)
+                if (bs_give_up(++spins, A.err)) return wait_value(out + (-cd - 1), A.err);   // read it directly
             }
         };
         for (int s = 0; s < D - 1; s++) issue(s);
@@ -345,10 +358,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
             if (w < 0) {   // last step of a level: publish it to the solver threads and the fetchers
                 named_bar_sync(1, kBsThreads);
-                if (t == 0) {
-                    __threadfence_block();
-                    *vdone = s;
-                }
+                if (t == 0) bs_st_release(&done_step, s);
             }
         }
         cp_async_wait<0>();
