@@ -173,7 +173,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][kBsThreads] remote values
     X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
-    __shared__ int slot_step[kBsF];                     // step whose remote values rbuf slot holds
     const int t = threadIdx.x;
     const bool solver = t < kBsThreads;
     int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
@@ -181,8 +180,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     for (;;) {
         __syncthreads();   // every thread is done with the previous block
         if (t == 0) blk_sh = atomicAdd(A.ticket, 1);
-        if (t < kBsF) slot_step[t] = -1;
         if (t == 0) done_step = -1;
+        for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = Pending<X>::value();
         __syncthreads();
         const int b = blk_sh;
         if (b >= A.nblk) break;
@@ -220,6 +219,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     }
                     __nanosleep(128);
                 }
+                // (the solver threads reset each entry to the pending pattern after reading it)
                 int jj[kBsBatch][4];
 #pragma unroll
                 for (int k = 0; k < kBsBatch; k++) {
@@ -228,12 +228,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     for (int q = 0; q < 4; q++) {
                         const int r = l + 32 * q;
                         jj[k][q] = (k < k1 && r < d.y) ? __ldg(A.rj + d.x + r) : -1;
-                        if (k < k1) vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + r] = Pending<X>::value();
                     }
                 }
-                __syncwarp();
-                __threadfence_block();
-                if (l < k1) bs_st_release(&slot_step[(s0 + l) & (kBsF - 1)], s0 + l);   // slots reset: publish
                 // poll until every remote value of the batch has been deposited
                 unsigned todo = 0;
 #pragma unroll
@@ -296,18 +292,21 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
             bs_commit();
         };
-        // the first remote dependency of this thread's row of step s, from the fetchers' ring
+        // the first remote dependency of this thread's row of step s, from the fetchers' ring; the
+        // entry goes back to the pending pattern for its next use (kBsF steps later)
         auto remote_first = [&](int s, int cd) -> X {
-            const int slot = s & (kBsF - 1);
+            volatile X *e = vrbuf + (s & (kBsF - 1)) * kBsThreads + t;
             int spins = 0;
-            X v = Pending<X>::value();
-            for (;;) {
-                if (bs_ld_acquire(&slot_step[slot]) == s) {   // the slot's reset precedes its step number
-                    v = vrbuf[slot * kBsThreads + t];
-                    if (!Pending<X>::is(v)) return v;
+            X v = *e;
+            while (Pending<X>::is(v)) {
+                if (bs_give_up(++spins, A.err)) {
+                    v = wait_value(out + (-cd - 1), A.err);   // read it directly (bounded)
+                    break;
                 }
-                if (bs_give_up(++spins, A.err)) return wait_value(out + (-cd - 1), A.err);   // read it directly
+                v = *e;
             }
+            *e = Pending<X>::value();
+            return v;
         };
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
