@@ -230,42 +230,39 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                         jj[k][q] = (k < k1 && r < d.y) ? __ldg(A.rj + d.x + r) : -1;
                     }
                 }
-                // poll until every remote value of the batch has been deposited
-                unsigned todo = 0;
+                // poll the batch's steps in order (the block before produces them in that order):
+                // the four values of one step per lane per round, a short sleep when none is ready
+                spins = 0;
 #pragma unroll
-                for (int k = 0; k < kBsBatch; k++)
+                for (int k = 0; k < kBsBatch; k++) {
+                    unsigned todo = 0;
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        if (jj[k][q] >= 0) todo |= 1u << (4 * k + q);
-                spins = 0;
-                while (todo) {
-                    const unsigned before = todo;
-                    X v[kBsBatch][4];
-#pragma unroll
-                    for (int k = 0; k < kBsBatch; k++)
+                        if (jj[k][q] >= 0) todo |= 1u << q;
+                    while (todo) {
+                        X v[4];
 #pragma unroll
                         for (int q = 0; q < 4; q++)
-                            if (todo & (1u << (4 * k + q))) v[k][q] = ld_relaxed(out + jj[k][q]);
-#pragma unroll
-                    for (int k = 0; k < kBsBatch; k++)
+                            if (todo & (1u << q)) v[q] = ld_relaxed(out + jj[k][q]);
+                        const unsigned before = todo;
 #pragma unroll
                         for (int q = 0; q < 4; q++)
-                            if ((todo & (1u << (4 * k + q))) && !Pending<X>::is(v[k][q])) {
-                                vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] = v[k][q];
-                                todo &= ~(1u << (4 * k + q));
+                            if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
+                                vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] = v[q];
+                                todo &= ~(1u << q);
                             }
-                    if (todo == before) __nanosleep(64);   // nothing produced yet: back off a little
-                    if (todo && (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping)) {
-                        // give up: deposit NaN so that the solver threads terminate too
-                        atomicOr(A.err, DEV_ERR_TIMEOUT);
-#pragma unroll
-                        for (int k = 0; k < kBsBatch; k++)
+                        if (!todo) break;
+                        if (todo == before) __nanosleep(32);
+                        if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
+                            // give up: deposit NaN so that the solver threads terminate too
+                            atomicOr(A.err, DEV_ERR_TIMEOUT);
 #pragma unroll
                             for (int q = 0; q < 4; q++)
-                                if (todo & (1u << (4 * k + q)))
+                                if (todo & (1u << q))
                                     vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] =
                                         Pending<X>::canon(Pending<X>::value());
-                        todo = 0;
+                            todo = 0;
+                        }
                     }
                 }
             }
