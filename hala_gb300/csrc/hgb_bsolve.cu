@@ -32,8 +32,7 @@ namespace hgb {
 constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
-constexpr int kBsBatch = 4;       // steps per fetcher-warp batch
-constexpr int kBsF = 32;          // steps in the remote-value ring (>= 2 * kBsFetchWarps * kBsBatch)
+constexpr int kBsF = 32;          // steps in the remote-value ring
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
@@ -165,7 +164,7 @@ __global__ void __launch_bounds__(kBsCta, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, NP = 1 + NV;
     static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
-    static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps * kBsBatch, "remote ring shape");
+    static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps, "remote ring shape");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
@@ -205,66 +204,63 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         __syncthreads();
 
         if (!solver) {
-            // ---- fetcher warps: warp w takes the batches of kBsBatch steps numbered w, w+4, ...
+            // ---- fetcher warps: warp w takes steps w, w+4, w+8, ... one at a time, polling the
+            // step's remote values (four rows per lane) until all are deposited; the remote rows of
+            // its next step are loaded meanwhile
             const int w = (t - kBsThreads) >> 5, l = t & 31;
-            for (int s0 = w * kBsBatch; s0 < ns; s0 += kBsFetchWarps * kBsBatch) {
-                const int k1 = min(kBsBatch, ns - s0);
-                // the ring slots of these steps were last used kBsF steps earlier
-                const int need = s0 + k1 - 1 - kBsF;
+            int jq[4], jn[4];
+            auto load_rj = [&](int s, int (&jr)[4]) {
+                const int4 d = (s < ns) ? sdesc[s] : make_int4(0, 0, 0, 0);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int r = l + 32 * q;
+                    jr[q] = (r < d.y) ? __ldg(A.rj + d.x + r) : -1;
+                }
+            };
+            load_rj(w, jq);
+            for (int s = w; s < ns; s += kBsFetchWarps) {
+                load_rj(s + kBsFetchWarps, jn);
+                // the ring slot of step s was last used by step s - kBsF (the solver threads reset
+                // each entry to the pending pattern after reading it)
                 int spins = 0;
-                while (bs_ld_acquire(&done_step) < need) {   // sleeping: the solver threads share the LSU
+                while (bs_ld_acquire(&done_step) < s - kBsF) {   // sleeping: the solver threads share the LSU
                     if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
                         atomicOr(A.err, DEV_ERR_TIMEOUT);
                         break;
                     }
                     __nanosleep(128);
                 }
-                // (the solver threads reset each entry to the pending pattern after reading it)
-                int jj[kBsBatch][4];
+                volatile X *slot = vrbuf + (s & (kBsF - 1)) * kBsThreads + l;
+                unsigned todo = 0;
 #pragma unroll
-                for (int k = 0; k < kBsBatch; k++) {
-                    const int4 d = (k < k1) ? sdesc[s0 + k] : make_int4(0, 0, 0, 0);
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int r = l + 32 * q;
-                        jj[k][q] = (k < k1 && r < d.y) ? __ldg(A.rj + d.x + r) : -1;
-                    }
-                }
-                // poll the batch's steps in order (the block before produces them in that order):
-                // the four values of one step per lane per round, a short sleep when none is ready
+                for (int q = 0; q < 4; q++)
+                    if (jq[q] >= 0) todo |= 1u << q;
                 spins = 0;
-#pragma unroll
-                for (int k = 0; k < kBsBatch; k++) {
-                    unsigned todo = 0;
+                while (todo) {
+                    X v[4];
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        if (jj[k][q] >= 0) todo |= 1u << q;
-                    while (todo) {
-                        X v[4];
+                        if (todo & (1u << q)) v[q] = ld_relaxed(out + jq[q]);
+                    const unsigned before = todo;
 #pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if (todo & (1u << q)) v[q] = ld_relaxed(out + jj[k][q]);
-                        const unsigned before = todo;
-#pragma unroll
-                        for (int q = 0; q < 4; q++)
-                            if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
-                                vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] = v[q];
-                                todo &= ~(1u << q);
-                            }
-                        if (!todo) break;
-                        if (todo == before) __nanosleep(32);
-                        if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
-                            // give up: deposit NaN so that the solver threads terminate too
-                            atomicOr(A.err, DEV_ERR_TIMEOUT);
-#pragma unroll
-                            for (int q = 0; q < 4; q++)
-                                if (todo & (1u << q))
-                                    vrbuf[((s0 + k) & (kBsF - 1)) * kBsThreads + l + 32 * q] =
-                                        Pending<X>::canon(Pending<X>::value());
-                            todo = 0;
+                    for (int q = 0; q < 4; q++)
+                        if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
+                            slot[32 * q] = v[q];
+                            todo &= ~(1u << q);
                         }
+                    if (!todo) break;
+                    if (todo == before) __nanosleep(32);
+                    if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
+                        // give up: deposit NaN so that the solver threads terminate too
+                        atomicOr(A.err, DEV_ERR_TIMEOUT);
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (todo & (1u << q)) slot[32 * q] = Pending<X>::canon(Pending<X>::value());
+                        todo = 0;
                     }
                 }
+#pragma unroll
+                for (int q = 0; q < 4; q++) jq[q] = jn[q];
             }
             continue;   // to the block-end barrier
         }
