@@ -285,22 +285,18 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
             bs_commit();
         };
-        // the first remote dependency of this thread's row of step s, from the fetchers' ring; the
-        // entry goes back to the pending pattern for its next use (kBsF steps later)
-        auto remote_first = [&](int s, int cd) -> X {
-            volatile X *e = vrbuf + (s & (kBsF - 1)) * kBsThreads + t;
+        // the first remote dependency of this thread's row of step s, once the fetchers' ring
+        // entry e showed the pending pattern: wait for the deposit (bounded, then read directly)
+        auto remote_wait = [&](volatile X *e, int cd) -> X {
             int spins = 0;
             X v = *e;
             while (Pending<X>::is(v)) {
-                if (bs_give_up(++spins, A.err)) {
-                    v = wait_value(out + (-cd - 1), A.err);   // read it directly (bounded)
-                    break;
-                }
+                if (bs_give_up(++spins, A.err)) return wait_value(out + (-cd - 1), A.err);
                 v = *e;
             }
-            *e = Pending<X>::value();
             return v;
         };
+        int last_pub = -1;   // thread 0: the last step published to the fetchers
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
@@ -316,15 +312,25 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             X xv[kBsInline];
 #pragma unroll
             for (int k = 0; k < kBsInline; k++) xv[k] = xs[max(code[k], 0)];
-            if ((code[0] | code[1] | code[2]) < 0) {
-                // dependencies on earlier blocks: the first from the fetchers, any other one polled
-                bool first = true;
+            // dependencies on earlier blocks: the first one comes from the fetchers' ring (the entry
+            // goes back to the pending pattern for its next use, kBsF steps later); any further one
+            // is polled directly
+            {
+                const int k0 = code[0] < 0 ? 0 : (code[1] < 0 ? 1 : (code[2] < 0 ? 2 : -1));
+                volatile X *e = vrbuf + (s & (kBsF - 1)) * kBsThreads + t;
+                X rv = *e;
+                if (k0 >= 0) {
+                    if (Pending<X>::is(rv)) rv = remote_wait(e, code[k0]);
+                    *e = Pending<X>::value();
+                }
 #pragma unroll
                 for (int k = 0; k < kBsInline; k++)
-                    if (code[k] < 0) {
-                        xv[k] = first ? remote_first(s, code[k]) : wait_value(out + (-code[k] - 1), A.err);
-                        first = false;
-                    }
+                    if (k == k0) xv[k] = rv;
+                if (k0 >= 0 && k0 < kBsInline - 1 && (code[k0 + 1 < kBsInline ? k0 + 1 : 0] | code[kBsInline - 1]) < 0) {
+#pragma unroll
+                    for (int k = 0; k < kBsInline; k++)
+                        if (k > k0 && code[k] < 0) xv[k] = wait_value(out + (-code[k] - 1), A.err);
+                }
             }
             X acc = (MODE == 0) ? xin : X(0);
 #pragma unroll
@@ -348,9 +354,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 st_relaxed(outb + sl, acc);
                 if (pendb) pendb[sl] = Pending<X>::value();
             }
-            if (w < 0) {   // last step of a level: publish it to the solver threads and the fetchers
+            if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
+                           // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
                 named_bar_sync(1, kBsThreads);
-                if (t == 0) bs_st_release(&done_step, s);
+                if (t == 0 && s - last_pub >= 8) {
+                    bs_st_release(&done_step, s);
+                    last_pub = s;
+                }
             }
         }
         cp_async_wait<0>();
@@ -512,7 +522,9 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                 const size_t ob = ovf_codes.size();
                 if (ob + (size_t)kx * nr > (size_t)INT_MAX || pk0.size() + nr > (size_t)INT_MAX)
                     return fail(HGB_ERR_UNSUPPORTED, "block solve: packed arrays exceed 2^31 entries");
-                const int bar = (k + nr == start[l + 1]) ? 1 : 0;
+                // a barrier ends every level, and every 16th step inside a long level, so that the
+                // solver threads' progress reaches the fetchers at least every 16 steps
+                const int bar = (k + nr == start[l + 1] || ((k - start[l]) / kBsThreads) % 16 == 15) ? 1 : 0;
                 desc.push_back(make_int4((int)pk0.size(), nr, (int)ob, kx | (bar << 16)));
                 ovf_codes.resize(ob + (size_t)kx * nr, 0);
                 ovf_map.resize(ob + (size_t)kx * nr, -1);

@@ -39,7 +39,25 @@ MATS = {
     "chain_40000": lambda rng: P.poisson2d(40000, 1),
     # rows with more than three dependencies in each triangle, several blocks
     "random_40000": lambda rng: P.random_csr_sparse(40000, 10, rng),
+    # one level of 16384+ rows per block, every row depending on the block before (long levels)
+    "shift_50000": lambda rng: shifted_diagonals(50000, 16384),
 }
+
+
+def shifted_diagonals(n, off):
+    """Diagonal plus the two diagonals at distance off: row i couples to i - off and i + off."""
+    rows, cols = [], []
+    for o in (-off, 0, off):
+        i = np.arange(max(0, -o), min(n, n - o))
+        rows.append(i)
+        cols.append(i + o)
+    r, c = np.concatenate(rows), np.concatenate(cols)
+    order = np.lexsort((c, r))
+    r, c = r[order], c[order]
+    v = np.where(r == c, 4.0, -1.0)
+    p = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(r, minlength=n), out=p[1:])
+    return p.astype(np.int32), c.astype(np.int32), v
 
 
 @pytest.mark.parametrize("name", list(MATS))
@@ -107,9 +125,12 @@ def test_f32_factor_and_apply_bit_exact(eng, rng):
     assert np.array_equal(ilu.apply(T(x)).cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
 
 
+@pytest.mark.parametrize("mat", ["aniso3d_18", "aniso3d_44", "shift_80000"])
 @pytest.mark.parametrize("store", [torch.float32, torch.bfloat16])
-def test_mixed_store_apply(eng, rng, store):
-    p, i, v = P.aniso3d(18)
+def test_mixed_store_apply(eng, rng, store, mat):
+    # aniso3d_44 and shift_80000 span several 32768-row solve blocks of the FP32 store
+    p, i, v = {"aniso3d_18": lambda: P.aniso3d(18), "aniso3d_44": lambda: P.aniso3d(44),
+               "shift_80000": lambda: shifted_diagonals(80000, 20000)}[mat]()
     n = len(p) - 1
     fo, do, _ = O.ilu_factor(p, i, v)
     ilu = E.make_ilu(eng, T(p), T(i), T(v), store=store)
