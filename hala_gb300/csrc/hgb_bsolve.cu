@@ -16,7 +16,11 @@
 // ends each level.  Four fetcher warps poll the first dependency on an earlier block of every row
 // in the coming steps from L2 (many loads in flight, re-polled until produced) and deposit each
 // value in a shared-memory ring as soon as it is ready.  A solver thread therefore waits on
-// shared memory, not on an L2 round trip, when it needs a value from the block before.  Entries
+// shared memory, not on an L2 round trip, when it needs a value from the block before.  The
+// launch groups the CTAs into thread-block clusters that take consecutive blocks: inside a
+// cluster, the CTA of block b writes each value that block b+1 needs first straight into the
+// ring of block b+1's CTA (distributed shared memory, st.shared::cluster), so most hops between
+// blocks skip L2 altogether; the fetchers serve the hop into a cluster's first block.  Entries
 // keep the reference's accumulation order within each row, so results are bit-identical to the
 // sequential loops of apply_ilu_array / sparse_trsv_array (sparse/hala_sparse_utils.hpp).
 #include "hgb_internal.cuh"
@@ -39,7 +43,7 @@ constexpr int kBsInline = 3;      // dependencies carried in a row packet; more 
 // value pieces per packet (NV) and packet-ring depth in steps (D, a power of two)
 template <typename V> struct BsCfg;
 template <> struct BsCfg<double> { static constexpr int NV = 3, D = 4; };
-template <> struct BsCfg<float> { static constexpr int NV = 1, D = 8; };
+template <> struct BsCfg<float> { static constexpr int NV = 2, D = 8; };
 template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 8; };
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
@@ -50,7 +54,8 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
     return (int)((unsigned)slot | ((unsigned)nd << 15) | ((unsigned)bar << 31));
 }
 
-inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
+inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
+constexpr int kBsMaxCluster = 8;   // portable thread-block cluster size
 
 // shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
 //                 remote-value ring kBsF x 128 | solution slice + zero slot]
@@ -61,39 +66,48 @@ constexpr size_t bs_smem_bytes(int R) {
 }
 
 // One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
-//   FP64 {v0, v1} {v2, RN(1/d)} {d, 0};  FP32 {v0, v1, v2, dv};  BF16 {v0 | v1 << 16, v2, dv, 0}
+//   FP64 {v0, v1} {v2, RN(1/d)} {d, push, 0};  FP32 {v0, v1, v2, dv} {push, 0, 0, 0};
+//   BF16 {v0 | v1 << 16, v2, dv, push}
 // dv is the FP32 diagonal (divided by) or the FP32 reciprocal of an FP64 pivot (multiplied by).
+// push: where the row's value goes in the next block's remote ring (consumer step << 7 | thread),
+// or -1.
 template <typename V> struct BsRow;
 template <> struct BsRow<double> {
     double v[3], d, dinv;
+    int push;
     __device__ __forceinline__ void load(const int4 *p) {
-        const double2 a = *(const double2 *)p, b = *(const double2 *)(p + kBsThreads),
-                      c = *(const double2 *)(p + 2 * kBsThreads);
+        const double2 a = *(const double2 *)p, b = *(const double2 *)(p + kBsThreads);
+        const int4 c = p[2 * kBsThreads];
         v[0] = a.x;
         v[1] = a.y;
         v[2] = b.x;
         dinv = b.y;
-        d = c.x;
+        d = __hiloint2double(c.y, c.x);
+        push = c.z;
     }
 };
 template <> struct BsRow<float> {
     float v[3], d;
+    int push;
     __device__ __forceinline__ void load(const int4 *p) {
         const float4 a = *(const float4 *)p;
         v[0] = a.x;
         v[1] = a.y;
         v[2] = a.z;
         d = a.w;
+        push = p[kBsThreads].x;
     }
 };
 template <> struct BsRow<uint16_t> {
     float v[3], d;
+    int push;
     __device__ __forceinline__ void load(const int4 *p) {
         const int4 a = *p;
         v[0] = __uint_as_float((unsigned)a.x << 16);
         v[1] = __uint_as_float((unsigned)a.x & 0xFFFF0000u);
         v[2] = __uint_as_float((unsigned)a.y << 16);
         d = __int_as_float(a.z);
+        push = a.w;
     }
 };
 
@@ -129,6 +143,7 @@ struct BsArgs {
     const int *ovf_codes;   // dependency k >= 3 of row t of a step: [first + (k - 3) * rows + t]
     const void *ovf_vals;
     int R;                  // rows per block; slot R of the solution slice holds 0 (padding code)
+    int cl;                 // CTAs per cluster the packets' push targets were planned for
     int *ticket;
     int *err;
     const int *skip;
@@ -149,6 +164,42 @@ __device__ __forceinline__ int bs_ld_acquire(const int *p) {
 }
 __device__ __forceinline__ void bs_st_release(int *p, int v) {
     asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void bs_st_release_cluster(int *p, int v) {
+    asm volatile("st.release.cluster.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+// thread-block cluster: rank, size, barrier over all its threads, peer shared-memory access
+__device__ __forceinline__ unsigned bs_cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned bs_cluster_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void bs_cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t bs_peer(const void *local, unsigned rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_addr(local)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void bs_peer_store(uint32_t a, int v) {
+    asm volatile("st.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void bs_peer_store(uint32_t a, float v) {
+    asm volatile("st.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(__float_as_uint(v)) : "memory");
+}
+__device__ __forceinline__ void bs_peer_store(uint32_t a, double v) {
+    asm volatile("st.shared::cluster.b64 [%0], %1;" ::"r"(a), "l"(__double_as_longlong(v)) : "memory");
+}
+__device__ __forceinline__ int bs_peer_load_acquire(uint32_t a) {
+    int v;
+    asm volatile("ld.acquire.cluster.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
 }
 // a timed-out wait anywhere in the launch ends this one too (checked every 256 polls)
 __device__ __forceinline__ bool bs_give_up(int spins, int *err) {
@@ -173,17 +224,30 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
     const int t = threadIdx.x;
+    const unsigned rank = bs_cluster_rank(), ncl = bs_cluster_size();
+    if ((int)ncl != A.cl) {   // the push targets assume clusters of A.cl CTAs
+        if (t == 0) atomicOr(A.err, DEV_ERR_CSR);
+        return;
+    }
     const bool solver = t < kBsThreads;
     int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
     volatile X *vrbuf = rbuf;
     for (;;) {
-        __syncthreads();   // every thread is done with the previous block
-        if (t == 0) blk_sh = atomicAdd(A.ticket, 1);
+        // clusters take tickets; rank r of the cluster with ticket q solves block q * ncl + r.  The
+        // cluster barriers: every CTA of the cluster is done with the previous round (including its
+        // writes into its peers' rings), then the new ticket and the reset rings are visible
+        bs_cluster_sync();
+        if (t == 0 && rank == 0) {
+            const int q = atomicAdd(A.ticket, 1);
+            for (unsigned r = 0; r < ncl; r++) bs_peer_store(bs_peer(&blk_sh, r), q);
+        }
         if (t == 0) done_step = -1;
         for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = Pending<X>::value();
-        __syncthreads();
-        const int b = blk_sh;
-        if (b >= A.nblk) break;
+        bs_cluster_sync();
+        const int q = blk_sh;
+        if (q * (int)ncl >= A.nblk) break;   // the same for the whole cluster
+        const int b = q * (int)ncl + (int)rank;
+        if (b >= A.nblk) continue;            // the last cluster may have spare ranks
         const int4 bi = __ldg(A.blk + b);
         const int ns = bi.y - bi.x, row_lo = bi.z, cnt = bi.w;
 
@@ -296,7 +360,12 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
             return v;
         };
-        int last_pub = -1;   // thread 0: the last step published to the fetchers
+        int last_pub = -1;   // thread 0: the last step published to the fetchers and the cluster
+        // the next block's CTA (the next rank of this cluster): its ring and its published progress
+        const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
+        const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
+        const uint32_t next_done = has_next ? bs_peer(&done_step, rank + 1) : 0u;
+        int next_seen = -1;   // the next block's done_step as last read by this thread
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
@@ -353,12 +422,26 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 xs[sl] = acc;
                 st_relaxed(outb + sl, acc);
                 if (pendb) pendb[sl] = Pending<X>::value();
+                if (rw.push >= 0 && has_next) {
+                    // the next block reads this value first: write it into that CTA's ring once it
+                    // has released the slot (its step push_step - kBsF is done)
+                    const int ps = rw.push >> 7, pt = rw.push & 127;
+                    int spins = 0;
+                    while (next_seen < ps - kBsF) {
+                        next_seen = bs_peer_load_acquire(next_done);
+                        if (next_seen < ps - kBsF && bs_give_up(++spins, A.err)) {
+                            atomicOr(A.err, DEV_ERR_TIMEOUT);
+                            break;
+                        }
+                    }
+                    bs_peer_store(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)), acc);
+                }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
                            // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
                 named_bar_sync(1, kBsThreads);
                 if (t == 0 && s - last_pub >= 8) {
-                    bs_st_release(&done_step, s);
+                    bs_st_release_cluster(&done_step, s);
                     last_pub = s;
                 }
             }
@@ -378,13 +461,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 // value pieces of the packets (layout in BsRow)
 template <typename V>
 __global__ void bs_pack_kernel(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
-                               const int *__restrict__ dv_row, const V *__restrict__ src,
-                               const double *__restrict__ piv, int4 *__restrict__ pkv);
+                               const int *__restrict__ dv_row, const int *__restrict__ push,
+                               const V *__restrict__ src, const double *__restrict__ piv, int4 *__restrict__ pkv);
 
 template <>
 __global__ void bs_pack_kernel<double>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
-                                       const int *__restrict__ dv_row, const double *__restrict__ src,
-                                       const double *__restrict__ piv, int4 *__restrict__ pkv) {
+                                       const int *__restrict__ dv_row, const int *__restrict__ push,
+                                       const double *__restrict__ src, const double *__restrict__ piv,
+                                       int4 *__restrict__ pkv) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
         double v[3];
         for (int k = 0; k < 3; k++) {
@@ -396,14 +480,15 @@ __global__ void bs_pack_kernel<double>(long npk, const int *__restrict__ map3, c
         ((double2 *)pkv)[i] = make_double2(v[0], v[1]);
         const bool fast = bs_markstein_range(((unsigned)__double2hiint(d) >> 20) & 0x7FFu);
         ((double2 *)(pkv + npk))[i] = make_double2(v[2], fast ? 1.0 / d : 0.0);   // correctly rounded reciprocal
-        ((double2 *)(pkv + 2 * npk))[i] = make_double2(d, 0.0);
+        pkv[2 * npk + i] = make_int4(__double2loint(d), __double2hiint(d), push[i], 0);
     }
 }
 
 template <>
 __global__ void bs_pack_kernel<float>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
-                                      const int *__restrict__ dv_row, const float *__restrict__ src,
-                                      const double *__restrict__ piv, int4 *__restrict__ pkv) {
+                                      const int *__restrict__ dv_row, const int *__restrict__ push,
+                                      const float *__restrict__ src, const double *__restrict__ piv,
+                                      int4 *__restrict__ pkv) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
         float v[3];
         for (int k = 0; k < 3; k++) {
@@ -413,13 +498,15 @@ __global__ void bs_pack_kernel<float>(long npk, const int *__restrict__ map3, co
         const int dm = dv_map[i], r = dv_row[i];
         const float dv = piv ? (float)(1.0 / piv[r]) : (dm >= 0 ? src[dm] : 1.0f);
         ((float4 *)pkv)[i] = make_float4(v[0], v[1], v[2], dv);
+        pkv[npk + i] = make_int4(push[i], 0, 0, 0);
     }
 }
 
 template <>
 __global__ void bs_pack_kernel<uint16_t>(long npk, const int *__restrict__ map3, const int *__restrict__ dv_map,
-                                         const int *__restrict__ dv_row, const uint16_t *__restrict__ src,
-                                         const double *__restrict__ piv, int4 *__restrict__ pkv) {
+                                         const int *__restrict__ dv_row, const int *__restrict__ push,
+                                         const uint16_t *__restrict__ src, const double *__restrict__ piv,
+                                         int4 *__restrict__ pkv) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npk; i += (long)gridDim.x * blockDim.x) {
         unsigned v[3];
         for (int k = 0; k < 3; k++) {
@@ -428,7 +515,7 @@ __global__ void bs_pack_kernel<uint16_t>(long npk, const int *__restrict__ map3,
         }
         const int dm = dv_map[i], r = dv_row[i];
         const float dv = piv ? (float)(1.0 / piv[r]) : (dm >= 0 ? __uint_as_float((unsigned)src[dm] << 16) : 1.0f);
-        pkv[i] = make_int4((int)(v[0] | (v[1] << 16)), (int)v[2], __float_as_int(dv), 0);
+        pkv[i] = make_int4((int)(v[0] | (v[1] << 16)), (int)v[2], __float_as_int(dv), push[i]);
     }
 }
 
@@ -445,6 +532,7 @@ void BlockSolve::release() {
     cudaFree(desc);
     cudaFree(pk0);
     cudaFree(rj);
+    cudaFree(push);
     cudaFree(pkv);
     cudaFree(ovf_codes);
     cudaFree(ovf_vals);
@@ -454,6 +542,43 @@ void BlockSolve::release() {
     cudaFree(ovf_map);
     cudaFree(ticket);
     *this = BlockSolve();
+}
+
+// Largest portable cluster size (8, 4, 2) at which at least one cluster of the block-solve CTAs
+// fits on the device, or 1.  HGB_BS_CLUSTER=1 turns clusters off (for comparisons).
+static int bs_cluster_plan(hgb_ctx *c, int R) {
+    const char *e = getenv("HGB_BS_CLUSTER");
+    const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
+    auto fits = [&](auto kernel, size_t smem, int cl) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cl * 16);
+        cfg.blockDim = dim3(kBsCta);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return n;
+    };
+    DeviceGuard g(c->device);
+    for (int cl = cap; cl > 1; cl /= 2) {
+        const int n = (R <= 16384) ? fits(bsolve_kernel<double, double, 0, true, false>, bs_smem_bytes<double, double>(R), cl)
+                                   : fits(bsolve_kernel<float, float, 0, true, false>, bs_smem_bytes<float, float>(R), cl);
+        if (n >= 1) return cl;
+    }
+    return 1;
 }
 
 template <typename T>
@@ -560,17 +685,67 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         blk.push_back(make_int4(s_first, (int)desc.size(), row_lo, rows));
         p0 = p1;
     }
+    // Push targets.  Blocks are grouped in runs of cl (one thread-block cluster each); inside a
+    // run, the value that a row of block b+1 needs first from block b is written by block b's CTA
+    // straight into block b+1's ring (consumer step << 7 | consumer thread).  A producer row feeds
+    // at most one consumer row; further ones stay with the fetchers.  The producer steps must not
+    // decrease along the consumer steps (then a producer waiting for ring space can never wait on
+    // itself); a pair of blocks that breaks this keeps the fetchers.
+    const int cl = bs_cluster_plan(c, R);
+    std::vector<int> push(pk0.size(), -1);
+    if (cl > 1) {
+        std::vector<int> pk_of_row(n, -1), blk_of_row(n, -1), step_of_pk(pk0.size(), 0);
+        for (int bb = 0; bb < (int)blk.size(); bb++)
+            for (int st = blk[bb].x; st < blk[bb].y; st++)
+                for (int t = 0; t < desc[st].y; t++) {
+                    const int pkt = desc[st].x + t;
+                    const int row = blk[bb].z + (pk0[pkt].w & 0x7FFF);
+                    pk_of_row[row] = pkt;
+                    blk_of_row[row] = bb;
+                    step_of_pk[pkt] = st - blk[bb].x;
+                }
+        std::vector<std::pair<int, int>> planned;   // (consumer packet, producer packet)
+        for (int bb = 1; bb < (int)blk.size(); bb++) {
+            if (bb / cl != (bb - 1) / cl) continue;
+            planned.clear();
+            int prev_max = -1;
+            bool monotone = true;
+            for (int st = blk[bb].x; st < blk[bb].y && monotone; st++) {
+                int smin = INT_MAX, smax = -1;
+                for (int t = 0; t < desc[st].y; t++) {
+                    const int cp = desc[st].x + t, j = rj[cp];
+                    if (j < 0 || blk_of_row[j] != bb - 1) continue;
+                    const int pp = pk_of_row[j];
+                    if (push[pp] >= 0) continue;
+                    push[pp] = ((st - blk[bb].x) << 7) | t;
+                    planned.push_back({cp, pp});
+                    smin = std::min(smin, step_of_pk[pp]);
+                    smax = std::max(smax, step_of_pk[pp]);
+                }
+                if (smax >= 0) {
+                    if (smin < prev_max) monotone = false;
+                    prev_max = std::max(prev_max, smax);
+                }
+            }
+            for (auto &pc : planned) {
+                if (monotone) rj[pc.first] = -1;     // pushed: the fetchers skip it
+                else push[pc.second] = -1;
+            }
+        }
+    }
     S.release();
     S.n = n;
     S.nblk = (int)blk.size();
     S.nsteps = (int)desc.size();
     S.R = R;
+    S.cl = cl;
     S.npk = (long)pk0.size();
     S.novf = (long)ovf_codes.size();
     HGB_TRY(upload(&S.blk, blk));
     HGB_TRY(upload(&S.desc, desc));
     HGB_TRY(upload(&S.pk0, pk0));
     HGB_TRY(upload(&S.rj, rj));
+    HGB_TRY(upload(&S.push, push));
     HGB_TRY(upload(&S.map3, map3));
     HGB_TRY(upload(&S.dv_map, dv_map));
     HGB_TRY(upload(&S.dv_row, dv_row));
@@ -595,13 +770,13 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
     const int g = (int)std::max<long>(1, std::min<long>((S.npk + 255) / 256, c->num_sms * 8));
     const int go = (int)std::max<long>(1, std::min<long>((S.novf + 255) / 256, c->num_sms * 8));
     if (vsize == 8) {
-        bs_pack_kernel<double><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const double *)svals, piv, S.pkv);
+        bs_pack_kernel<double><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, S.push, (const double *)svals, piv, S.pkv);
         if (S.novf) bs_gather_kernel<double><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const double *)svals, (double *)S.ovf_vals);
     } else if (vsize == 4) {
-        bs_pack_kernel<float><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const float *)svals, piv, S.pkv);
+        bs_pack_kernel<float><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, S.push, (const float *)svals, piv, S.pkv);
         if (S.novf) bs_gather_kernel<float><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const float *)svals, (float *)S.ovf_vals);
     } else {
-        bs_pack_kernel<uint16_t><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, (const uint16_t *)svals, piv, S.pkv);
+        bs_pack_kernel<uint16_t><<<g, 256, 0, c->stream>>>(S.npk, S.map3, S.dv_map, S.dv_row, S.push, (const uint16_t *)svals, piv, S.pkv);
         if (S.novf)
             bs_gather_kernel<uint16_t><<<go, 256, 0, c->stream>>>(S.novf, S.ovf_map, (const uint16_t *)svals, (uint16_t *)S.ovf_vals);
     }
@@ -620,8 +795,37 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
                                       (int)smem));
         attr_dev = c->device;
     }
-    const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-    bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsCta, smem, c->stream>>>(A, alpha, in, out, pend);
+    if (S.cl <= 1) {
+        const int grid = std::max(1, std::min(S.nblk, c->num_sms));
+        bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsCta, smem, c->stream>>>(A, alpha, in, out, pend);
+        return launch_check("bsolve_kernel");
+    }
+    // thread-block clusters of S.cl CTAs (the push targets were planned for that size); as many
+    // clusters as are co-resident, at most one per run of S.cl blocks
+    static int clusters_dev[kBsMaxCluster + 1] = {};
+    static int clusters_max[kBsMaxCluster + 1] = {};
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = S.cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kBsCta);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (clusters_dev[S.cl] != c->device + 1) {
+        cfg.gridDim = dim3(S.cl * 16);
+        int n = 0;
+        HGB_CUDA(cudaOccupancyMaxActiveClusters(&n, bsolve_kernel<V, X, MODE, UNIT, RECIP>, &cfg));
+        if (n < 1) return fail(HGB_ERR_UNSUPPORTED, "bsolve: no cluster of %d CTAs fits", S.cl);
+        clusters_max[S.cl] = n;
+        clusters_dev[S.cl] = c->device + 1;
+    }
+    const int runs = (S.nblk + S.cl - 1) / S.cl;
+    cfg.gridDim = dim3(S.cl * std::max(1, std::min(runs, clusters_max[S.cl])));
+    HGB_CUDA(cudaLaunchKernelEx(&cfg, bsolve_kernel<V, X, MODE, UNIT, RECIP>, A, alpha, in, out, pend));
     return launch_check("bsolve_kernel");
 }
 
@@ -642,6 +846,7 @@ int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, 
     A.ovf_codes = S.ovf_codes;
     A.ovf_vals = S.ovf_vals;
     A.R = S.R;
+    A.cl = S.cl;
     A.ticket = S.ticket;
     A.err = c->err;
     A.skip = skip;

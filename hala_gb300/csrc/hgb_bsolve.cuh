@@ -13,7 +13,9 @@ struct BlockSolve {
     int4 *desc = nullptr;       // [nsteps] {first packet, rows, first overflow entry, overflow width | barrier << 16}
     int4 *pk0 = nullptr;        // [npk] {code0, code1, code2, slot | ndeps << 16}
     int4 *pkv = nullptr;        // [NV * npk] value pieces (store precision, diagonal terms)
-    int *rj = nullptr;          // [npk] first dependency of the row on an earlier block, or -1
+    int *rj = nullptr;          // [npk] first dependency of the row on an earlier block (fetched), or -1
+    int *push = nullptr;        // [npk] where the row's value goes in the next block's ring, or -1
+    int cl = 1;                 // CTAs per thread-block cluster the push targets assume
     int *ovf_codes = nullptr;   // [novf] dependencies beyond the third, column-major per step
     void *ovf_vals = nullptr;
     int *map3 = nullptr, *dv_map = nullptr, *dv_row = nullptr, *ovf_map = nullptr;   // value gather maps
