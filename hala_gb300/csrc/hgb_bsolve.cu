@@ -35,7 +35,7 @@ namespace hgb {
 
 constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
-constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
+constexpr int kBsCta = kBsThreads + 32 * (kBsFetchWarps + 1);   // + a publisher warp
 constexpr int kBsF = 32;          // steps in the remote-value ring
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
@@ -223,6 +223,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][kBsThreads] remote values
     X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
+    __shared__ int done_cluster;                        // done_step as published to the cluster
     const int t = threadIdx.x;
     const unsigned rank = bs_cluster_rank(), ncl = bs_cluster_size();
     if ((int)ncl != A.cl) {   // the push targets assume clusters of A.cl CTAs
@@ -241,7 +242,10 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             const int q = atomicAdd(A.ticket, 1);
             for (unsigned r = 0; r < ncl; r++) bs_peer_store(bs_peer(&blk_sh, r), q);
         }
-        if (t == 0) done_step = -1;
+        if (t == 0) {
+            done_step = -1;
+            done_cluster = -1;
+        }
         for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = Pending<X>::value();
         bs_cluster_sync();
         const int q = blk_sh;
@@ -267,6 +271,28 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         cp_async_wait<0>();
         __syncthreads();
 
+        if (t >= kBsThreads + 32 * kBsFetchWarps) {
+            // ---- publisher warp: relays the solver threads' progress to the cluster (a release at
+            // cluster scope waits for earlier memory operations; here it stalls no solver thread)
+            if (ncl > 1 && rank > 0) {
+                int last = -1, spins = 0;
+                while (last < ns - 1) {
+                    const int v = bs_ld_acquire(&done_step);
+                    if (v != last) {
+                        bs_st_release_cluster(&done_cluster, v);
+                        last = v;
+                        spins = 0;
+                    } else {
+                        if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
+                            atomicOr(A.err, DEV_ERR_TIMEOUT);
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                }
+            }
+            continue;   // to the block-end barrier
+        }
         if (!solver) {
             // ---- fetcher warps: warp w takes steps w, w+4, w+8, ... one at a time, polling the
             // step's remote values (four rows per lane) until all are deposited; the remote rows of
@@ -364,7 +390,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // the next block's CTA (the next rank of this cluster): its ring and its published progress
         const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
         const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
-        const uint32_t next_done = has_next ? bs_peer(&done_step, rank + 1) : 0u;
+        const uint32_t next_done = has_next ? bs_peer(&done_cluster, rank + 1) : 0u;
         int next_seen = -1;   // the next block's done_step as last read by this thread
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
@@ -389,13 +415,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 volatile X *e = vrbuf + (s & (kBsF - 1)) * kBsThreads + t;
                 X rv = *e;
                 if (k0 >= 0) {
-                    if (Pending<X>::is(rv)) rv = remote_wait(e, code[k0]);
+                    const int c0 = (k0 == 0) ? code[0] : (k0 == 1 ? code[1] : code[2]);
+                    if (Pending<X>::is(rv)) rv = remote_wait(e, c0);
                     *e = Pending<X>::value();
                 }
 #pragma unroll
                 for (int k = 0; k < kBsInline; k++)
                     if (k == k0) xv[k] = rv;
-                if (k0 >= 0 && k0 < kBsInline - 1 && (code[k0 + 1 < kBsInline ? k0 + 1 : 0] | code[kBsInline - 1]) < 0) {
+                if ((code[0] < 0) + (code[1] < 0) + (code[2] < 0) > 1) {
 #pragma unroll
                     for (int k = 0; k < kBsInline; k++)
                         if (k > k0 && code[k] < 0) xv[k] = wait_value(out + (-code[k] - 1), A.err);
@@ -440,8 +467,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
                            // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
                 named_bar_sync(1, kBsThreads);
-                if (t == 0 && s - last_pub >= 8) {
-                    bs_st_release_cluster(&done_step, s);
+                if (t == 0 && (s - last_pub >= 8 || s == ns - 1)) {
+                    bs_st_release(&done_step, s);
                     last_pub = s;
                 }
             }
