@@ -43,7 +43,7 @@ constexpr int kBsInline = 3;      // dependencies carried in a row packet; more 
 // value pieces per packet (NV) and packet-ring depth in steps (D, a power of two)
 template <typename V> struct BsCfg;
 template <> struct BsCfg<double> { static constexpr int NV = 3, D = 4; };
-template <> struct BsCfg<float> { static constexpr int NV = 1, D = 8; };
+template <> struct BsCfg<float> { static constexpr int NV = 2, D = 8; };
 template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 8; };
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
@@ -54,7 +54,7 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
     return (int)((unsigned)slot | ((unsigned)nd << 15) | ((unsigned)bar << 31));
 }
 
-inline int bs_nv(int vsize) { return vsize == 8 ? 3 : 1; }
+inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
 constexpr int kBsMaxCluster = 8;   // portable thread-block cluster size
 
 // shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
@@ -66,10 +66,11 @@ constexpr size_t bs_smem_bytes(int R) {
 }
 
 // One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
-//   FP64 {v0, v1} {v2, RN(1/d)} {d, push, 0};  FP32 {v0, v1, v2, dv};  BF16 {v0 | v1 << 16, v2, dv, push}
+//   FP64 {v0, v1} {v2, RN(1/d)} {d, push, 0};  FP32 {v0, v1, v2, dv} {push, 0, 0, 0};
+//   BF16 {v0 | v1 << 16, v2, dv, push}
 // dv is the FP32 diagonal (divided by) or the FP32 reciprocal of an FP64 pivot (multiplied by).
 // push: where the row's value goes in the next block's remote ring (consumer step << 7 | thread),
-// or -1 (the FP32 store is solved without clusters and carries none).
+// or -1.
 template <typename V> struct BsRow;
 template <> struct BsRow<double> {
     double v[3], d, dinv;
@@ -94,7 +95,7 @@ template <> struct BsRow<float> {
         v[1] = a.y;
         v[2] = a.z;
         d = a.w;
-        push = -1;
+        push = p[kBsThreads].x;
     }
 };
 template <> struct BsRow<uint16_t> {
@@ -524,6 +525,7 @@ __global__ void bs_pack_kernel<float>(long npk, const int *__restrict__ map3, co
         const int dm = dv_map[i], r = dv_row[i];
         const float dv = piv ? (float)(1.0 / piv[r]) : (dm >= 0 ? src[dm] : 1.0f);
         ((float4 *)pkv)[i] = make_float4(v[0], v[1], v[2], dv);
+        pkv[npk + i] = make_int4(push[i], 0, 0, 0);
     }
 }
 
@@ -570,12 +572,8 @@ void BlockSolve::release() {
 }
 
 // Largest portable cluster size (8, 4, 2) at which at least one cluster of the block-solve CTAs
-// fits on the device, or 1.  HGB_BS_CLUSTER=1 turns clusters off (for comparisons).  The 32768-row
-// blocks of the FP32 / BF16 stores run without clusters: measured on GB300 at 128^3, the pushes
-// slowed the producing CTAs more than they shortened the hops (0.82 vs 0.80 ms per apply), while
-// the FP64 store gains 0.92 vs 1.28 ms.
+// fits on the device, or 1.  HGB_BS_CLUSTER=1 turns clusters off (for comparisons).
 static int bs_cluster_plan(hgb_ctx *c, int R) {
-    if (R > 16384) return 1;
     const char *e = getenv("HGB_BS_CLUSTER");
     const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
     auto fits = [&](auto kernel, size_t smem, int cl) {

@@ -3,6 +3,8 @@
 
 #include "hgb_internal.cuh"
 
+#include <cstdlib>
+
 namespace hgb {
 
 struct BlockSolve {
@@ -23,8 +25,13 @@ struct BlockSolve {
     void release();
 };
 
-// rows per block: the block's solution slice (128 KB) lives in shared memory
-inline int bsolve_rows(int xsize) { return xsize == 8 ? 16384 : 32768; }
+// rows per block: the block's solution slice lives in shared memory (128 KB for FP64).
+// HGB_BS_ROWS32 sets the rows of the FP32 / BF16 stores' blocks (16384 or 32768).
+inline int bsolve_rows(int xsize) {
+    if (xsize == 8) return 16384;
+    const char *e = getenv("HGB_BS_ROWS32");
+    return (e && atoi(e) == 32768) ? 32768 : 16384;
+}
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
                    int rev, int R, BlockSolve &S);
