@@ -18,9 +18,12 @@
 // value in a shared-memory ring as soon as it is ready.  A solver thread therefore waits on
 // shared memory, not on an L2 round trip, when it needs a value from the block before.  The
 // launch groups the CTAs into thread-block clusters that take consecutive blocks: inside a
-// cluster, the CTA of block b writes each value that block b+1 needs first straight into the
-// ring of block b+1's CTA (distributed shared memory, st.shared::cluster), so most hops between
-// blocks skip L2 altogether; the fetchers serve the hop into a cluster's first block.  Entries
+// cluster, the CTA of block b also offers each value that block b+1 needs first straight to the
+// ring of block b+1's CTA (a compare-and-swap in distributed shared memory), so most hops between
+// blocks skip the L2 round trip.  Ring entries hold a NaN pattern tagged with the step they wait
+// for; a deposit (offered value or fetched one) replaces exactly that pattern, so an offer that
+// comes too early or too late is dropped and the fetchers deliver the value instead: the offers
+// never wait and never decide correctness.  Entries
 // keep the reference's accumulation order within each row, so results are bit-identical to the
 // sequential loops of apply_ilu_array / sparse_trsv_array (sparse/hala_sparse_utils.hpp).
 #include "hgb_internal.cuh"
@@ -35,7 +38,7 @@ namespace hgb {
 
 constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
-constexpr int kBsCta = kBsThreads + 32 * (kBsFetchWarps + 1);   // + a publisher warp
+constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
 constexpr int kBsF = 32;          // steps in the remote-value ring
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
@@ -165,9 +168,6 @@ __device__ __forceinline__ int bs_ld_acquire(const int *p) {
 __device__ __forceinline__ void bs_st_release(int *p, int v) {
     asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
 }
-__device__ __forceinline__ void bs_st_release_cluster(int *p, int v) {
-    asm volatile("st.release.cluster.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
-}
 // thread-block cluster: rank, size, barrier over all its threads, peer shared-memory access
 __device__ __forceinline__ unsigned bs_cluster_rank() {
     unsigned r;
@@ -190,22 +190,39 @@ __device__ __forceinline__ uint32_t bs_peer(const void *local, unsigned rank) {
 __device__ __forceinline__ void bs_peer_store(uint32_t a, int v) {
     asm volatile("st.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
-__device__ __forceinline__ void bs_peer_store(uint32_t a, float v) {
-    asm volatile("st.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(__float_as_uint(v)) : "memory");
-}
-__device__ __forceinline__ void bs_peer_store(uint32_t a, double v) {
-    asm volatile("st.shared::cluster.b64 [%0], %1;" ::"r"(a), "l"(__double_as_longlong(v)) : "memory");
-}
-__device__ __forceinline__ int bs_peer_load_acquire(uint32_t a) {
-    int v;
-    asm volatile("ld.acquire.cluster.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
-    return v;
-}
 // a timed-out wait anywhere in the launch ends this one too (checked every 256 polls)
 __device__ __forceinline__ bool bs_give_up(int spins, int *err) {
     return spins > kSpinLimit || ((spins & 255) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT));
 }
 constexpr int kBsSpinLimitSleeping = 1 << 22;   // polls with a 128 ns sleep: about half a second
+
+// Remote-ring entries: a signalling-NaN pattern tagged with the step whose value the entry awaits
+// (arithmetic never produces signalling NaNs, and solver outputs are canonicalised).
+template <typename X> struct RingTag;
+template <> struct RingTag<double> {
+    using U = unsigned long long;
+    __device__ static U tag(int s) { return 0x7FF4BEEF00000000ull | (unsigned)s; }
+    __device__ static bool is(double v) { return ((U)__double_as_longlong(v) >> 32) == 0x7FF4BEEFull; }
+    __device__ static U bits(double v) { return (U)__double_as_longlong(v); }
+    __device__ static double val(U b) { return __longlong_as_double((long long)b); }
+};
+template <> struct RingTag<float> {
+    using U = unsigned;
+    __device__ static U tag(int s) { return 0x7FA00000u | ((unsigned)s & 0x1FFFFFu); }
+    __device__ static bool is(float v) { return (__float_as_uint(v) & 0xFFE00000u) == 0x7FA00000u; }
+    __device__ static U bits(float v) { return __float_as_uint(v); }
+    __device__ static float val(U b) { return __uint_as_float(b); }
+};
+__device__ __forceinline__ unsigned long long bs_peer_cas(uint32_t a, unsigned long long expect, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.shared::cluster.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "r"(a), "l"(expect), "l"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned bs_peer_cas(uint32_t a, unsigned expect, unsigned v) {
+    unsigned old;
+    asm volatile("atom.shared::cluster.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(a), "r"(expect), "r"(v) : "memory");
+    return old;
+}
 
 // MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
@@ -223,7 +240,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][kBsThreads] remote values
     X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
-    __shared__ int done_cluster;                        // done_step as published to the cluster
     const int t = threadIdx.x;
     const unsigned rank = bs_cluster_rank(), ncl = bs_cluster_size();
     if ((int)ncl != A.cl) {   // the push targets assume clusters of A.cl CTAs
@@ -242,11 +258,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             const int q = atomicAdd(A.ticket, 1);
             for (unsigned r = 0; r < ncl; r++) bs_peer_store(bs_peer(&blk_sh, r), q);
         }
-        if (t == 0) {
-            done_step = -1;
-            done_cluster = -1;
-        }
-        for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = Pending<X>::value();
+        if (t == 0) done_step = -1;
+        for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = RingTag<X>::val(RingTag<X>::tag(i / kBsThreads));
         bs_cluster_sync();
         const int q = blk_sh;
         if (q * (int)ncl >= A.nblk) break;   // the same for the whole cluster
@@ -271,28 +284,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         cp_async_wait<0>();
         __syncthreads();
 
-        if (t >= kBsThreads + 32 * kBsFetchWarps) {
-            // ---- publisher warp: relays the solver threads' progress to the cluster (a release at
-            // cluster scope waits for earlier memory operations; here it stalls no solver thread)
-            if (ncl > 1 && rank > 0) {
-                int last = -1, spins = 0;
-                while (last < ns - 1) {
-                    const int v = bs_ld_acquire(&done_step);
-                    if (v != last) {
-                        bs_st_release_cluster(&done_cluster, v);
-                        last = v;
-                        spins = 0;
-                    } else {
-                        if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) {
-                            atomicOr(A.err, DEV_ERR_TIMEOUT);
-                            break;
-                        }
-                        __nanosleep(64);
-                    }
-                }
-            }
-            continue;   // to the block-end barrier
-        }
         if (!solver) {
             // ---- fetcher warps: warp w takes steps w, w+4, w+8, ... one at a time, polling the
             // step's remote values (four rows per lane) until all are deposited; the remote rows of
@@ -320,11 +311,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     }
                     __nanosleep(128);
                 }
-                volatile X *slot = vrbuf + (s & (kBsF - 1)) * kBsThreads + l;
+                X *slot = rbuf + (s & (kBsF - 1)) * kBsThreads + l;
+                volatile X *vslot = slot;
+                using U = typename RingTag<X>::U;
+                const U want = RingTag<X>::tag(s);
                 unsigned todo = 0;
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (jq[q] >= 0) todo |= 1u << q;
+                for (int q = 0; q < 4; q++)   // rows whose value the block before has not offered yet
+                    if (jq[q] >= 0 && RingTag<X>::bits(vslot[32 * q]) == want) todo |= 1u << q;
                 spins = 0;
                 while (todo) {
                     X v[4];
@@ -335,7 +329,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 #pragma unroll
                     for (int q = 0; q < 4; q++)
                         if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
-                            slot[32 * q] = v[q];
+                            atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(v[q]));
                             todo &= ~(1u << q);
                         }
                     if (!todo) break;
@@ -345,7 +339,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                         atomicOr(A.err, DEV_ERR_TIMEOUT);
 #pragma unroll
                         for (int q = 0; q < 4; q++)
-                            if (todo & (1u << q)) slot[32 * q] = Pending<X>::canon(Pending<X>::value());
+                            if (todo & (1u << q))
+                                atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(Pending<X>::canon(Pending<X>::value())));
                         todo = 0;
                     }
                 }
@@ -380,18 +375,16 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         auto remote_wait = [&](volatile X *e, int cd) -> X {
             int spins = 0;
             X v = *e;
-            while (Pending<X>::is(v)) {
+            while (RingTag<X>::is(v)) {
                 if (bs_give_up(++spins, A.err)) return wait_value(out + (-cd - 1), A.err);
                 v = *e;
             }
             return v;
         };
-        int last_pub = -1;   // thread 0: the last step published to the fetchers and the cluster
-        // the next block's CTA (the next rank of this cluster): its ring and its published progress
+        int last_pub = -1;   // thread 0: the last step published to the fetchers
+        // the next block's CTA (the next rank of this cluster): its remote ring
         const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
         const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
-        const uint32_t next_done = has_next ? bs_peer(&done_cluster, rank + 1) : 0u;
-        int next_seen = -1;   // the next block's done_step as last read by this thread
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
@@ -416,9 +409,9 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 X rv = *e;
                 if (k0 >= 0) {
                     const int c0 = (k0 == 0) ? code[0] : (k0 == 1 ? code[1] : code[2]);
-                    if (Pending<X>::is(rv)) rv = remote_wait(e, c0);
-                    *e = Pending<X>::value();
+                    if (RingTag<X>::is(rv)) rv = remote_wait(e, c0);
                 }
+                *e = RingTag<X>::val(RingTag<X>::tag(s + kBsF));   // the entry's next use
 #pragma unroll
                 for (int k = 0; k < kBsInline; k++)
                     if (k == k0) xv[k] = rv;
@@ -450,24 +443,17 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 st_relaxed(outb + sl, acc);
                 if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
-                    // the next block reads this value first: write it into that CTA's ring once it
-                    // has released the slot (its step push_step - kBsF is done)
+                    // the next block reads this value first: offer it to that CTA's ring (taken only
+                    // if the entry awaits exactly that step; otherwise the fetchers deliver it)
                     const int ps = rw.push >> 7, pt = rw.push & 127;
-                    int spins = 0;
-                    while (next_seen < ps - kBsF) {
-                        next_seen = bs_peer_load_acquire(next_done);
-                        if (next_seen < ps - kBsF && bs_give_up(++spins, A.err)) {
-                            atomicOr(A.err, DEV_ERR_TIMEOUT);
-                            break;
-                        }
-                    }
-                    bs_peer_store(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)), acc);
+                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
+                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
                            // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
                 named_bar_sync(1, kBsThreads);
-                if (t == 0 && (s - last_pub >= 8 || s == ns - 1)) {
+                if (t == 0 && s - last_pub >= 8) {
                     bs_st_release(&done_step, s);
                     last_pub = s;
                 }
@@ -713,15 +699,13 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         p0 = p1;
     }
     // Push targets.  Blocks are grouped in runs of cl (one thread-block cluster each); inside a
-    // run, the value that a row of block b+1 needs first from block b is written by block b's CTA
-    // straight into block b+1's ring (consumer step << 7 | consumer thread).  A producer row feeds
-    // at most one consumer row; further ones stay with the fetchers.  The producer steps must not
-    // decrease along the consumer steps (then a producer waiting for ring space can never wait on
-    // itself); a pair of blocks that breaks this keeps the fetchers.
+    // run, the value that a row of block b+1 needs first from block b is offered by block b's CTA
+    // straight to block b+1's ring (consumer step << 7 | consumer thread).  A producer row offers
+    // to at most one consumer row.  The fetchers still cover every row (offers only save time).
     const int cl = bs_cluster_plan(c, R);
     std::vector<int> push(pk0.size(), -1);
     if (cl > 1) {
-        std::vector<int> pk_of_row(n, -1), blk_of_row(n, -1), step_of_pk(pk0.size(), 0);
+        std::vector<int> pk_of_row(n, -1), blk_of_row(n, -1);
         for (int bb = 0; bb < (int)blk.size(); bb++)
             for (int st = blk[bb].x; st < blk[bb].y; st++)
                 for (int t = 0; t < desc[st].y; t++) {
@@ -729,35 +713,16 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     const int row = blk[bb].z + (pk0[pkt].w & 0x7FFF);
                     pk_of_row[row] = pkt;
                     blk_of_row[row] = bb;
-                    step_of_pk[pkt] = st - blk[bb].x;
                 }
-        std::vector<std::pair<int, int>> planned;   // (consumer packet, producer packet)
         for (int bb = 1; bb < (int)blk.size(); bb++) {
             if (bb / cl != (bb - 1) / cl) continue;
-            planned.clear();
-            int prev_max = -1;
-            bool monotone = true;
-            for (int st = blk[bb].x; st < blk[bb].y && monotone; st++) {
-                int smin = INT_MAX, smax = -1;
+            for (int st = blk[bb].x; st < blk[bb].y; st++)
                 for (int t = 0; t < desc[st].y; t++) {
                     const int cp = desc[st].x + t, j = rj[cp];
                     if (j < 0 || blk_of_row[j] != bb - 1) continue;
                     const int pp = pk_of_row[j];
-                    if (push[pp] >= 0) continue;
-                    push[pp] = ((st - blk[bb].x) << 7) | t;
-                    planned.push_back({cp, pp});
-                    smin = std::min(smin, step_of_pk[pp]);
-                    smax = std::max(smax, step_of_pk[pp]);
+                    if (push[pp] < 0) push[pp] = ((st - blk[bb].x) << 7) | t;
                 }
-                if (smax >= 0) {
-                    if (smin < prev_max) monotone = false;
-                    prev_max = std::max(prev_max, smax);
-                }
-            }
-            for (auto &pc : planned) {
-                if (monotone) rj[pc.first] = -1;     // pushed: the fetchers skip it
-                else push[pc.second] = -1;
-            }
         }
     }
     S.release();
