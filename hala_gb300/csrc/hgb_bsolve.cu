@@ -40,6 +40,7 @@ constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
 constexpr int kBsF = 32;          // steps in the remote-value ring
+constexpr int kBsOfferTries = 24; // retries of an offer to the next block's ring (128 ns apart)
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
@@ -444,10 +445,19 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
-                    // if the entry awaits exactly that step; otherwise the fetchers deliver it)
+                    // if the entry awaits exactly that step).  While the entry still serves the step
+                    // kBsF earlier, the next block is running behind: retry for a few microseconds
+                    // (that keeps the two blocks in step); after that the fetchers deliver it.
+                    using U = typename RingTag<X>::U;
                     const int ps = rw.push >> 7, pt = rw.push & 127;
-                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
-                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
+                    const uint32_t a = next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X));
+                    const U want = RingTag<X>::tag(ps), before = RingTag<X>::tag(ps - kBsF);
+                    U old = bs_peer_cas(a, want, RingTag<X>::bits(acc));
+                    for (int tries = 0; old != want && tries < kBsOfferTries; tries++) {
+                        if (old != before && RingTag<X>::is(RingTag<X>::val(old))) break;
+                        __nanosleep(128);
+                        old = bs_peer_cas(a, want, RingTag<X>::bits(acc));
+                    }
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
