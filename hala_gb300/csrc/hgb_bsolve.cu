@@ -40,7 +40,8 @@ constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
 constexpr int kBsF = 32;          // steps in the remote-value ring
-constexpr int kBsOfferTries = 24; // retries of an offer to the next block's ring (128 ns apart)
+constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on its ring entry before
+                                             // reading the value from L2 itself
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
@@ -373,11 +374,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         };
         // the first remote dependency of this thread's row of step s, once the fetchers' ring
         // entry e showed the pending pattern: wait for the deposit (bounded, then read directly)
+        // (an offer that was dropped, or a slow fetcher, costs at most kBsDirectAfter cycles: then
+        // the thread reads the value from L2 itself)
         auto remote_wait = [&](volatile X *e, int cd) -> X {
-            int spins = 0;
+            const long long t0 = clock64();
             X v = *e;
             while (RingTag<X>::is(v)) {
-                if (bs_give_up(++spins, A.err)) return wait_value(out + (-cd - 1), A.err);
+                if (clock64() - t0 > kBsDirectAfter) return wait_value(out + (-cd - 1), A.err);
                 v = *e;
             }
             return v;
@@ -445,19 +448,10 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
-                    // if the entry awaits exactly that step).  While the entry still serves the step
-                    // kBsF earlier, the next block is running behind: retry for a few microseconds
-                    // (that keeps the two blocks in step); after that the fetchers deliver it.
-                    using U = typename RingTag<X>::U;
+                    // if the entry awaits exactly that step; the result is not waited for)
                     const int ps = rw.push >> 7, pt = rw.push & 127;
-                    const uint32_t a = next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X));
-                    const U want = RingTag<X>::tag(ps), before = RingTag<X>::tag(ps - kBsF);
-                    U old = bs_peer_cas(a, want, RingTag<X>::bits(acc));
-                    for (int tries = 0; old != want && tries < kBsOfferTries; tries++) {
-                        if (old != before && RingTag<X>::is(RingTag<X>::val(old))) break;
-                        __nanosleep(128);
-                        old = bs_peer_cas(a, want, RingTag<X>::bits(acc));
-                    }
+                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
+                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
@@ -711,7 +705,8 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     // Push targets.  Blocks are grouped in runs of cl (one thread-block cluster each); inside a
     // run, the value that a row of block b+1 needs first from block b is offered by block b's CTA
     // straight to block b+1's ring (consumer step << 7 | consumer thread).  A producer row offers
-    // to at most one consumer row.  The fetchers still cover every row (offers only save time).
+    // to at most one consumer row.  Offered rows leave the fetchers' lists; an offer that is dropped
+    // (the consumer more than a ring's length behind) is read from L2 by the consumer itself.
     const int cl = bs_cluster_plan(c, R);
     std::vector<int> push(pk0.size(), -1);
     if (cl > 1) {
@@ -731,7 +726,10 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     const int cp = desc[st].x + t, j = rj[cp];
                     if (j < 0 || blk_of_row[j] != bb - 1) continue;
                     const int pp = pk_of_row[j];
-                    if (push[pp] < 0) push[pp] = ((st - blk[bb].x) << 7) | t;
+                    if (push[pp] < 0) {
+                        push[pp] = ((st - blk[bb].x) << 7) | t;
+                        rj[cp] = -1;
+                    }
                 }
         }
     }
