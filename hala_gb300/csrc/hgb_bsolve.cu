@@ -561,12 +561,16 @@ void BlockSolve::release() {
     *this = BlockSolve();
 }
 
-// Largest portable cluster size (8, 4, 2) at which at least one cluster of the block-solve CTAs
-// fits on the device, or 1.  HGB_BS_CLUSTER=1 turns clusters off (for comparisons).
-static int bs_cluster_plan(hgb_ctx *c, int R) {
-    const char *e = getenv("HGB_BS_CLUSTER");
-    const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
-    auto fits = [&](auto kernel, size_t smem, int cl) {
+// Co-resident thread-block clusters of cl block-solve CTAs for blocks of R rows (queried once per
+// device, cluster size and block-size class).  On GB300 one CTA per SM fits, and 15 clusters of 8,
+// 36 of 4 or 76 of 2 are co-resident.
+static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
+    static int cache[64][2][kBsMaxCluster + 1];
+    static bool init[64][2][kBsMaxCluster + 1];
+    const int ri = R <= 16384 ? 0 : 1;
+    if (c->device < 0 || c->device >= 64 || cl < 1 || cl > kBsMaxCluster) return 0;
+    if (init[c->device][ri][cl]) return cache[c->device][ri][cl];
+    auto fits = [&](auto kernel, size_t smem) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
             cudaGetLastError();
             return 0;
@@ -590,12 +594,42 @@ static int bs_cluster_plan(hgb_ctx *c, int R) {
         return n;
     };
     DeviceGuard g(c->device);
+    // the largest shared-memory layout of the class (FP64 / FP32 store; BF16 needs less)
+    const int n = (ri == 0) ? fits(bsolve_kernel<double, double, 0, true, false>, bs_smem_bytes<double, double>(16384))
+                            : fits(bsolve_kernel<float, float, 0, true, false>, bs_smem_bytes<float, float>(32768));
+    cache[c->device][ri][cl] = n;
+    init[c->device][ri][cl] = true;
+    return n;
+}
+
+// Cluster size for nblk blocks of R rows: the largest of 8, 4, 2 whose co-resident clusters hold
+// every block at once (a block waiting for a free cluster starts a whole block-time late); with
+// more blocks than any size holds, 8 (fewest hops through L2).  HGB_BS_CLUSTER caps the size
+// (1: no clusters, for comparisons).
+static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
+    const char *e = getenv("HGB_BS_CLUSTER");
+    const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
+    int best = 1;
     for (int cl = cap; cl > 1; cl /= 2) {
-        const int n = (R <= 16384) ? fits(bsolve_kernel<double, double, 0, true, false>, bs_smem_bytes<double, double>(R), cl)
-                                   : fits(bsolve_kernel<float, float, 0, true, false>, bs_smem_bytes<float, float>(R), cl);
-        if (n >= 1) return cl;
+        const int n = bs_clusters_fit(c, R, cl);
+        if (n < 1) continue;
+        if (best == 1) best = cl;            // largest size that fits at all
+        if (n * cl >= nblk) return cl;       // largest size that holds every block
     }
-    return 1;
+    return best;
+}
+
+// Rows per block.  FP64: 16384 (the slice fills 128 KB).  FP32 / BF16: between 16384 and 32768,
+// as small as lets every block be co-resident in clusters of 8 (smaller blocks have fewer local
+// levels; the hops between them are cheap inside a cluster).  HGB_BS_ROWS32 overrides.
+int bsolve_rows(hgb_ctx *c, int xsize, int n) {
+    if (xsize == 8) return 16384;
+    const char *e = getenv("HGB_BS_ROWS32");
+    if (e && atoi(e) >= 1024) return std::min(32768, atoi(e) / 128 * 128);
+    const int ctas = 8 * bs_clusters_fit(c, 32768, 8);
+    if (ctas <= 0) return 32768;
+    const long want = ((long)n + ctas - 1) / ctas;
+    return (int)std::min<long>(32768, std::max<long>(16384, (want + 127) / 128 * 128));
 }
 
 template <typename T>
@@ -707,7 +741,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     // straight to block b+1's ring (consumer step << 7 | consumer thread).  A producer row offers
     // to at most one consumer row.  Offered rows leave the fetchers' lists; an offer that is dropped
     // (the consumer more than a ring's length behind) is read from L2 by the consumer itself.
-    const int cl = bs_cluster_plan(c, R);
+    const int cl = bs_cluster_plan(c, R, (int)blk.size());
     std::vector<int> push(pk0.size(), -1);
     if (cl > 1) {
         std::vector<int> pk_of_row(n, -1), blk_of_row(n, -1);

@@ -3,8 +3,6 @@
 
 #include "hgb_internal.cuh"
 
-#include <cstdlib>
-
 namespace hgb {
 
 struct BlockSolve {
@@ -25,13 +23,9 @@ struct BlockSolve {
     void release();
 };
 
-// rows per block: the block's solution slice lives in shared memory (128 KB for FP64).
-// HGB_BS_ROWS32 sets the rows of the FP32 / BF16 stores' blocks (16384 or 32768).
-inline int bsolve_rows(int xsize) {
-    if (xsize == 8) return 16384;
-    const char *e = getenv("HGB_BS_ROWS32");
-    return (e && atoi(e) == 32768) ? 32768 : 16384;
-}
+// Rows per block for a solve over n rows with an xsize-byte solution (the block's slice lives in
+// shared memory: at most 16384 FP64 or 32768 FP32 rows).
+int bsolve_rows(hgb_ctx *c, int xsize, int n);
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
                    int rev, int R, BlockSolve &S);
