@@ -602,34 +602,30 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
     return n;
 }
 
-// Cluster size for nblk blocks of R rows: the largest of 8, 4, 2 whose co-resident clusters hold
-// every block at once (a block waiting for a free cluster starts a whole block-time late); with
-// more blocks than any size holds, 8 (fewest hops through L2).  HGB_BS_CLUSTER caps the size
-// (1: no clusters, for comparisons).
+// Cluster size: the largest of 8, 4, 2 at which a cluster fits.  Measured at 128^3 (128 blocks):
+// clusters of 8 (15 co-resident, so the last 8 blocks start when a cluster frees up) beat
+// clusters of 4 (all 128 co-resident, twice the hops through L2): 0.43 vs 0.51 ms per FP32-store
+// apply, 0.83 vs 0.93 ms FP64.  HGB_BS_CLUSTER caps the size (1: no clusters, for comparisons).
 static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
     const char *e = getenv("HGB_BS_CLUSTER");
     const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
-    int best = 1;
-    for (int cl = cap; cl > 1; cl /= 2) {
-        const int n = bs_clusters_fit(c, R, cl);
-        if (n < 1) continue;
-        if (best == 1) best = cl;            // largest size that fits at all
-        if (n * cl >= nblk) return cl;       // largest size that holds every block
-    }
-    return best;
+    if (nblk < 2) return 1;
+    for (int cl = cap; cl > 1; cl /= 2)
+        if (bs_clusters_fit(c, R, cl) >= 1) return cl;
+    return 1;
 }
 
-// Rows per block.  FP64: 16384 (the slice fills 128 KB).  FP32 / BF16: between 16384 and 32768,
-// as small as lets every block be co-resident in clusters of 8 (smaller blocks have fewer local
-// levels; the hops between them are cheap inside a cluster).  HGB_BS_ROWS32 overrides.
+// Rows per block: 16384 (the FP64 slice fills 128 KB).  For natural-ordered grids whose planes
+// hold 16384 rows this puts one plane in a block; blocks that cut planes make a block's first
+// local levels wait for the previous block's last ones, which serialises the wavefront.
+// HGB_BS_ROWS32 sets the FP32 / BF16 block rows (up to 32768) for comparisons.
 int bsolve_rows(hgb_ctx *c, int xsize, int n) {
+    (void)c;
+    (void)n;
     if (xsize == 8) return 16384;
     const char *e = getenv("HGB_BS_ROWS32");
     if (e && atoi(e) >= 1024) return std::min(32768, atoi(e) / 128 * 128);
-    const int ctas = 8 * bs_clusters_fit(c, 32768, 8);
-    if (ctas <= 0) return 32768;
-    const long want = ((long)n + ctas - 1) / ctas;
-    return (int)std::min<long>(32768, std::max<long>(16384, (want + 127) / 128 * 128));
+    return 16384;
 }
 
 template <typename T>
@@ -820,15 +816,20 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
 template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
 static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
     const size_t smem = bs_smem_bytes<V, X>(S.R);
+    // the attribute allows the largest block of the class (16384 FP64 / 32768 FP32 rows), so
+    // solves with smaller blocks launch too
+    const size_t smem_max = bs_smem_bytes<V, X>(sizeof(X) == 8 ? 16384 : 32768);
     static int attr_dev = -1;   // device on which the kernel's shared-memory attribute was set
     if (attr_dev != c->device) {
         int mx = 0;
         HGB_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-        if (smem > (size_t)mx) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem, mx);
+        if (smem_max > (size_t)mx)
+            return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem_max, mx);
         HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+                                      (int)smem_max));
         attr_dev = c->device;
     }
+    if (smem > smem_max) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %d rows per block", S.R);
     if (S.cl <= 1) {
         const int grid = std::max(1, std::min(S.nblk, c->num_sms));
         bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsCta, smem, c->stream>>>(A, alpha, in, out, pend);
