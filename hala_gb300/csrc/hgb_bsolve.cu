@@ -39,23 +39,17 @@ namespace hgb {
 constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
-// Per solution type: steps in the remote-value ring (F) and steps per block (the block's
-// descriptors sit in shared memory).  The FP32 layout fits two CTAs per SM, so that 16 clusters
-// of 8 (128 blocks) are co-resident; FP64 needs the whole SM for its 16384-row slice.
-template <typename X> struct BsShape;
-template <> struct BsShape<double> { static constexpr int F = 32, StepCap = 1024; };
-template <> struct BsShape<float> { static constexpr int F = 16, StepCap = 512; };
-inline int bs_step_cap(int xsize) { return xsize == 8 ? BsShape<double>::StepCap : BsShape<float>::StepCap; }
-inline int bs_ring_steps(int xsize) { return xsize == 8 ? BsShape<double>::F : BsShape<float>::F; }
+constexpr int kBsF = 32;          // steps in the remote-value ring
 constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on its ring entry before
                                              // reading the value from L2 itself
+constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
 // value pieces per packet (NV) and packet-ring depth in steps (D, a power of two)
 template <typename V> struct BsCfg;
 template <> struct BsCfg<double> { static constexpr int NV = 3, D = 4; };
-template <> struct BsCfg<float> { static constexpr int NV = 2, D = 4; };
-template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 4; };
+template <> struct BsCfg<float> { static constexpr int NV = 2, D = 8; };
+template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 8; };
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
 // dependencies (kBsIdle: no row for this thread in this step), bit 31 set on the last step of a
@@ -69,11 +63,11 @@ inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
 constexpr int kBsMaxCluster = 8;   // portable thread-block cluster size
 
 // shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
-//                 remote-value ring F x 128 | solution slice + zero slot]
+//                 remote-value ring kBsF x 128 | solution slice + zero slot]
 template <typename V, typename X>
 constexpr size_t bs_smem_bytes(int R) {
-    return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)BsShape<X>::StepCap * 16 +
-           (size_t)BsShape<X>::F * kBsThreads * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
+    return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)kBsStepCap * 16 +
+           (size_t)kBsF * kBsThreads * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
 }
 
 // One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
@@ -239,7 +233,6 @@ template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
 __global__ void __launch_bounds__(kBsCta, 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, NP = 1 + NV;
-    constexpr int kBsF = BsShape<X>::F, kBsStepCap = BsShape<X>::StepCap;
     static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
     static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps, "remote ring shape");
     if (A.skip && *A.skip) return;
@@ -461,10 +454,10 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                                 RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
-            if (w < 0) {   // end of a level (or of F/2 steps of one): publish it to the solver threads,
-                           // and to the fetchers when F/4 steps have passed (they lag by < 3F/4 steps)
+            if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
+                           // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
                 named_bar_sync(1, kBsThreads);
-                if (t == 0 && s - last_pub >= kBsF / 4) {
+                if (t == 0 && s - last_pub >= 8) {
                     bs_st_release(&done_step, s);
                     last_pub = s;
                 }
@@ -645,8 +638,7 @@ static int upload(T **dst, const std::vector<T> &src) {
 // Host-side analysis: blocks, local levels, steps and the packets (structure only; the values are
 // gathered on the device through map3 / dv_map / dv_row / ovf_map).
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
-                   int rev, int R, int xsize, BlockSolve &S) {
-    const int kBsStepCap = bs_step_cap(xsize), kBarEvery = bs_ring_steps(xsize) / 2;
+                   int rev, int R, BlockSolve &S) {
     std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(std::max(n, 1));
     HGB_CUDA(cudaMemcpyAsync(pntr.data(), pntr_d, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
     if (nnz > 0)
@@ -702,9 +694,9 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                 const size_t ob = ovf_codes.size();
                 if (ob + (size_t)kx * nr > (size_t)INT_MAX || pk0.size() + nr > (size_t)INT_MAX)
                     return fail(HGB_ERR_UNSUPPORTED, "block solve: packed arrays exceed 2^31 entries");
-                // a barrier ends every level, and every (F/2)th step inside a long level, so that the
-                // solver threads' progress reaches the fetchers at least every F/2 steps
-                const int bar = (k + nr == start[l + 1] || ((k - start[l]) / kBsThreads) % kBarEvery == kBarEvery - 1) ? 1 : 0;
+                // a barrier ends every level, and every 16th step inside a long level, so that the
+                // solver threads' progress reaches the fetchers at least every 16 steps
+                const int bar = (k + nr == start[l + 1] || ((k - start[l]) / kBsThreads) % 16 == 15) ? 1 : 0;
                 desc.push_back(make_int4((int)pk0.size(), nr, (int)ob, kx | (bar << 16)));
                 ovf_codes.resize(ob + (size_t)kx * nr, 0);
                 ovf_map.resize(ob + (size_t)kx * nr, -1);
