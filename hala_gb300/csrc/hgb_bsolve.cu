@@ -389,6 +389,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // the next block's CTA (the next rank of this cluster): its remote ring
         const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
         const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
+        typename RingTag<X>::U offer_prev = 0, offer_sink = 0;
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
@@ -448,10 +449,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
-                    // if the entry awaits exactly that step; the result is not waited for)
+                    // if the entry awaits exactly that step).  The result is only folded into a sink
+                    // one step later, so the atomic's round trip overlaps the next step and its
+                    // destination register differs from the next offer's
                     const int ps = rw.push >> 7, pt = rw.push & 127;
-                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
-                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
+                    offer_sink ^= offer_prev;
+                    offer_prev = bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
+                                             RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
@@ -464,6 +468,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
         }
         cp_async_wait<0>();
+        offer_sink ^= offer_prev;
+        if (offer_sink == (typename RingTag<X>::U)1) atomicOr(A.err, 0);   // keeps the offers' results live
     }
     // the last CTA to leave resets the ticket for the next launch
     if (t == 0) {
@@ -638,7 +644,7 @@ static int upload(T **dst, const std::vector<T> &src) {
 // Host-side analysis: blocks, local levels, steps and the packets (structure only; the values are
 // gathered on the device through map3 / dv_map / dv_row / ovf_map).
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
-                   int rev, int R, BlockSolve &S) {
+                   int rev, int R, int xsize, BlockSolve &S) {
     std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(std::max(n, 1));
     HGB_CUDA(cudaMemcpyAsync(pntr.data(), pntr_d, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
     if (nnz > 0)
@@ -647,18 +653,32 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     HGB_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<int4> blk, desc, pk0;
     std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj;
-    std::vector<int> lev(R), cnt, start, cur, order;
+    std::vector<int> lev(std::max(R, 32768)), cnt, start, cur, order;
     auto row_of = [&](int pos) { return lower ? pos : n - 1 - pos; };
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
     auto deps = [&](int row, int &a, int &e) {
         a = lower ? pntr[row] : diag[row] + 1;
         e = lower ? diag[row] : pntr[row + 1];
     };
+    // FP32 / BF16 solutions: when there are more blocks of R rows than CTAs co-resident in
+    // clusters of 8, the last ones take 2R rows (the slice still fits), so every block starts at
+    // once; a block that waits for a free cluster would start a whole block-time late
+    int merge_from = n, Rmax = R;
+    if (xsize == 4 && 2 * R <= 32768) {
+        const int ctas = 8 * bs_clusters_fit(c, 32768, 8);
+        const long nb = ((long)n + R - 1) / R;
+        if (ctas > 0 && nb > ctas) {
+            const long m = std::min<long>(nb - ctas, nb / 2);
+            merge_from = (int)std::max<long>(0, (long)n - 2 * m * R);
+            Rmax = 2 * R;
+        }
+    }
     for (int p0 = 0; p0 < n;) {
-        // grow the block in solve order while it fits R rows and kBsStepCap steps
+        // grow the block in solve order while it fits Rb rows and kBsStepCap steps
+        const int Rb = p0 >= merge_from ? Rmax : R;
         cnt.clear();
         int steps = 0, p1 = p0;
-        while (p1 < n && p1 - p0 < R) {
+        while (p1 < n && p1 - p0 < Rb) {
             int a, e;
             deps(row_of(p1), a, e);
             if (e - a >= kBsIdle) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row_of(p1), e - a);
@@ -767,7 +787,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     S.n = n;
     S.nblk = (int)blk.size();
     S.nsteps = (int)desc.size();
-    S.R = R;
+    S.R = Rmax;
     S.cl = cl;
     S.npk = (long)pk0.size();
     S.novf = (long)ovf_codes.size();

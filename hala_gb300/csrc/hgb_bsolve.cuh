@@ -28,7 +28,7 @@ struct BlockSolve {
 int bsolve_rows(hgb_ctx *c, int xsize, int n);
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
-                   int rev, int R, BlockSolve &S);
+                   int rev, int R, int xsize, BlockSolve &S);
 int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, const double *piv);
 template <typename V, typename X>
 int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,

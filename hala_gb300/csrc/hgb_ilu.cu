@@ -583,8 +583,8 @@ static int ilu_build_T(hgb_ilu *M) {
     HGB_TRY(analyse(c, M->n, M->T.pntr, M->T.row, M->diagT, 0, M->UT));
     if (M->use_bs) {
         const int R = bsolve_rows(c, (int)xsize(M->store), M->n);
-        int st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 1, 0, R, M->BLT);
-        if (!st) st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 0, 1, R, M->BUT);
+        int st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 1, 0, R, (int)xsize(M->store), M->BLT);
+        if (!st) st = bsolve_analyse(c, M->n, M->nnz, M->T.pntr, M->T.row, M->diagT, 0, 1, R, (int)xsize(M->store), M->BUT);
         if (!st) st = bsolve_load_values(c, M->BLT, M->svalsT, (int)vsize(M->store), M->piv);
         if (!st) st = bsolve_load_values(c, M->BUT, M->svalsT, (int)vsize(M->store), nullptr);
         if (st == HGB_OK) M->use_bsT = true;
@@ -707,8 +707,8 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
         if (cudaMalloc(&M->tmp, xsize(store) * n) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
         if (ilu_solver_kind() == 0) {
             const int R = bsolve_rows(c, (int)xsize(store), n);
-            int bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 1, 0, R, M->BL);
-            if (!bs) bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 0, 0, R, M->BU);
+            int bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 1, 0, R, (int)xsize(store), M->BL);
+            if (!bs) bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 0, 0, R, (int)xsize(store), M->BU);
             if (!bs) bs = bsolve_load_values(c, M->BL, M->svals, (int)vsize(store), nullptr);
             if (!bs) bs = bsolve_load_values(c, M->BU, M->svals, (int)vsize(store), M->piv);
             if (bs == HGB_OK) M->use_bs = true;

@@ -202,3 +202,20 @@ def test_bounded_wait_times_out_and_context_survives(eng, rng):
     fo, do, _ = O.ilu_factor(p, i, v)
     x = rng.standard_normal(len(p) - 1)
     assert np.array_equal(ilu.apply(T(x)).cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
+
+
+def test_apply_bit_exact_at_bench_size(eng, rng):
+    # the 128^3 workload: 128 one-plane blocks in clusters (the FP32 store's last blocks hold two
+    # planes), both sweeps, 'N' and 'T', against the oracle bit for bit
+    p, i, v = P.aniso3d(128)
+    n = len(p) - 1
+    fo, do, _ = O.ilu_factor(p, i, v)
+    x = rng.standard_normal(n)
+    ilu = E.make_ilu(eng, T(p), T(i), T(v))
+    assert np.array_equal(ilu.apply(T(x)).cpu().numpy(), O.ilu_apply(p, i, do, fo, x))
+    assert np.array_equal(ilu.apply(T(x), trans="T").cpu().numpy(), O.ilu_apply(p, i, do, fo, x, trans="T"))
+    ilu32 = E.make_ilu(eng, T(p), T(i), T(v), store=torch.float32)
+    x32 = x.astype(np.float32)
+    exact = O.ilu_apply_mixed(p, i, do, fo.astype(np.float32), fo[do], x32)
+    for _ in range(2):
+        assert np.array_equal(ilu32.apply(T(x32)).cpu().numpy().view(np.uint32), exact.view(np.uint32))
