@@ -725,7 +725,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     int a, e;
                     deps(row, a, e);
                     const int nd = e - a;
-                    int cd[kBsInline] = {R, R, R}, mp[kBsInline] = {-1, -1, -1};   // padding: the zero slot
+                    int cd[kBsInline] = {Rmax, Rmax, Rmax}, mp[kBsInline] = {-1, -1, -1};   // padding: the zero slot
                     for (int q = 0; q < nd; q++) {
                         const int p = rev ? e - 1 - q : a + q;
                         const int col = indx[p];
