@@ -389,7 +389,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // the next block's CTA (the next rank of this cluster): its remote ring
         const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
         const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
-        typename RingTag<X>::U offer_prev = 0, offer_sink = 0;
         for (int s = 0; s < D - 1; s++) issue(s);
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
@@ -449,13 +448,11 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
-                    // if the entry awaits exactly that step).  The result is only folded into a sink
-                    // one step later, so the atomic's round trip overlaps the next step and its
-                    // destination register differs from the next offer's
+                    // if the entry awaits exactly that step; the result is not read, which measured
+                    // faster than reading it a step later)
                     const int ps = rw.push >> 7, pt = rw.push & 127;
-                    offer_sink ^= offer_prev;
-                    offer_prev = bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
-                                             RingTag<X>::tag(ps), RingTag<X>::bits(acc));
+                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
+                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
@@ -468,8 +465,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             }
         }
         cp_async_wait<0>();
-        offer_sink ^= offer_prev;
-        if (offer_sink == (typename RingTag<X>::U)1) atomicOr(A.err, 0);   // keeps the offers' results live
     }
     // the last CTA to leave resets the ticket for the next launch
     if (t == 0) {
