@@ -648,32 +648,20 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     HGB_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<int4> blk, desc, pk0;
     std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj;
-    std::vector<int> lev(std::max(R, 32768)), cnt, start, cur, order;
+    std::vector<int> lev(R), cnt, start, cur, order;
     auto row_of = [&](int pos) { return lower ? pos : n - 1 - pos; };
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
     auto deps = [&](int row, int &a, int &e) {
         a = lower ? pntr[row] : diag[row] + 1;
         e = lower ? diag[row] : pntr[row + 1];
     };
-    // FP32 / BF16 solutions: when there are more blocks of R rows than CTAs co-resident in
-    // clusters of 8, the last ones take 2R rows (the slice still fits), so every block starts at
-    // once; a block that waits for a free cluster would start a whole block-time late
-    int merge_from = n, Rmax = R;
-    if (xsize == 4 && 2 * R <= 32768) {
-        const int ctas = 8 * bs_clusters_fit(c, 32768, 8);
-        const long nb = ((long)n + R - 1) / R;
-        if (ctas > 0 && nb > ctas) {
-            const long m = std::min<long>(nb - ctas, nb / 2);
-            merge_from = (int)std::max<long>(0, (long)n - 2 * m * R);
-            Rmax = 2 * R;
-        }
-    }
+    (void)xsize;   // the block layout is the same for every solution type
+    const int Rmax = R;
     for (int p0 = 0; p0 < n;) {
-        // grow the block in solve order while it fits Rb rows and kBsStepCap steps
-        const int Rb = p0 >= merge_from ? Rmax : R;
+        // grow the block in solve order while it fits R rows and kBsStepCap steps
         cnt.clear();
         int steps = 0, p1 = p0;
-        while (p1 < n && p1 - p0 < Rb) {
+        while (p1 < n && p1 - p0 < R) {
             int a, e;
             deps(row_of(p1), a, e);
             if (e - a >= kBsIdle) return fail(HGB_ERR_UNSUPPORTED, "row %d has %d dependencies", row_of(p1), e - a);

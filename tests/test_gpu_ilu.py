@@ -205,8 +205,8 @@ def test_bounded_wait_times_out_and_context_survives(eng, rng):
 
 
 def test_apply_bit_exact_at_bench_size(eng, rng):
-    # the 128^3 workload: 128 one-plane blocks in clusters (the FP32 store's last blocks hold two
-    # planes), both sweeps, 'N' and 'T', against the oracle bit for bit
+    # the 128^3 workload: 128 one-plane blocks in clusters of 8 (more than are co-resident), both
+    # sweeps, 'N' and 'T', against the oracle bit for bit
     p, i, v = P.aniso3d(128)
     n = len(p) - 1
     fo, do, _ = O.ilu_factor(p, i, v)
