@@ -171,6 +171,12 @@ class gpu_sparse_matrix:
         check(_h.lib().hgb_csr_gemv(self.h, ch_(trans), float(alpha), _p(x), float(beta), _p(y)), "gemv")
         return y
 
+    def gemm(self, nrhs, alpha, x, beta, y):
+        """Y = alpha A X + beta Y for n x nrhs column-major blocks (sparse_gemm 'N','N')."""
+        check(_h.lib().hgb_csr_gemm(self.h, int(nrhs), float(alpha), _p(x), self.cols, float(beta), _p(y),
+                                    self.rows), "gemm")
+        return y
+
     def gemv_dot(self, x, y, dot_out):
         """y = A x and dot_out[0] = <x, y> (device scalar, float64 tensor)."""
         check(_h.lib().hgb_csr_gemv_dot(self.h, _p(x), _p(y), _p(dot_out)), "gemv_dot")
@@ -217,6 +223,12 @@ class gpu_ilu:
     def apply(self, x, r=None, trans="N"):
         r = torch.empty_like(x) if r is None else r
         check(_h.lib().hgb_ilu0_apply(self.h, ch_(trans), _p(x), _p(r)), "ilu apply")
+        return r
+
+    def apply_nrhs(self, x, nrhs, r=None, trans="N"):
+        """apply(x, r, num_rhs): nrhs column-major right-hand sides."""
+        r = torch.empty_like(x) if r is None else r
+        check(_h.lib().hgb_ilu0_apply_nrhs(self.h, ch_(trans), int(nrhs), _p(x), _p(r)), "ilu apply nrhs")
         return r
 
     def factor(self):
@@ -304,6 +316,29 @@ def solve_cg_ilu(engine, stop, pntr, indx, vals, b, x, ilu=None, policy="N"):
     """solve_cg_ilu: factorises on the fly when no ILU is given (hala_solvers_cg.hpp:359-369)."""
     ilu = ilu or make_ilu(engine, pntr, indx, vals, policy)
     return solve_cg(engine, stop, pntr, indx, vals, b, x, ilu=ilu)
+
+
+def sparse_gemm(A, nrhs, alpha, x, beta, y):
+    return A.gemm(nrhs, alpha, x, beta, y)
+
+
+def solve_batch_cg(engine, stop, pntr, indx, vals, B, X, ilu=None, matrix=None):
+    """solve_batch_cg / solve_batch_cg_ilu(gpu_engine, ...), hex/solvers/hala_solvers_cg_batch.hpp:
+    B, X hold nrhs = B.numel() / n column-major right-hand sides; all columns iterate together until
+    the largest column residual is below stop.tol.  Returns the iteration count; X in place."""
+    s = _stop(stop)
+    n = pntr.numel() - 1
+    nrhs = B.numel() // n
+    A = matrix or gpu_sparse_matrix(engine, n, pntr, indx, vals)
+    info = SolveInfo()
+    check(_h.lib().hgb_cg_solve_nrhs(engine.h, A.h, ilu.h if ilu else None, nrhs, _p(B), _p(X), s.tol, s.max_iter,
+                                     C.byref(info)), "solve_batch_cg")
+    return info.iterations
+
+
+def solve_batch_cg_ilu(engine, stop, pntr, indx, vals, B, X, ilu=None, policy="N"):
+    ilu = ilu or make_ilu(engine, pntr, indx, vals, policy)
+    return solve_batch_cg(engine, stop, pntr, indx, vals, B, X, ilu=ilu)
 
 
 def solve_cg_info(engine, A, ilu, b, x, tol, max_iter=INT_MAX):

@@ -74,6 +74,9 @@ _SIGS = {
     "hgb_cg_solve": ([vp, vp, vp, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_ir_pcg_solve": ([vp, vp, vp, vp, vp, vp, f64, f64, i32, i32, C.POINTER(SolveInfo)], i32),
     "hgb_cg_solve_op": ([vp, vp, vp, ch, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
+    "hgb_csr_gemm": ([vp, i32, f64, vp, i32, f64, vp, i32], i32),
+    "hgb_ilu0_apply_nrhs": ([vp, ch, i32, vp, vp], i32),
+    "hgb_cg_solve_nrhs": ([vp, vp, vp, i32, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_ir_pcg_solve_op": ([vp, vp, vp, vp, ch, vp, vp, f64, f64, i32, i32, C.POINTER(SolveInfo)], i32),
     "hgb_csr_pattern_grad": ([vp, f64, vp, vp, vp], i32),
     "hgb_gmres_solve": ([vp, vp, vp, i32, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),

@@ -12,6 +12,7 @@
  *   dot / norm2 / axpy / scal / vcopy / set_zero   gpu/hala_gpu_blas1.hpp, engine.hpp:336
  *   stop_criteria         hex/solvers/hala_solvers_core.hpp:52-70
  *   solve_cg / solve_cg_ilu / solve_gmres_ilu   hex/solvers/hala_solvers_cg.hpp, _gmres.hpp
+ *   solve_batch_cg_ilu                          hex/solvers/hala_solvers_cg_batch.hpp
  *   mixed_engine          wax/hala_lib_extensions.hpp:68 (host vectors in, device compute)
  * Errors throw std::runtime_error carrying the library message, as the reference's check_cuda()
  * does (gpu/hala_cuda_common.hpp:78-152).  Header only; link with -lhgb -lcudart.
@@ -353,6 +354,29 @@ int solve_cg(gpu_engine const &e, stop_criteria<T> const &stop, gpu_vector<int> 
               "solve_cg");
     return info.iterations;
 }
+/* solve_batch_cg_ilu(gpu_engine, stop, pntr, indx, vals, ilu, B, X), hex/solvers/hala_solvers_cg_batch.hpp:
+ * B and X hold num_rhs = B.size() / n column-major right-hand sides */
+template <typename T>
+int solve_batch_cg_ilu(gpu_engine const &e, stop_criteria<T> const &stop, gpu_vector<int> const &pntr,
+                       gpu_vector<int> const &indx, gpu_vector<T> const &vals, gpu_ilu<T> const &ilu,
+                       gpu_vector<T> const &B, gpu_vector<T> &X) {
+    int n = (int)pntr.size() - 1;
+    int nrhs = (int)(B.size() / (size_t)n);
+    if (X.size() < B.size()) { X.resize(B.size()); set_zero(e, X); }
+    auto A = make_sparse_matrix(e, n, pntr, indx, vals);
+    hgb_solve_info info{};
+    hgb_check(hgb_cg_solve_nrhs(e.handle(), A.handle(), ilu.handle(), nrhs, B.data(), X.data(), (double)stop.tol,
+                                stop.max_iter, &info), "solve_batch_cg_ilu");
+    return info.iterations;
+}
+template <typename T>
+int solve_batch_cg_ilu(gpu_engine const &e, stop_criteria<T> const &stop, gpu_vector<int> const &pntr,
+                       gpu_vector<int> const &indx, gpu_vector<T> const &vals, gpu_vector<T> const &B,
+                       gpu_vector<T> &X, char policy = 'N') {
+    auto ilu = make_ilu(e, pntr, indx, vals, policy);
+    return solve_batch_cg_ilu(e, stop, pntr, indx, vals, ilu, B, X);
+}
+
 /* solve_gmres_ilu(gpu_engine, stop, restart, pntr, indx, vals, ilu, b, x) */
 inline int solve_gmres_ilu(gpu_engine const &e, stop_criteria<double> const &stop, int restart,
                            gpu_vector<int> const &pntr, gpu_vector<int> const &indx, gpu_vector<double> const &vals,

@@ -176,6 +176,26 @@ int hgb_cg_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, const void *b, void *x, d
  * transpose and the preconditioner applies (LU)^-T.  The adjoint solve A^T lambda = g. */
 int hgb_cg_solve_op(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, char trans, const void *b, void *x,
                     double tol, int max_iter, hgb_solve_info *info);
+
+/* ---- several right-hand sides with one matrix (n x nrhs column-major blocks) ---- */
+
+/* Y = alpha A X + beta Y, one column at a time: sparse_gemm_array 'N','N'
+ * (sparse/hala_sparse_utils.hpp:127-133) through sparse_gemm (wax); each column is bit-identical to
+ * hgb_csr_gemv.  ldx >= columns of A, ldy >= rows of A. */
+int hgb_csr_gemm(hgb_csr *A, int nrhs, double alpha, const void *x, int ldx, double beta, void *y, int ldy);
+
+/* R = M^-1 X (trans 'N') or M^-T X, column by column: gpu_ilu::apply with num_rhs
+ * (gpu/hala_gpu_ilu.hpp:150-164) / apply_ilu_array per column. */
+int hgb_ilu0_apply_nrhs(hgb_ilu *M, char trans, int nrhs, const void *x, void *r);
+
+/* Multi right-hand side PCG, solve_batch_cg / solve_batch_cg_ilu
+ * (hex/solvers/hala_solvers_cg_batch.hpp:68-248): the CG recurrence of solve_cg_core with one
+ * scalar per column; all columns iterate until iterations >= max_iter or the largest column
+ * residual norm (batch_max_norm2) is below tol (absolute).  M may be NULL (no preconditioner).
+ * B, X: device, n x nrhs column-major, the matrix's precision (FP32 vectors for BF16 values). */
+int hgb_cg_solve_nrhs(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int nrhs, const void *B, void *X, double tol,
+                      int max_iter, hgb_solve_info *info);
+
 /* Mixed precision iterative refinement: FP64 outer residual, update and stopping test on A64
  * (F64); inner ILU(0)-PCG on A_inner (F32 or BF16 values, FP32 vectors and accumulation) with
  * M_inner (store F32 or BF16, FP64 pivots), each inner solve to ||r|| < inner_rtol * ||r0||.

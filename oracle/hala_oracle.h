@@ -71,6 +71,11 @@ void or_spmv_bf16f32(char trans, int m, int ncols, float alpha, const int *pntr,
      * reference's iteration count; *res_out (if not NULL) gets the last ||r||. */              \
     int or_cg_##S(int n, const int *pntr, const int *indx, const T *vals, const int *diag,     \
                   const T *ilu, const T *b, T *x, T tol, int max_iter, T *res_out);            \
+    /* solve_batch_cg[_ilu], hex/solvers/hala_solvers_cg_batch.hpp:68-248: nrhs column-major   \
+     * right-hand sides, one CG scalar per column, stop on the largest column residual. */      \
+    int or_batch_cg_##S(int n, const int *pntr, const int *indx, const T *vals, const int *diag, \
+                        const T *ilu, int nrhs, const T *b, T *x, T tol, int max_iter,           \
+                        T *res_out);                                                             \
     /* solve_gmres, hex/solvers/hala_solvers_gmres.hpp:127-230 (left preconditioned, one       \
      * classical Gram-Schmidt pass, host Givens).  Returns total operator applications. */      \
     int or_gmres_##S(int n, const int *pntr, const int *indx, const T *vals, const int *diag,  \

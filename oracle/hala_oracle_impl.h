@@ -194,6 +194,53 @@ int OR_FN(or_cg)(int n, const int *pntr, const int *indx, const OT *vals, const 
     return iterations;
 }
 
+/* solve_batch_cg / solve_batch_cg_ilu, hex/solvers/hala_solvers_cg_batch.hpp:68-248: the
+ * recurrence of solve_cg_core on n x nrhs column-major blocks with one scalar per column
+ * (batch_dot, vdivide, batch_axpy, batch_scal, wax/hala_blas_extensions.hpp:30-140); stops when
+ * iterations == max_iter or batch_max_norm2(r) = sqrt(max_c <r_c, r_c>) < tol (:369-380). */
+int OR_FN(or_batch_cg)(int n, const int *pntr, const int *indx, const OT *vals, const int *diag,
+                       const OT *ilu, int nrhs, const OT *b, OT *x, OT tol, int max_iter, OT *res_out) {
+    const size_t tot = (size_t)n * nrhs, sz = sizeof(OT) * tot;
+    OT *r = (OT *)malloc(sz), *p = (OT *)malloc(sz), *Ap = (OT *)malloc(sz), *z = (OT *)malloc(sz);
+    OT *zr = (OT *)malloc(sizeof(OT) * nrhs), *nzr = (OT *)malloc(sizeof(OT) * nrhs), *a = (OT *)malloc(sizeof(OT) * nrhs);
+    memcpy(r, b, sz);
+    for (int c = 0; c < nrhs; c++) OR_FN(or_spmv)('N', n, n, 1, pntr, indx, vals, x + (size_t)c * n, 0, p + (size_t)c * n);
+    for (size_t i = 0; i < tot; i++) r[i] += (OT)(-1.0) * p[i];                  /* axpy(-1, p, r) */
+    for (int c = 0; c < nrhs; c++) OR_FN(or_precond)(n, pntr, indx, diag, ilu, r + (size_t)c * n, z + (size_t)c * n);
+    memcpy(p, z, sz);
+    for (int c = 0; c < nrhs; c++) zr[c] = OR_FN(or_dot)(n, r + (size_t)c * n, z + (size_t)c * n);
+    int iterations = 1;
+    OT res = 0;
+    for (;;) {
+        for (int c = 0; c < nrhs; c++)
+            OR_FN(or_spmv)('N', n, n, 1, pntr, indx, vals, p + (size_t)c * n, 0, Ap + (size_t)c * n);
+        iterations++;
+        for (int c = 0; c < nrhs; c++) nzr[c] = OR_FN(or_dot)(n, p + (size_t)c * n, Ap + (size_t)c * n);
+        for (int c = 0; c < nrhs; c++) a[c] = zr[c] / nzr[c];                     /* vdivide */
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) x[(size_t)c * n + i] += ((OT)1.0 * a[c]) * p[(size_t)c * n + i];
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) r[(size_t)c * n + i] += ((OT)(-1.0) * a[c]) * Ap[(size_t)c * n + i];
+        OT mx = 0;
+        for (int c = 0; c < nrhs; c++) {
+            OT d = OR_FN(or_dot)(n, r + (size_t)c * n, r + (size_t)c * n);
+            if (OFABS(d) > mx) mx = OFABS(d);
+        }
+        res = OSQRT(mx);
+        if (iterations == max_iter || res < tol) break;
+        for (int c = 0; c < nrhs; c++) OR_FN(or_precond)(n, pntr, indx, diag, ilu, r + (size_t)c * n, z + (size_t)c * n);
+        for (int c = 0; c < nrhs; c++) nzr[c] = OR_FN(or_dot)(n, r + (size_t)c * n, z + (size_t)c * n);
+        for (int c = 0; c < nrhs; c++) a[c] = nzr[c] / zr[c];
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) p[(size_t)c * n + i] *= a[c];               /* batch_scal */
+        for (size_t i = 0; i < tot; i++) p[i] += z[i];                             /* axpy(1, z, p) */
+        memcpy(zr, nzr, sizeof(OT) * nrhs);
+    }
+    if (res_out) *res_out = res;
+    free(r); free(p); free(Ap); free(z); free(zr); free(nzr); free(a);
+    return iterations;
+}
+
 static void OR_FN(or_rotg)(OT *a, OT *b, OT *c, OT *s) {
     OT roe = (OFABS(*a) > OFABS(*b)) ? *a : *b;
     OT scale = OFABS(*a) + OFABS(*b), r, zz;

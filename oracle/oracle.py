@@ -55,6 +55,8 @@ def _load():
         getattr(lib, f"or_nrm2_{s}").restype = ft
         getattr(lib, f"or_cg_{s}").argtypes = [i, _i32p, _i32p, fp, vp, vp, fp, fp, ft, i, C.POINTER(ft)]
         getattr(lib, f"or_cg_{s}").restype = i
+        getattr(lib, f"or_batch_cg_{s}").argtypes = [i, _i32p, _i32p, fp, vp, vp, i, fp, fp, ft, i, C.POINTER(ft)]
+        getattr(lib, f"or_batch_cg_{s}").restype = i
         getattr(lib, f"or_gmres_{s}").argtypes = [i, _i32p, _i32p, fp, vp, vp, i, fp, fp, ft, i]
         getattr(lib, f"or_gmres_{s}").restype = i
     lib.or_ir_pcg.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, _f64p, _f64p,
@@ -204,6 +206,19 @@ def cg(pntr, indx, vals, b, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu
                                                      np.ascontiguousarray(b, vals.dtype), x, tol,
                                                      max_iter, C.byref(res))
     return x, it, res.value
+
+
+def batch_cg(pntr, indx, vals, B, nrhs, X0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):
+    """solve_batch_cg / solve_batch_cg_ilu restated (B, X: n x nrhs column-major, flattened).
+    Returns (X, iterations, final batch_max_norm2(r))."""
+    n = len(pntr) - 1
+    X = np.zeros(n * nrhs, vals.dtype) if X0 is None else np.array(X0, vals.dtype, copy=True).reshape(-1)
+    ft = C.c_double if vals.dtype == np.float64 else C.c_float
+    res = ft(0)
+    it = getattr(lib(), f"or_batch_cg_{_sfx(vals.dtype)}")(n, pntr, indx, vals, _ptr(diag), _ptr(ilu), nrhs,
+                                                           np.ascontiguousarray(B, vals.dtype).reshape(-1), X,
+                                                           tol, max_iter, C.byref(res))
+    return X, it, res.value
 
 
 def gmres(pntr, indx, vals, b, restart, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):

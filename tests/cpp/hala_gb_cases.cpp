@@ -1,5 +1,5 @@
 // C++ replay of the reference's sparse/solver test cases through include/hala_gb/hala_gb.hpp
-// (tests/sparse_tests.hpp test_ilu, tests/solvers_tests.hpp test_cg and test_gmres,
+// (tests/sparse_tests.hpp test_ilu, tests/solvers_tests.hpp test_cg, test_cg_batch and test_gmres,
 // tests/cuda_sparse_tests.hpp sparse_matvec).  Exit code 0 when every check passes.
 #include "hala_gb/hala_gb.hpp"
 
@@ -105,6 +105,43 @@ int main() {
         hala::solve_gmres_ilu(engine, hala::stop_criteria<double>(1e-9), 6, gp, gi, gv, hala::make_gpu_vector(b), gx);
         gx.unload(x);
         CHECK(testvec(x, xref), "gmres nonsymmetric");
+    }
+    {   // test_cg_batch: three right-hand sides, exact tridiagonal then cyclic with (1e-9, 6)
+        std::vector<double> xb(15);
+        for (int k = 0; k < 15; k++) xb[k] = k + 1;
+        double nrm = 0;
+        for (double v : xb) nrm += v * v;
+        nrm = std::sqrt(nrm);
+        auto block_b = [&](std::vector<int> const &p, std::vector<int> const &i, std::vector<double> const &v) {
+            std::vector<double> b;
+            for (int k = 0; k < 3; k++) {
+                auto col = matvec(p, i, v, std::vector<double>(xb.begin() + 5 * k, xb.begin() + 5 * k + 5));
+                b.insert(b.end(), col.begin(), col.end());
+            }
+            return b;
+        };
+        std::vector<int> pntr = {0, 2, 5, 8, 11, 13}, indx = {0, 1, 0, 1, 2, 1, 2, 3, 2, 3, 4, 3, 4};
+        std::vector<double> vals = {2, 1, 1, 2, 1, 1, 2, 1, 1, 2, 1, 1, 2}, x;
+        auto gp = hala::make_gpu_vector(pntr);
+        auto gi = hala::make_gpu_vector(indx);
+        auto gv = hala::make_gpu_vector(vals);
+        auto ilu = hala::make_ilu(engine, gp, gi, gv, 'N');
+        gpu_vector<double> gx;
+        hala::solve_batch_cg_ilu(engine, hala::stop_criteria<double>(2), gp, gi, gv, ilu,
+                                 hala::make_gpu_vector(block_b(pntr, indx, vals)), gx);
+        gx.unload(x);
+        CHECK(testvec(x, xb, nrm), "batch cg exact");
+        pntr = {0, 3, 6, 9, 12, 15};
+        indx = {0, 1, 4, 0, 1, 2, 1, 2, 3, 2, 3, 4, 0, 3, 4};
+        vals = {2, 1, 1, 1, 2, 1, 1, 2, 1, 1, 2, 1, 1, 1, 2};
+        auto cp = hala::make_gpu_vector(pntr);
+        auto ci = hala::make_gpu_vector(indx);
+        auto cv = hala::make_gpu_vector(vals);
+        gpu_vector<double> gx2;
+        hala::solve_batch_cg_ilu(engine, hala::stop_criteria<double>(1e-9, 6), cp, ci, cv,
+                                 hala::make_gpu_vector(block_b(pntr, indx, vals)), gx2);
+        gx2.unload(x);
+        CHECK(testvec(x, xb, nrm), "batch cg_ilu approximate");
     }
     std::printf("%s\n", failures ? "HALA-GB CASES: FAIL" : "HALA-GB CASES: ALL PASS");
     return failures ? 1 : 0;

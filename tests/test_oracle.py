@@ -214,3 +214,27 @@ def test_oracle_matches_fixture(path):
     xo, ito = O.gmres(p, i, v, g["b"], int(g["gmres_restart"]), tol=float(g["gmres_tol"]),
                       max_iter=int(g["gmres_max_iter"]), diag=d, ilu=f)
     assert ito == int(g["gmres_iters"]) and np.array_equal(xo, g["gmres_x"])
+
+
+def test_batch_cg_reference_cases():
+    # tests/solvers_tests.hpp:56-104 (test_cg_batch): xref = make_vector(15), three columns
+    xref = R.make_vector(0, 15)
+    for case, tol, cap in [(R.TRIDIAG5, 0.0, 2), (R.CYCLIC5, 1e-9, 6)]:
+        A = R.dense(case)
+        B = np.concatenate([A @ xref[5 * c:5 * c + 5] for c in range(3)])
+        f, d, _ = O.ilu_factor(case["pntr"], case["indx"], case["vals"])
+        X, it, _ = O.batch_cg(case["pntr"], case["indx"], case["vals"], B, 3, tol=tol, max_iter=cap, diag=d, ilu=f)
+        assert R.testvec(X, xref, np.linalg.norm(xref))
+
+
+@needs_ref
+def test_batch_cg_matches_reference_build(rng):
+    p, i, v = P.aniso3d(9, 8, 7)
+    n, k = len(p) - 1, 3
+    B = rng.standard_normal(n * k)
+    tol = 1e-9 * np.linalg.norm(B[:n])
+    f, d, _ = O.ilu_factor(p, i, v)
+    X, it, _ = O.batch_cg(p, i, v, B, k, tol=tol, max_iter=500, diag=d, ilu=f)
+    Xr = np.zeros(n * k)
+    itr = O.ref().ref_solve_batch_cg_ilu_d(n, p, i, v, k, B, Xr, tol, 500)
+    assert it == itr and np.array_equal(X, Xr)
