@@ -11,6 +11,7 @@
 #include "hgb_kernels.cuh"
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <vector>
 
@@ -344,165 +345,407 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
 }  // extern "C"
 
 // ===================================================================== GMRES ===========
+// solve_gmres (hex/solvers/hala_solvers_gmres.hpp:127-230), device resident.  The reference
+// reads the projection coefficients back to the host in every inner iteration (:67-72) and
+// rotates on the host; here the Hessenberg columns, the Givens rotations, the residual estimate
+// and the back substitution (tpsv) live in a GmresState in device memory and are updated by the
+// last CTA of the projection's grid reduction.  Inner iteration j of a cycle always projects
+// against j+1 basis vectors, so one whole restart cycle is captured once into a CUDA graph; the
+// launches of iterations after the inner stop are no-ops, and the host reads the state once per
+// cycle.  The arithmetic of the rotations, of tpsv and of the x update is the reference's
+// operation for operation (explicitly rounded, no contraction); the inner products are parallel.
 namespace hgb {
 
-// r -= W c (k columns) and ||r||^2 -> out   (krylov_project's gemv 'N' fused with norm2)
-__global__ void cgs_update_kernel(long n, int k, const double *__restrict__ W, const double *__restrict__ cf,
-                                  double *__restrict__ r, double *partials, unsigned *counter, double *out) {
-    double acc[1] = {0.0};
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double ri = r[i];
-        for (int j = 0; j < k; j++) ri = __dadd_rn(ri, __dmul_rn(-cf[j], W[(long)j * n + i]));
-        r[i] = ri;
-        acc[0] += ri * ri;
-    }
-    grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) { *out = v[0]; });
-}
+constexpr int kGmresMaxRestart = 64;
 
-__global__ void scale_copy_kernel(long n, double a, double *__restrict__ r, double *__restrict__ wcol) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        double v = r[i] * a;
-        r[i] = v;
-        if (wcol) wcol[i] = v;
-    }
-}
+struct GmresState {
+    // header (read by the host after every cycle)
+    double tol;          // threshold on the preconditioned residual estimate
+    double rel;          // > 0: tol = max(tol, rel * first estimate) (inner solves of a refinement)
+    double inner_res, outer_res;
+    double inv;          // reciprocal of the norm of the vector being appended
+    int k, stop, done, wcol, upd, total, outer, max_outer, restart, first;
+    // rotations and the triangular factor
+    double Z[kGmresMaxRestart + 1];
+    double C[kGmresMaxRestart], S[kGmresMaxRestart];
+    double H[kGmresMaxRestart * (kGmresMaxRestart + 1) / 2];
+};
 
-static void rotg(double &a, double &b, double &c, double &s) {
-    double roe = (std::fabs(a) > std::fabs(b)) ? a : b;
-    double scale = std::fabs(a) + std::fabs(b), r, z;
-    if (scale == 0.0) { c = 1.0; s = 0.0; r = 0.0; z = 0.0; }
-    else {
-        r = scale * std::sqrt((a / scale) * (a / scale) + (b / scale) * (b / scale));
+__device__ __forceinline__ void gm_rotg(double &a, double &b, double &c, double &s) {
+    double roe = (fabs(a) > fabs(b)) ? a : b;
+    double scale = __dadd_rn(fabs(a), fabs(b)), r, z;
+    if (scale == 0.0) {
+        c = 1.0; s = 0.0; r = 0.0; z = 0.0;
+    } else {
+        double as = __ddiv_rn(a, scale), bs = __ddiv_rn(b, scale);
+        r = __dmul_rn(scale, __dsqrt_rn(__dadd_rn(__dmul_rn(as, as), __dmul_rn(bs, bs))));
         if (roe < 0.0) r = -r;
-        c = a / r;
-        s = b / r;
+        c = __ddiv_rn(a, r);
+        s = __ddiv_rn(b, r);
         z = 1.0;
-        if (std::fabs(a) > std::fabs(b)) z = s;
-        if (std::fabs(b) >= std::fabs(a) && c != 0.0) z = 1.0 / c;
+        if (fabs(a) > fabs(b)) z = s;
+        if (fabs(b) >= fabs(a) && c != 0.0) z = __ddiv_rn(1.0, c);
     }
     a = r;
     b = z;
 }
 
-static void rot(double &x, double &y, double c, double s) {
-    double t = c * x + s * y;
-    y = c * y - s * x;
+__device__ __forceinline__ void gm_rot(double &x, double &y, double c, double s) {
+    double t = __dadd_rn(__dmul_rn(c, x), __dmul_rn(s, y));
+    y = __dsub_rn(__dmul_rn(c, y), __dmul_rn(s, x));
     x = t;
+}
+
+__global__ void gm_init_kernel(GmresState *st, double tol, double rel, int max_outer, int restart) {
+    st->tol = tol;
+    st->rel = rel;
+    st->inner_res = 0.0;
+    st->outer_res = tol + 1.0;
+    st->inv = 0.0;
+    st->k = 0;
+    st->stop = 1;
+    st->done = !(max_outer > 0);
+    st->wcol = -1;
+    st->upd = 0;
+    st->total = 0;
+    st->outer = 0;
+    st->max_outer = max_outer;
+    st->restart = restart;
+    st->first = 1;
+}
+
+__global__ void gm_begin_kernel(GmresState *st) {
+    st->k = 0;
+    st->upd = 0;
+    st->wcol = -1;
+    st->stop = 1;
+}
+
+template <typename X>
+__global__ void gm_copy_kernel(long n, const int *skip, const X *__restrict__ a, X *__restrict__ b) {
+    if (*skip) return;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+// beta = ||P^-1 (b - A x)||: the first estimate of the cycle (Z[0]); basis vector 0 follows
+template <typename X>
+__global__ void gm_start_kernel(long n, GmresState *st, const X *__restrict__ r, double *partials,
+                                unsigned *counter) {
+    if (st->done) return;
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        acc[0] += (double)r[i] * (double)r[i];
+    grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
+        double beta = __dsqrt_rn(v[0]);
+        if (st->first) {
+            st->first = 0;
+            if (st->rel > 0.0) st->tol = fmax(st->tol, st->rel * beta);
+        }
+        st->total += 1;
+        st->inner_res = beta;
+        st->Z[0] = beta;
+        bool go = beta > st->tol;
+        st->stop = !go;
+        st->wcol = go ? 0 : -1;
+        st->inv = __ddiv_rn(1.0, beta);
+    });
+}
+
+// r *= inv; W[:, wcol] = r   (scal(1/nrm, r) and the copy into the basis)
+template <typename X>
+__global__ void gm_scale_kernel(long n, const GmresState *__restrict__ st, X *__restrict__ r, X *__restrict__ W) {
+    const int col = st->wcol;
+    if (col < 0) return;
+    const X a = (X)st->inv;
+    X *w = W + (long)col * n;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        X v = mul_rn(r[i], a);
+        r[i] = v;
+        w[i] = v;
+    }
+}
+
+// cf[0..k] = W[:, 0..k]^T r   (krylov_project's gemv 'T', :67-70)
+template <typename X, int KMAX>
+__global__ void gm_dots_kernel(long n, int k1, const GmresState *__restrict__ st, const X *__restrict__ W,
+                               const X *__restrict__ r, double *cf, double *partials, unsigned *counter) {
+    if (st->stop) return;
+    double acc[KMAX];
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) acc[j] = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double ri = (double)r[i];
+#pragma unroll
+        for (int j = 0; j < KMAX; j++)
+            if (j < k1) acc[j] += (double)W[(long)j * n + i] * ri;
+    }
+    grid_sum<KMAX>(acc, partials, counter, [&](double (&s)[KMAX]) {
+        for (int j = 0; j < k1; j++) cf[j] = s[j];
+    });
+}
+
+// r -= W cf (krylov_project's gemv 'N', :71-76), ||r||, then in the last CTA the Givens step of
+// solve_gmres (:190-216) for column k of the Hessenberg matrix.
+template <typename X>
+__global__ void gm_update_kernel(long n, int k, GmresState *st, const X *__restrict__ W, const double *__restrict__ cf,
+                                 X *__restrict__ r, double *partials, unsigned *counter) {
+    if (st->stop) return;
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        X ri = r[i];
+        for (int j = 0; j <= k; j++) ri = add_rn(ri, mul_rn((X)-cf[j], W[(long)j * n + i]));
+        r[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+    }
+    grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
+        const double nrm = __dsqrt_rn(v[0]);
+        double h[kGmresMaxRestart + 1];
+        for (int j = 0; j <= k; j++) h[j] = cf[j];
+        for (int i = 0; i < k; i++) gm_rot(h[i], h[i + 1], st->C[i], st->S[i]);
+        double beta = nrm, ic, is;
+        gm_rotg(h[k], beta, ic, is);
+        double *Hk = st->H + (long)k * (k + 1) / 2;
+        for (int j = 0; j <= k; j++) Hk[j] = h[j];
+        st->S[k] = is;
+        st->C[k] = ic;
+        const double res = fabs(__dmul_rn(is, st->Z[k]));
+        st->inner_res = res;
+        st->total += 1;
+        st->k = k + 1;
+        const bool expand = (res > st->tol) && (k + 1 < st->restart);
+        if (expand) {
+            st->Z[k + 1] = 0.0;
+            gm_rot(st->Z[k], st->Z[k + 1], ic, is);
+            st->wcol = k + 1;
+            st->inv = __ddiv_rn(1.0, nrm);
+        } else {
+            st->wcol = -1;
+            st->stop = 1;
+        }
+    });
+}
+
+// End of a cycle: tpsv('U','N','N', k, H, Z) (:219-223), the restart bookkeeping (:225-229)
+__global__ void gm_end_kernel(GmresState *st) {
+    if (st->done) return;
+    const int nz = st->k;
+    if (nz > 0) {
+        long kk = (long)nz * (nz + 1) / 2 - 1;
+        for (int j = nz - 1; j >= 0; j--) {
+            if (st->Z[j] != 0.0) {
+                st->Z[j] = __ddiv_rn(st->Z[j], st->H[kk]);
+                const double tt = st->Z[j];
+                long q = kk - 1;
+                for (int i = j - 1; i >= 0; i--, q--) st->Z[i] = __dsub_rn(st->Z[i], __dmul_rn(tt, st->H[q]));
+            }
+            kk -= j + 1;
+        }
+        st->upd = 1;
+    }
+    st->outer += 1;
+    st->outer_res = st->inner_res;
+    st->done = !(st->outer_res > st->tol && st->outer < st->max_outer);
+}
+
+// x += W[:, 0..k-1] Z   (krylov_combine, :53-60), column by column in the reference's order
+template <typename X>
+__global__ void gm_xupdate_kernel(long n, const GmresState *__restrict__ st, const X *__restrict__ W, X *__restrict__ x) {
+    if (!st->upd) return;
+    const int nz = st->k;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        X xi = x[i];
+        for (int j = 0; j < nz; j++) xi = add_rn(xi, mul_rn((X)st->Z[j], W[(long)j * n + i]));
+        x[i] = xi;
+    }
+}
+
+template <typename X>
+static int gm_dots_launch(hgb_ctx *c, long n, int k1, const GmresState *st, const X *W, const X *r, double *cf) {
+    const int grid = reduce_grid(c, n, 256 * 8);
+    if (k1 <= 8) gm_dots_kernel<X, 8><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
+    else if (k1 <= 16) gm_dots_kernel<X, 16><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
+    else if (k1 <= 32) gm_dots_kernel<X, 32><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
+    else gm_dots_kernel<X, 64><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
+    return launch_check("gm_dots_kernel");
+}
+
+// Runs restarted GMRES on (A, M) for b -> x (x holds the initial guess).  tol: absolute threshold
+// on the preconditioned residual estimate; rel > 0 also stops at rel * the first estimate;
+// max_outer: restart cycles.
+template <typename V, typename X>
+static int gmres_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int restart, const X *b, X *x, double tol, double rel,
+                     int max_outer, int *total, int *outer, double *res, long long *launches) {
+    const long n = csr_rows(A);
+    CaptureStream cs(c);
+    X *t = nullptr, *r = nullptr, *W = nullptr;
+    double *cf = nullptr;
+    GmresState *st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int pre = M ? 2 : 1;          // ILU: L and U sweeps; none: a copy
+    const long long per_cycle = 6 + pre + (long long)restart * (4 + pre);
+    int rc = HGB_OK;
+    do {
+        if (cudaMalloc(&t, sizeof(X) * n) || cudaMalloc(&r, sizeof(X) * n) || cudaMalloc(&W, sizeof(X) * n * restart) ||
+            cudaMalloc(&cf, sizeof(double) * (kGmresMaxRestart + 1)) || cudaMalloc(&st, sizeof(GmresState))) {
+            rc = cuda_fail(cudaErrorMemoryAllocation, "gmres workspace");
+            break;
+        }
+        gm_init_kernel<<<1, 1, 0, c->stream>>>(st, tol, rel, max_outer, restart);
+        *launches += 1;
+        if ((rc = launch_check("gm_init_kernel"))) break;
+        auto precon = [&](const X *in, X *out, const int *skip) -> int {
+            if (M) return ilu_apply_internal(M, 'N', in, out, skip);
+            gm_copy_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, skip, in, out);
+            return launch_check("gm_copy_kernel");
+        };
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)) { rc = cuda_fail(cudaGetLastError(), "begin capture"); break; }
+        do {
+            // t = b - A x ; r = P^-1 t ; beta = ||r|| ; W[:,0] = r / beta
+            gm_begin_kernel<<<1, 1, 0, c->stream>>>(st);
+            gm_copy_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, &st->done, b, t);
+            if ((rc = spmv_A<V, X>(c, A, X(-1), x, X(1), t, nullptr, &st->done))) break;
+            if ((rc = precon(t, r, &st->done))) break;
+            gm_start_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, st, r, c->partials, c->counter);
+            gm_scale_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, st, r, W);
+            for (int k = 0; k < restart && !rc; k++) {
+                if ((rc = spmv_A<V, X>(c, A, X(1), r, X(0), t, nullptr, &st->stop))) break;
+                if ((rc = precon(t, r, &st->stop))) break;
+                if ((rc = gm_dots_launch<X>(c, n, k + 1, st, W, r, cf))) break;
+                gm_update_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, k, st, W, cf, r, c->partials,
+                                                                                       c->counter);
+                gm_scale_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, st, r, W);
+            }
+            if (rc) break;
+            gm_end_kernel<<<1, 1, 0, c->stream>>>(st);
+            gm_xupdate_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, st, W, x);
+            rc = launch_check("gmres cycle");
+        } while (0);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (rc) break;
+        if (ce != cudaSuccess) { rc = cuda_fail(ce, "end capture"); break; }
+        if (cudaGraphInstantiate(&exec, graph, 0)) { rc = cuda_fail(cudaGetLastError(), "graph instantiate"); break; }
+        GmresState hs{};
+        const size_t head = offsetof(GmresState, Z);
+        for (;;) {
+            if (cudaGraphLaunch(exec, c->stream)) { rc = cuda_fail(cudaGetLastError(), "graph launch"); break; }
+            *launches += per_cycle;
+            if (cudaMemcpyAsync(c->host_result, st, head, cudaMemcpyDeviceToHost, c->stream) ||
+                cudaStreamSynchronize(c->stream)) { rc = cuda_fail(cudaGetLastError(), "gmres"); break; }
+            memcpy(&hs, c->host_result, head);
+            if (hs.done) break;
+        }
+        *total = hs.total;
+        *outer = hs.outer;
+        *res = hs.inner_res;
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(t);
+    cudaFree(r);
+    cudaFree(W);
+    cudaFree(cf);
+    cudaFree(st);
+    if (rc) return rc;
+    return collect_dev_error(c);
 }
 
 }  // namespace hgb
 
 extern "C" int hgb_gmres_solve(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int restart, const void *bv, void *xv, double tol,
                                int max_iter, hgb_solve_info *info) {
-    if (!c || !A || !bv || !xv || restart < 1 || restart > 64) return fail(HGB_ERR_ARG, "gmres: bad arguments (restart 1..64)");
-    if (csr_dtype(A) != HGB_F64) return fail(HGB_ERR_UNSUPPORTED, "gmres: F64 only");
-    if (M && ilu_store(M) != HGB_F64) return fail(HGB_ERR_ARG, "gmres: preconditioner must be F64");
-    const long n = csr_rows(A);
-    const double *b = (const double *)bv;
-    double *x = (double *)xv;
+    if (!c || !A || !bv || !xv || restart < 1 || restart > kGmresMaxRestart)
+        return fail(HGB_ERR_ARG, "gmres: bad arguments (restart 1..%d)", kGmresMaxRestart);
+    if (csr_rows(A) != csr_cols(A)) return fail(HGB_ERR_ARG, "gmres: square matrix required");
+    const hgb_dtype dt = csr_dtype(A);
+    if (M) {
+        if (ilu_n(M) != csr_rows(A)) return fail(HGB_ERR_ARG, "gmres: preconditioner size");
+        bool ok = (dt == HGB_F64) ? (ilu_store(M) == HGB_F64) : (ilu_store(M) != HGB_F64);
+        if (!ok) return fail(HGB_ERR_ARG, "gmres: preconditioner precision does not match the matrix");
+    }
     DeviceGuard g(c->device);
-    double *t = nullptr, *r = nullptr, *W = nullptr, *dc = nullptr;
-    int st = HGB_OK;
     int total = 0, outer = 0;
+    double res = 0.0;
     long long launches = 0;
-    double inner_res = 0.0, outer_res = tol + 1.0;
-    std::vector<double> H, S, C, Z, cf(restart + 2);
-    double *hbuf = c->host_result;   // pinned, >= 8 doubles; coefficients go through dc
-    std::vector<double> hcf(restart + 2);
-    do {
-        if (cudaMalloc(&t, sizeof(double) * n) || cudaMalloc(&r, sizeof(double) * n) ||
-            cudaMalloc(&W, sizeof(double) * n * restart) || cudaMalloc(&dc, sizeof(double) * (restart + 2))) {
-            st = cuda_fail(cudaErrorMemoryAllocation, "gmres workspace");
-            break;
-        }
-        auto precon = [&](const double *in, double *out) -> int {
-            if (M) return ilu_apply_internal(M, 'N', in, out, nullptr);
-            return cudaMemcpyAsync(out, in, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream) ? HGB_ERR_CUDA : HGB_OK;
-        };
-        auto norm_sync = [&](const double *v, double *out) -> int {
-            residual_norm_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, v, c->partials, c->counter, c->result);
-            HGB_CUDA(cudaMemcpyAsync(hbuf, c->result, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-            HGB_CUDA(cudaStreamSynchronize(c->stream));
-            *out = std::sqrt(hbuf[0]);
-            return HGB_OK;
-        };
-        while (outer_res > tol && outer < max_iter) {
-            H.clear(); S.clear(); C.clear(); Z.clear();
-            // t = b - A x ; r = P^-1 t
-            if (cudaMemcpyAsync(t, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream)) { st = HGB_ERR_CUDA; break; }
-            if ((st = spmv_A<double, double>(c, A, -1.0, x, 1.0, t, nullptr, nullptr))) break;
-            if ((st = precon(t, r))) break;
-            total++;
-            launches += 1 + (M ? 2 : 0) + 2;
-            if ((st = norm_sync(r, &inner_res))) break;
-            scale_copy_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, 1.0 / inner_res, r, W);
-            Z.push_back(inner_res);
-            int k = 0;
-            while (inner_res > tol && k < restart) {
-                if ((st = spmv_A<double, double>(c, A, 1.0, r, 0.0, t, nullptr, nullptr))) break;
-                if ((st = precon(t, r))) break;
-                total++;
-                launches += 1 + (M ? 2 : 0) + 3;
-                // krylov_project: cf = W^T r (k+1 columns) ; r -= W cf ; nrm = ||r||
-                if ((st = hgb_gemv_f64(c, 'T', (int)n, k + 1, 1.0, W, r, 0.0, dc))) break;
-                cgs_update_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, k + 1, W, dc, r, c->partials,
-                                                                                    c->counter, dc + restart + 1);
-                if ((st = launch_check("cgs_update_kernel"))) break;
-                if (cudaMemcpyAsync(hcf.data(), dc, sizeof(double) * (restart + 2), cudaMemcpyDeviceToHost, c->stream) ||
-                    cudaStreamSynchronize(c->stream)) { st = cuda_fail(cudaGetLastError(), "gmres"); break; }
-                double nrm = std::sqrt(hcf[restart + 1]);
-                for (int j = 0; j <= k; j++) cf[j] = hcf[j];
-                for (int i = 0; i < k; i++) rot(cf[i], cf[i + 1], C[i], S[i]);
-                double beta = nrm, ic, is;
-                rotg(cf[k], beta, ic, is);
-                H.insert(H.end(), cf.begin(), cf.begin() + k + 1);
-                S.push_back(is);
-                C.push_back(ic);
-                inner_res = std::fabs(S.back() * Z.back());
-                k++;
-                bool expand = (inner_res > tol) && (k < restart);
-                scale_copy_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, 1.0 / nrm, r, expand ? W + (long)k * n : nullptr);
-                if (expand) {
-                    Z.push_back(0.0);
-                    rot(Z[k - 1], Z[k], C.back(), S.back());
-                }
-            }
-            if (st) break;
-            if (!H.empty()) {
-                // tpsv('U','N','N', nz, H, Z), column-oriented back substitution (packed upper)
-                int nz = (int)Z.size();
-                long kk = (long)nz * (nz + 1) / 2 - 1;
-                for (int j = nz - 1; j >= 0; j--) {
-                    if (Z[j] != 0.0) {
-                        Z[j] /= H[kk];
-                        double tt = Z[j];
-                        long q = kk - 1;
-                        for (int i = j - 1; i >= 0; i--, q--) Z[i] -= tt * H[q];
-                    }
-                    kk -= j + 1;
-                }
-                if (cudaMemcpyAsync(dc, Z.data(), sizeof(double) * nz, cudaMemcpyHostToDevice, c->stream)) { st = HGB_ERR_CUDA; break; }
-                if ((st = hgb_gemv_f64(c, 'N', (int)n, nz, 1.0, W, dc, 1.0, x))) break;
-                launches += 1;
-                if (cudaStreamSynchronize(c->stream)) { st = cuda_fail(cudaGetLastError(), "gmres"); break; }
-            }
-            outer++;
-            outer_res = inner_res;
-        }
-    } while (0);
-    cudaFree(t);
-    cudaFree(r);
-    cudaFree(W);
-    cudaFree(dc);
+    int st;
+    if (dt == HGB_F64)
+        st = gmres_run<double, double>(c, A, M, restart, (const double *)bv, (double *)xv, tol, 0.0, max_iter, &total, &outer, &res, &launches);
+    else if (dt == HGB_F32)
+        st = gmres_run<float, float>(c, A, M, restart, (const float *)bv, (float *)xv, tol, 0.0, max_iter, &total, &outer, &res, &launches);
+    else
+        st = gmres_run<uint16_t, float>(c, A, M, restart, (const float *)bv, (float *)xv, tol, 0.0, max_iter, &total, &outer, &res, &launches);
     if (st) return st;
-    HGB_TRY(collect_dev_error(c));
     if (info) {
         info->iterations = total;
         info->outer = outer;
-        info->residual = inner_res;
+        info->residual = res;
         info->true_residual = -1.0;
         info->kernel_launches = launches;
     }
+    return HGB_OK;
+}
+
+// Mixed-precision GMRES: FP64 iterative refinement around an FP32-vector GMRES(restart) with an
+// FP32 or BF16 matrix and ILU(0) (no reference counterpart; the inner solver is solve_gmres).
+extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, int restart, const double *b,
+                                  double *x, double tol, double inner_rtol, int max_inner, int max_outer,
+                                  hgb_solve_info *info) {
+    if (!c || !A64 || !Ai || !b || !x || restart < 1 || restart > kGmresMaxRestart)
+        return fail(HGB_ERR_ARG, "ir_gmres: bad arguments (restart 1..%d)", kGmresMaxRestart);
+    if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the outer matrix must be F64");
+    if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the inner matrix must be F32 or BF16");
+    if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the inner preconditioner must store F32 or BF16");
+    const long n = csr_rows(A64);
+    if (csr_rows(Ai) != n || csr_cols(A64) != n || csr_cols(Ai) != n || (Mi && ilu_n(Mi) != n))
+        return fail(HGB_ERR_ARG, "ir_gmres: sizes");
+    if (max_inner < 1 || max_outer < 0 || !(inner_rtol > 0.0)) return fail(HGB_ERR_ARG, "ir_gmres: limits");
+    DeviceGuard g(c->device);
+    double *r64 = nullptr;
+    float *r32 = nullptr, *d32 = nullptr;
+    int st = HGB_OK;
+    int total = 0, outer = 0;
+    double res = 0.0;
+    long long launches = 0;
+    const int cycles = (max_inner + restart - 1) / restart;
+    do {
+        if (cudaMalloc(&r64, sizeof(double) * n) || cudaMalloc(&r32, sizeof(float) * n) || cudaMalloc(&d32, sizeof(float) * n)) {
+            st = cuda_fail(cudaErrorMemoryAllocation, "ir_gmres workspace");
+            break;
+        }
+        for (;;) {
+            if ((st = true_residual(c, A64, b, x, r64, &res, &launches))) break;
+            if (res < tol || outer >= max_outer || !(res == res)) break;
+            f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, r32);
+            zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d32);
+            launches += 3;   // residual cast, zero, update
+            // as the refinement CG: this sweep reduces its (preconditioned) residual as far as the
+            // target needs with a factor 2 of margin, never by less than inner_rtol
+            const double rel = std::min(0.5, std::max(inner_rtol, 0.5 * tol / res));
+            int it = 0, cyc = 0;
+            double ires = 0.0;
+            if (csr_dtype(Ai) == HGB_F32)
+                st = gmres_run<float, float>(c, Ai, Mi, restart, r32, d32, 0.0, rel, cycles, &it, &cyc, &ires, &launches);
+            else
+                st = gmres_run<uint16_t, float>(c, Ai, Mi, restart, r32, d32, 0.0, rel, cycles, &it, &cyc, &ires, &launches);
+            if (st) break;
+            total += it;
+            add_f32_to_f64_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d32, x);
+            if ((st = launch_check("ir update"))) break;
+            outer++;
+        }
+    } while (0);
+    cudaFree(r64);
+    cudaFree(r32);
+    cudaFree(d32);
+    if (st) return st;
+    if (info) {
+        info->iterations = total;
+        info->outer = outer;
+        info->residual = res;
+        info->true_residual = res;
+        info->kernel_launches = launches;
+    }
+    if (!(res < tol)) return fail(HGB_ERR_NOT_CONVERGED, "ir_gmres: ||b-Ax|| = %g after %d sweeps (tol %g)", res, outer, tol);
     return HGB_OK;
 }
 

@@ -373,7 +373,8 @@ def pattern_grad(A, alpha, lam, u, grad):
 
 
 def solve_gmres(engine, stop, restart, pntr, indx, vals, b, x, ilu=None, matrix=None):
-    """solve_gmres / solve_gmres_ilu(gpu_engine, ...), hex/solvers/hala_solvers_gmres.hpp:127-267."""
+    """solve_gmres / solve_gmres_ilu(gpu_engine, ...), hex/solvers/hala_solvers_gmres.hpp:127-267.
+    Returns the number of operator applications (the reference's return value)."""
     s = _stop(stop)
     A = matrix or gpu_sparse_matrix(engine, pntr.numel() - 1, pntr, indx, vals)
     info = SolveInfo()
@@ -394,6 +395,18 @@ def solve_ir_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, inner_rtol=1e-4, ma
     st = _h.lib().hgb_ir_pcg_solve(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, _p(b), _p(x),
                                    float(tol), float(inner_rtol), int(max_inner), int(max_outer), C.byref(info))
     check(st, "solve_ir_pcg")
+    return info
+
+
+def solve_ir_gmres(engine, A64, A_inner, ilu_inner, restart, b, x, tol, inner_rtol=1e-4, max_inner=3000,
+                   max_outer=50):
+    """Mixed-precision ILU(0)-GMRES(restart): FP32/BF16 inner solves, FP64 refinement to
+    ||b - A x|| < tol (no reference counterpart; the inner solver is solve_gmres).  Returns SolveInfo."""
+    info = SolveInfo()
+    st = _h.lib().hgb_ir_gmres_solve(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, int(restart),
+                                     _p(b), _p(x), float(tol), float(inner_rtol), int(max_inner), int(max_outer),
+                                     C.byref(info))
+    check(st, "solve_ir_gmres")
     return info
 
 

@@ -209,11 +209,22 @@ int hgb_ir_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M
                         const double *b, double *x, double tol, double inner_rtol, int max_inner,
                         int max_outer, hgb_solve_info *info);
 /* solve_gmres / solve_gmres_ilu over gpu_engine (hex/solvers/hala_solvers_gmres.hpp:127-267):
- * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations on
- * the host in the reference's order.  max_iter bounds the restarts, tol is absolute on the
- * preconditioned residual estimate.  F64 or F32 (A's precision). */
+ * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations in
+ * the reference's order.  The rotations and the back substitution run on the device and one
+ * restart cycle is one CUDA graph (one host synchronisation per cycle, where the reference
+ * reads the projection back in every inner iteration, :67-72).  max_iter bounds the restarts,
+ * tol is absolute on the preconditioned residual estimate, restart 1..64.  F64, F32 or BF16
+ * values (A's precision; FP32 vectors for BF16) with a preconditioner of matching precision. */
 int hgb_gmres_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int restart, const void *b, void *x,
                     double tol, int max_iter, hgb_solve_info *info);
+/* Mixed precision GMRES: FP64 iterative refinement (residual, update and stopping test
+ * ||b - A x||_2 < tol on A64) around GMRES(restart) on A_inner (F32 or BF16 values, FP32
+ * vectors) with M_inner (store F32 or BF16), each inner solve to a preconditioned residual
+ * estimate below inner_rtol times its first one (max_inner inner iterations per sweep).
+ * No reference counterpart; the inner solver is solve_gmres (hala_solvers_gmres.hpp:127-230). */
+int hgb_ir_gmres_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, int restart,
+                       const double *b, double *x, double tol, double inner_rtol, int max_inner,
+                       int max_outer, hgb_solve_info *info);
 /* mixed_engine form (wax/hala_lib_extensions.hpp:68; solve_cg_ilu(mixed_engine,...),
  * hala_solvers_cg.hpp:330-340): HOST pntr/indx/vals/b/x, loaded to the device per call, solved
  * with the device factor M, x written back to the host.  FP64. */

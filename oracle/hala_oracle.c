@@ -213,3 +213,145 @@ int or_ir_pcg(int n, const int *pntr, const int *indx, const double *vals, const
     free(r); free(rf); free(d); free(p); free(Ap); free(z);
     return total;
 }
+
+/* Givens helpers of the refinement's inner GMRES: drotg / drot in double, as or_gmres_d. */
+static void ir_rotg(double *a, double *b, double *c, double *s) {
+    double roe = (fabs(*a) > fabs(*b)) ? *a : *b;
+    double scale = fabs(*a) + fabs(*b), r, zz;
+    if (scale == 0) { *c = 1; *s = 0; r = 0; zz = 0; }
+    else {
+        r = scale * sqrt((*a / scale) * (*a / scale) + (*b / scale) * (*b / scale));
+        if (roe < 0) r = -r;
+        *c = *a / r; *s = *b / r;
+        zz = 1;
+        if (fabs(*a) > fabs(*b)) zz = *s;
+        if (fabs(*b) >= fabs(*a) && *c != 0) zz = 1 / *c;
+    }
+    *a = r; *b = zz;
+}
+
+static void ir_rot(double *x, double *y, double c, double s) {
+    double t = c * *x + s * *y;
+    *y = c * *y - s * *x;
+    *x = t;
+}
+
+/* Inner solve of or_ir_gmres: solve_gmres (hex/solvers/hala_solvers_gmres.hpp:127-230) on the
+ * FP32 system from d = 0, with FP32 vectors and basis, inner products and norms accumulated in
+ * double, the rotations, the residual estimate and tpsv in double, and the stopping threshold
+ * rel * (first preconditioned residual).  Returns the operator applications. */
+static int ir_gmres_inner(int n, const int *pntr, const int *indx, const float *vals32, const int *diag,
+                          const float *ilu32, const double *piv, int restart, const float *b, float *d,
+                          double rel, int max_cycles) {
+    size_t nf = sizeof(float) * (size_t)n;
+    float *t = (float *)malloc(nf), *r = (float *)malloc(nf), *W = (float *)malloc(nf * (size_t)restart);
+    double *H = (double *)malloc(sizeof(double) * (size_t)restart * (restart + 1));
+    double *S = (double *)malloc(sizeof(double) * (restart + 1)), *Cc = (double *)malloc(sizeof(double) * (restart + 1));
+    double *Z = (double *)malloc(sizeof(double) * (restart + 1)), *cf = (double *)malloc(sizeof(double) * (restart + 1));
+    double tol = 0, inner_res = 0, outer_res = 1;
+    int total = 0, cycles = 0, first = 1;
+    while (max_cycles > 0) {
+        /* t = b - A d ; r = P^-1 t ; beta = ||r|| */
+        memcpy(t, b, nf);
+        or_spmv_f('N', n, n, -1.0f, pntr, indx, vals32, d, 1.0f, t);
+        memcpy(r, t, nf);
+        ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, r);
+        double s2 = 0;
+        for (int i = 0; i < n; i++) s2 += (double)r[i] * r[i];
+        double beta = sqrt(s2);
+        if (first) { first = 0; if (rel * beta > tol) tol = rel * beta; }
+        total++;
+        inner_res = beta;
+        Z[0] = beta;
+        int nh = 0, k = 0;
+        if (beta > tol) {
+            float sc = (float)(1.0 / beta);
+            for (int i = 0; i < n; i++) { r[i] *= sc; W[i] = r[i]; }
+        }
+        while (inner_res > tol && k < restart) {
+            or_spmv_f('N', n, n, 1.0f, pntr, indx, vals32, r, 0.0f, t);
+            memcpy(r, t, nf);
+            ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, r);
+            for (int j = 0; j <= k; j++) {
+                double s = 0;
+                for (int i = 0; i < n; i++) s += (double)W[(size_t)j * n + i] * (double)r[i];
+                cf[j] = s;
+            }
+            double rn = 0;
+            for (int i = 0; i < n; i++) {
+                float ri = r[i];
+                for (int j = 0; j <= k; j++) ri = ri + (float)(-cf[j]) * W[(size_t)j * n + i];
+                r[i] = ri;
+                rn += (double)ri * ri;
+            }
+            double nrm = sqrt(rn);
+            for (int i = 0; i < k; i++) ir_rot(&cf[i], &cf[i + 1], Cc[i], S[i]);
+            double bt = nrm, ic, is;
+            ir_rotg(&cf[k], &bt, &ic, &is);
+            for (int j = 0; j <= k; j++) H[nh++] = cf[j];
+            S[k] = is; Cc[k] = ic;
+            inner_res = fabs(is * Z[k]);
+            total++;
+            k++;
+            if (inner_res > tol && k < restart) {
+                Z[k] = 0;
+                ir_rot(&Z[k - 1], &Z[k], ic, is);
+                float sc = (float)(1.0 / nrm);
+                for (int i = 0; i < n; i++) { r[i] *= sc; W[(size_t)k * n + i] = r[i]; }
+            }
+        }
+        if (nh > 0) {
+            long kk = (long)k * (k + 1) / 2 - 1;
+            for (int j = k - 1; j >= 0; j--) {
+                if (Z[j] != 0) {
+                    Z[j] /= H[kk];
+                    double tt = Z[j];
+                    long q = kk - 1;
+                    for (int i = j - 1; i >= 0; i--, q--) Z[i] -= tt * H[q];
+                }
+                kk -= j + 1;
+            }
+            for (int i = 0; i < n; i++) {
+                float di = d[i];
+                for (int j = 0; j < k; j++) di = di + (float)Z[j] * W[(size_t)j * n + i];
+                d[i] = di;
+            }
+        }
+        cycles++;
+        outer_res = inner_res;
+        if (!(outer_res > tol && cycles < max_cycles)) break;
+    }
+    free(t); free(r); free(W); free(H); free(S); free(Cc); free(Z); free(cf);
+    return total;
+}
+
+/* Mixed-precision GMRES (no reference counterpart): outer r = b - A x in FP64, inner GMRES(restart)
+ * in FP32 (ir_gmres_inner) with the FP32 ILU(0) and FP64 pivots, each sweep to
+ * rel = min(0.5, max(inner_rtol, 0.5 tol / ||r||)) of its first preconditioned residual,
+ * x += d in FP64.  Stops when ||b - A x|| < tol.  Returns the inner applications; *outer_out
+ * gets the sweeps. */
+int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, const float *vals32,
+                const int *diag, const float *ilu32, const double *piv, int restart, const double *b,
+                double *x, double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out) {
+    size_t nd = sizeof(double) * (size_t)n, nf = sizeof(float) * (size_t)n;
+    double *r = (double *)malloc(nd);
+    float *rf = (float *)malloc(nf), *d = (float *)malloc(nf);
+    int total = 0, outer = 0;
+    const int cycles = (max_inner + restart - 1) / restart;
+    for (;;) {
+        or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r);
+        for (int i = 0; i < n; i++) r[i] = b[i] - r[i];
+        double res = dnorm(n, r);
+        if (res < tol || outer >= max_outer || res != res) break;
+        for (int i = 0; i < n; i++) { rf[i] = (float)r[i]; d[i] = 0.0f; }
+        double rel = 0.5 * tol / res;
+        if (rel < inner_rtol) rel = inner_rtol;
+        if (rel > 0.5) rel = 0.5;
+        total += ir_gmres_inner(n, pntr, indx, vals32, diag, ilu32, piv, restart, rf, d, rel, cycles);
+        for (int i = 0; i < n; i++) x[i] += (double)d[i];
+        outer++;
+    }
+    if (outer_out) *outer_out = outer;
+    free(r); free(rf); free(d);
+    return total;
+}

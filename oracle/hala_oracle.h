@@ -98,6 +98,15 @@ int or_ir_pcg(int n, const int *pntr, const int *indx, const double *vals, const
               const int *diag, const float *ilu32, const double *piv, const double *b, double *x,
               double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out);
 
+/* Mixed-precision GMRES (no reference counterpart): outer r = b - A x in FP64, inner
+ * GMRES(restart) (solve_gmres's loop) in FP32 vectors with double inner products and rotations,
+ * on (vals32, ilu32 with FP64 pivots piv), each sweep to a relative preconditioned tolerance,
+ * x += d in FP64.  Stops when ||b - A x|| < tol.  Returns the inner operator applications;
+ * *outer_out gets the sweeps. */
+int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, const float *vals32,
+                const int *diag, const float *ilu32, const double *piv, int restart, const double *b,
+                double *x, double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out);
+
 #ifdef __cplusplus
 }
 #endif

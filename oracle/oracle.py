@@ -62,6 +62,9 @@ def _load():
     lib.or_ir_pcg.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, _f64p, _f64p,
                               C.c_double, C.c_double, i, i, C.POINTER(i)]
     lib.or_ir_pcg.restype = i
+    lib.or_ir_gmres.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, i, _f64p, _f64p,
+                                C.c_double, C.c_double, i, i, C.POINTER(i)]
+    lib.or_ir_gmres.restype = i
     return lib
 
 
@@ -238,6 +241,18 @@ def ir_pcg(pntr, indx, vals, vals32, diag, ilu32, piv, b, tol, inner_rtol=1e-4, 
     outer = C.c_int(0)
     tot = lib().or_ir_pcg(n, pntr, indx, vals, vals32, diag, ilu32, piv, b, x, tol, inner_rtol,
                           max_inner, max_outer, C.byref(outer))
+    return x, tot, outer.value
+
+
+def ir_gmres(pntr, indx, vals, vals32, diag, ilu32, piv, restart, b, tol, inner_rtol=1e-4, max_inner=3000,
+             max_outer=50, x0=None):
+    """Mixed FP32-inner / FP64-refined GMRES(restart) (no reference counterpart).
+    Returns (x, total inner applications, sweeps)."""
+    n = len(pntr) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    outer = C.c_int(0)
+    tot = lib().or_ir_gmres(n, pntr, indx, vals, vals32, diag, ilu32, piv, restart, b, x, tol, inner_rtol,
+                            max_inner, max_outer, C.byref(outer))
     return x, tot, outer.value
 
 

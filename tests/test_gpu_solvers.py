@@ -158,3 +158,90 @@ def test_mixed_engine_host_buffers(eng, rng):
     _, ito, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
     assert within5(info.iterations, ito)
     assert np.linalg.norm(b - P.csr_matvec(p, i, v, x)) < 2 * tol
+
+
+@pytest.mark.parametrize("restart", [3, 8])
+def test_gmres_several_cycles(eng, rng, restart):
+    # short restarts: several device-resident cycles, each one graph replay
+    p, i, v = P.convdiff3d(14)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    tol = 1e-9 * np.linalg.norm(O.ilu_apply(p, i, do, fo, b))
+    xo, ito = O.gmres(p, i, v, b, restart, tol=tol, diag=do, ilu=fo)
+    gp, gi, gv = T(p), T(i), T(v)
+    ilu = E.make_ilu(eng, gp, gi, gv)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    it = E.solve_gmres(eng, E.stop_criteria(tol), restart, gp, gi, gv, T(b), x, ilu=ilu)
+    assert ito > restart + 1          # more than one cycle
+    assert within5(it, ito), (it, ito)
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-7 * np.linalg.norm(xo)
+
+
+def test_gmres_cycle_limit_and_unpreconditioned(eng, rng):
+    p, i, v = P.convdiff3d(10)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    gp, gi, gv = T(p), T(i), T(v)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    # stop_criteria(int): the number of restart cycles only
+    it = E.solve_gmres(eng, E.stop_criteria(3), 4, gp, gi, gv, T(b), x)
+    xo, ito = O.gmres(p, i, v, b, 4, max_iter=3)
+    assert it == ito == 3 * 5
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
+
+
+def test_gmres_restart_bounds(eng):
+    from hala_gb300.hgb import HgbError
+    p, i, v = P.convdiff3d(4)
+    gp, gi, gv = T(p), T(i), T(v)
+    x = torch.zeros(len(p) - 1, dtype=torch.float64, device=dev)
+    b = torch.ones(len(p) - 1, dtype=torch.float64, device=dev)
+    with pytest.raises(HgbError):
+        E.solve_gmres(eng, E.stop_criteria(1e-9), 65, gp, gi, gv, b, x)
+
+
+def test_gmres_fp32(eng, rng):
+    p, i, v = P.convdiff3d(16)
+    n = len(p) - 1
+    v32 = v.astype(np.float32)
+    b = rng.uniform(-1, 1, n).astype(np.float32)
+    fo, do, _ = O.ilu_factor(p, i, v32)
+    tol = 1e-5 * float(np.linalg.norm(O.ilu_apply(p, i, do, fo, b)))
+    _, ito = O.gmres(p, i, v32, b, 30, tol=np.float32(tol), diag=do, ilu=fo)
+    gp, gi, gv = T(p), T(i), T(v32)
+    ilu = E.make_ilu(eng, gp, gi, gv)
+    x = torch.zeros(n, dtype=torch.float32, device=dev)
+    it = E.solve_gmres(eng, E.stop_criteria(tol), 30, gp, gi, gv, T(b), x, ilu=ilu)
+    # FP32 vectors; the device rotations are in double, the oracle's FP32 GMRES rotates in float
+    assert abs(it - ito) <= max(2, int(round(0.1 * ito))), (it, ito)
+    xs = x.cpu().numpy().astype(np.float64)
+    r = b - P.csr_matvec(p, i, v32.astype(np.float64), xs)
+    assert np.linalg.norm(r) <= 1e-4 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("inner", [torch.float32, torch.bfloat16])
+def test_ir_gmres(eng, rng, inner):
+    p, i, v = P.convdiff3d(24)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    tol = 1e-9 * np.linalg.norm(b)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    Ai = E.make_sparse_matrix(eng, n, gp, gi, gv.to(inner))
+    Mi = E.make_ilu(eng, gp, gi, gv, store=inner)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    rtol = 1e-4 if inner == torch.float32 else 1e-2
+    info = E.solve_ir_gmres(eng, A64, Ai, Mi, 30, T(b), x, tol, inner_rtol=rtol)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
+    assert info.outer >= 2
+    xf, _ = O.gmres(p, i, v, b, 30, tol=1e-13 * np.linalg.norm(b), diag=do, ilu=fo)
+    assert np.linalg.norm(xs - xf) <= 1e-7 * np.linalg.norm(xf)
+    if inner == torch.float32:
+        # the oracle's restatement of the same refinement: same sweeps, inner applications within 5%
+        xo, tot, outer = O.ir_gmres(p, i, v, v.astype(np.float32), do, fo.astype(np.float32), fo[do], 30, b, tol,
+                                    inner_rtol=rtol)
+        assert info.outer == outer, (info.outer, outer)
+        assert within5(info.iterations, tot), (info.iterations, tot)

@@ -132,6 +132,22 @@ def test_ir_pcg_reaches_tolerance(rng):
     assert outer >= 2
 
 
+@pytest.mark.parametrize("restart", [5, 30])
+def test_ir_gmres_reaches_tolerance(rng, restart):
+    p, i, v = P.convdiff3d(12)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    f, d, _ = O.ilu_factor(p, i, v)
+    tol = 1e-9 * np.linalg.norm(b)
+    x, tot, outer = O.ir_gmres(p, i, v, v.astype(np.float32), d, f.astype(np.float32), f[d], restart, b, tol,
+                               inner_rtol=1e-4)
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, x)) < tol
+    assert outer >= 2
+    # the same system in FP64 GMRES lands on the same solution
+    xo, _ = O.gmres(p, i, v, b, restart, tol=1e-12 * np.linalg.norm(b), diag=d, ilu=f)
+    assert np.linalg.norm(x - xo) <= 1e-7 * np.linalg.norm(xo)
+
+
 # --------------------------------------------- against the reference's compiled CPU path ---
 needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference CPU path not built here")
 
