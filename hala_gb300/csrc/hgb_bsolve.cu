@@ -656,6 +656,18 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         e = lower ? diag[row] : pntr[row + 1];
     };
     (void)xsize;   // the block layout is the same for every solution type
+    // Blocks hold a whole multiple of the bandwidth (in solve order), so that every dependency
+    // reaches at most one block back and block b+1 trails block b by a few steps.  Other sizes
+    // break the wavefront: on the 96^3 7-point pattern (bandwidth 9216), 16384-row blocks put the
+    // rows that block b+1 needs first at the end of block b's schedule, and the critical path
+    // grows from ~380 steps to ~4300.
+    int bw = 0;
+    for (int row = 0; row < n; row++) {
+        int a, e;
+        deps(row, a, e);
+        if (e > a) bw = std::max(bw, lower ? row - indx[a] : indx[e - 1] - row);
+    }
+    if (bw >= 1 && bw <= R) R = R / bw * bw;
     const int Rmax = R;
     for (int p0 = 0; p0 < n;) {
         // grow the block in solve order while it fits R rows and kBsStepCap steps
