@@ -1,6 +1,7 @@
 """Benchmark: ILU(0)-PCG solves/s on the 128^3 anisotropic 7-point system to a 1e-10 relative
-residual, mixed precision (FP32 inner PCG, FP64 refinement) against plain FP64, plus SpMV GB/s
-against the measured HBM copy bandwidth.
+residual, mixed precision (FP32 PCG with FP64 refinement by reliable updates) against plain FP64,
+plus SpMV GB/s against the measured HBM copy bandwidth.  The restarted refinement (a new FP32
+PCG per FP64 sweep) is timed beside it.
 
 One step = one complete solve from x0 = 0 (ILU setup excluded, timed separately).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -28,6 +29,7 @@ GRID = int(os.environ.get("HGB_BENCH_GRID", "128"))
 COEF = (1.0, 1.0, 0.01)
 RTOL = 1e-10
 IR_INNER_RTOL = 1e-5     # first refinement sweep; later sweeps stop at what the target needs
+RU_DELTA = 0.01          # reliable update when ||r|| has dropped 100x since the last one
 SEED = 2
 
 
@@ -269,6 +271,10 @@ def main():
 
     def solve_mixed():
         x.zero_()
+        return E.solve_ru_pcg(eng, A64, A32, M32, gb, x, tol, delta=RU_DELTA)
+
+    def solve_ir():
+        x.zero_()
         return E.solve_ir_pcg(eng, A64, A32, M32, gb, x, tol, inner_rtol=IR_INNER_RTOL)
 
     clocks = ClockSampler(torch.cuda.current_device())
@@ -280,6 +286,7 @@ def main():
     x64 = x.clone()
     msmx, infmx = timed(solve_mixed, args.steps, args.warmup)
     xmx = x.clone()
+    msir, infir = timed(solve_ir, args.steps, args.warmup)
     torch.cuda.synchronize()
 
     # ---- kernel timing for the roofline (same stream, CUDA events, L2 flushed per launch)
@@ -316,7 +323,7 @@ def main():
         hx[:] = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E.solve_ir_pcg_mixed(eng, tol, hp, hi, hv, M32, hb_, hx, inner_rtol=IR_INNER_RTOL)
+        E.solve_ru_pcg_mixed(eng, tol, hp, hi, hv, M32, hb_, hx, delta=RU_DELTA)
         if k >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     h2d = 4 * (n + 1) + 4 * nnz + 8 * nnz + 8 * n + 8 * n
@@ -346,7 +353,8 @@ def main():
     res64 = float(np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) / np.linalg.norm(b))
     resmx = float(np.linalg.norm(b - P.csr_matvec(p, i, v, xm)) / np.linalg.norm(b))
     it64 = inf64[-1].iterations
-    launches = sum(int(q.kernel_launches) for q in inf64) + sum(int(q.kernel_launches) for q in infmx)
+    launches = (sum(int(q.kernel_launches) for q in inf64) + sum(int(q.kernel_launches) for q in infmx)
+                + sum(int(q.kernel_launches) for q in infir))
     launches += 7 * 10     # roofline kernel timing: 3 SpMV + 2 ILU applies (2 launches each) x 10
     # dominant kernel of the headline (mixed) solve: the FP32-store triangular sweeps (ILU apply)
     ach_ilu = ib32 / (t_ilu32 * 1e-3) / 1e9
@@ -382,23 +390,27 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
         "config": {"workload": f"ILU(0)-PCG, 3D 7-point anisotropic {GRID}^3 coef (1,1,0.01), b = A x_true "
                                f"(x_true ~ N(0,1), seed {SEED}), x0 = 0, ||b-Ax|| < 1e-10 ||b||",
-                   "n": n, "nnz": nnz, "form": "mixed: FP32 values/vectors/ILU (FP64 pivots), FP64 IR",
+                   "n": n, "nnz": nnz, "form": "mixed: FP32 values/vectors/ILU (FP64 pivots) PCG, FP64 "
+                                               f"refinement by reliable updates (delta {RU_DELTA})",
                    "l2": "flushed between timed solves (256 MB write); matrix 217 MB > 129 MB L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"solves_per_s": world * 1e3 / t_64, "ms_per_solve": t_64, "iterations": it64,
                  "rel_residual": res64, "setup_ms": setup64 * 1e3},
         "mixed": {"solves_per_s": world * 1e3 / t_mx, "ms_per_solve": t_mx, "inner_iterations": infmx[-1].iterations,
-                  "outer": infmx[-1].outer, "rel_residual": resmx,
+                  "reliable_updates": infmx[-1].outer, "rel_residual": resmx,
                   "err_vs_fp64": float(np.linalg.norm(xm - xs) / np.linalg.norm(xs)),
                   "err_vs_xtrue": float(np.linalg.norm(xm - xt) / np.linalg.norm(xt)), "setup_ms": setup32 * 1e3},
         "mixed_over_fp64": t_64 / t_mx,
+        "mixed_restarted_ir": {"solves_per_s": world * 1e3 / statistics.mean(msir),
+                               "ms_per_solve": statistics.mean(msir), "inner_iterations": infir[-1].iterations,
+                               "sweeps": infir[-1].outer, "inner_rtol": IR_INNER_RTOL},
         "roofline": roof, "spmv": spmv,
         "ilu_apply": {"f64": {"ms": t_ilu64, "gbs": ib64 / (t_ilu64 * 1e-3) / 1e9, "bytes": ib64,
                               "traffic": prof.get("ilu_apply_f64_bytes")},
                       "f32": {"ms": t_ilu32, "gbs": ib32 / (t_ilu32 * 1e-3) / 1e9, "bytes": ib32,
                               "traffic": prof.get("ilu_apply_f32_bytes")}},
         "e2e": {"value": world * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "entry": "hgb_mixed_ir_pcg_solve (host pntr/indx/vals/b/x)",
+                "d2h_bytes_per_step": d2h, "entry": "hgb_mixed_ru_pcg_solve (host pntr/indx/vals/b/x)",
                 "rel_residual": e2e_err},
         "gpu_launches": launches,
         "cpu_baseline": cpu,

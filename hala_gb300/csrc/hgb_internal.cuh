@@ -45,6 +45,10 @@ struct SolverScalars {
     double r0;                   // first residual norm of the current inner solve
     double rel;                  // inner relative tolerance (IR); 0 = absolute test only
     int it, done, max_iter, pad;
+    // reliable-update PCG: largest ||r||^2 since the last update, the update threshold (delta^2),
+    // 0 while an update is due in the current iteration, updates so far
+    double rmax2, delta2;
+    int ru_skip, updates;
 };
 
 }  // namespace hgb

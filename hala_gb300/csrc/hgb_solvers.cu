@@ -344,6 +344,198 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
 
 }  // extern "C"
 
+// ============================================== mixed PCG with reliable updates =======
+// One FP32 ILU(0)-PCG (solve_cg_core's order, hex/solvers/hala_solvers_cg.hpp:92-156) on the
+// correction d, with FP64 reliable updates (van der Vorst and Ye, "Residual replacement
+// strategies for Krylov subspace iterative methods for the convergence of true residuals",
+// SIAM J. Sci. Comput. 22 (2000)): when ||r|| falls below delta times its largest value since
+// the last update (or below tol, or at the iteration limit), x += d in FP64, r = b - A x in FP64
+// and the iteration continues from the new residual with the same search direction.  Unlike a
+// restarted refinement, the Krylov space is kept, so the iterations stay those of FP64 PCG.
+// No reference counterpart.  One iteration is nine launches, three of them (the update) no-ops
+// except in update iterations; kItersPerGraph iterations are one CUDA graph.
+namespace hgb {
+
+__global__ void ru_init_kernel(SolverScalars *s, double tol2, double delta2, double rr, int max_iter) {
+    s->it = 0;
+    s->done = 0;
+    s->max_iter = max_iter;
+    s->tol2 = tol2;
+    s->rel = 0.0;
+    s->zr = s->nzr = s->pap = 0.0;
+    s->rr = rr;
+    s->rmax2 = rr;
+    s->delta2 = delta2;
+    s->ru_skip = 1;
+    s->updates = 0;
+}
+
+// a = <r,z>/<p,Ap>; d += a p; r -= a Ap; ||r||^2; decide whether this iteration updates
+__global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict__ p, const float *__restrict__ Ap,
+                               float *__restrict__ d, float *__restrict__ r, double *partials, unsigned *counter) {
+    if (s->done) return;
+    const float a = (float)(s->zr / s->pap);
+    const float ma = -a;
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        d[i] = __fadd_rn(d[i], __fmul_rn(a, p[i]));
+        const float ri = __fadd_rn(r[i], __fmul_rn(ma, Ap[i]));
+        r[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+    }
+    grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
+        const double rr = v[0];
+        s->rr = rr;
+        s->it += 1;
+        s->rmax2 = fmax(s->rmax2, rr);
+        const bool upd = (rr < s->delta2 * s->rmax2) || (rr < s->tol2) || !(rr == rr) || (s->it >= s->max_iter);
+        s->ru_skip = upd ? 0 : 1;
+    });
+}
+
+// x += d (FP64); d = 0; r64 = b   (the FP64 product follows)
+__global__ void ru_fold_kernel(long n, const SolverScalars *__restrict__ s, const double *__restrict__ b,
+                               float *__restrict__ d, double *__restrict__ x, double *__restrict__ r64) {
+    if (s->ru_skip) return;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        x[i] += (double)d[i];
+        d[i] = 0.0f;
+        r64[i] = b[i];
+    }
+}
+
+// r = (float) r64; ||r64||^2; the stopping test on the FP64 residual
+__global__ void ru_replace_kernel(long n, SolverScalars *s, const double *__restrict__ r64, float *__restrict__ r,
+                                  double *partials, unsigned *counter) {
+    if (s->ru_skip) return;
+    double acc[1] = {0.0};
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double v = r64[i];
+        r[i] = (float)v;
+        acc[0] += v * v;
+    }
+    grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
+        const double rr = v[0];
+        s->rr = rr;
+        s->rmax2 = rr;
+        s->updates += 1;
+        s->done = (rr < s->tol2) || !(rr == rr) || (s->it >= s->max_iter);
+        s->ru_skip = 1;
+    });
+}
+
+template <typename V>
+static int ru_iteration(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, CgWork<float> &w, float *d, double *x,
+                        double *r64, const double *b, long n) {
+    SolverScalars *s = c->scal;
+    const int *done = &s->done;
+    HGB_TRY(spmv_A<V, float>(c, Ai, 1.0f, w.p, 0.0f, w.Ap, &s->pap, done));
+    ru_step_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.p, w.Ap, d, w.r, c->partials, c->counter);
+    ru_fold_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, b, d, x, r64);
+    HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r64, nullptr, &s->ru_skip));
+    ru_replace_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, r64, w.r, c->partials, c->counter);
+    float *z = M ? w.z : w.r;
+    if (M) HGB_TRY(ilu_apply_internal(M, 'N', w.r, w.z, done));
+    cg_rz_kernel<float><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
+    cg_p_kernel<float><<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, w.p, z);
+    return launch_check("ru iteration");
+}
+
+static int ru_launches_per_iter(bool precond) { return precond ? 9 : 7; }
+
+template <typename V>
+static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const double *b, double *x, double tol,
+                  double delta, int max_iter, int *iters, int *updates, double *res, long long *launches) {
+    const long n = csr_rows(A64);
+    CaptureStream cs(c);
+    CgWork<float> w;
+    float *d = nullptr;
+    double *r64 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    SolverScalars hs{};
+    int st = w.alloc(n, M != nullptr);
+    do {
+        if (st) break;
+        if (cudaMalloc(&d, sizeof(float) * n) || cudaMalloc(&r64, sizeof(double) * n)) {
+            st = cuda_fail(cudaErrorMemoryAllocation, "ru_pcg workspace");
+            break;
+        }
+        double rn = 0.0;
+        if ((st = true_residual(c, A64, b, x, r64, &rn, launches))) break;
+        *iters = 0;
+        *updates = 0;
+        *res = rn;
+        if (rn < tol || !(rn == rn) || max_iter < 1) break;
+        SolverScalars *s = c->scal;
+        ru_init_kernel<<<1, 1, 0, c->stream>>>(s, tol * tol, delta * delta, rn * rn, max_iter);
+        f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, w.r);
+        zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d);
+        float *z = M ? w.z : w.r;
+        if (M && (st = ilu_apply_internal(M, 'N', w.r, w.z, nullptr))) break;
+        copy_kernel<float><<<ew_grid(c, n), 256, 0, c->stream>>>(n, z, w.p);
+        // <r,z> of the first direction (the rr slot keeps the FP64 residual)
+        cg_rz_kernel<float><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
+        *launches += 5 + (M ? 2 : 0);
+        if ((st = launch_check("ru init"))) break;
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)) { st = cuda_fail(cudaGetLastError(), "begin capture"); break; }
+        for (int k = 0; k < kItersPerGraph && !st; k++) st = ru_iteration<V>(c, A64, Ai, M, w, d, x, r64, b, n);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+        if (st) break;
+        if (ce != cudaSuccess) { st = cuda_fail(ce, "end capture"); break; }
+        if (cudaGraphInstantiate(&exec, graph, 0)) { st = cuda_fail(cudaGetLastError(), "graph instantiate"); break; }
+        for (;;) {
+            if (cudaGraphLaunch(exec, c->stream)) { st = cuda_fail(cudaGetLastError(), "graph launch"); break; }
+            *launches += (long long)kItersPerGraph * ru_launches_per_iter(M != nullptr);
+            if (cudaMemcpyAsync(c->host_result, s, sizeof(SolverScalars), cudaMemcpyDeviceToHost, c->stream) ||
+                cudaStreamSynchronize(c->stream)) { st = cuda_fail(cudaGetLastError(), "ru_pcg sync"); break; }
+            memcpy(&hs, c->host_result, sizeof(SolverScalars));
+            if (hs.done) break;
+        }
+        *iters = hs.it;
+        *updates = hs.updates;
+        *res = sqrt(hs.rr);
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    w.release();
+    cudaFree(d);
+    cudaFree(r64);
+    if (st) return st;
+    return collect_dev_error(c);
+}
+
+}  // namespace hgb
+
+extern "C" int hgb_ru_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, const double *b, double *x,
+                                double tol, double delta, int max_iter, hgb_solve_info *info) {
+    if (!c || !A64 || !Ai || !b || !x) return fail(HGB_ERR_ARG, "ru_pcg: bad arguments");
+    if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the outer matrix must be F64");
+    if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the inner matrix must be F32 or BF16");
+    if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the preconditioner must store F32 or BF16");
+    const long n = csr_rows(A64);
+    if (csr_rows(Ai) != n || csr_cols(A64) != n || csr_cols(Ai) != n || (Mi && ilu_n(Mi) != n))
+        return fail(HGB_ERR_ARG, "ru_pcg: sizes");
+    if (max_iter < 0 || !(delta > 0.0 && delta < 1.0)) return fail(HGB_ERR_ARG, "ru_pcg: limits (0 < delta < 1)");
+    DeviceGuard g(c->device);
+    int it = 0, upd = 0;
+    double res = 0.0;
+    long long launches = 0;
+    int st = (csr_dtype(Ai) == HGB_F32)
+                 ? ru_run<float>(c, A64, Ai, Mi, b, x, tol, delta, max_iter, &it, &upd, &res, &launches)
+                 : ru_run<uint16_t>(c, A64, Ai, Mi, b, x, tol, delta, max_iter, &it, &upd, &res, &launches);
+    if (st) return st;
+    if (info) {
+        info->iterations = it;
+        info->outer = upd;
+        info->residual = res;
+        info->true_residual = res;
+        info->kernel_launches = launches;
+    }
+    if (!(res < tol)) return fail(HGB_ERR_NOT_CONVERGED, "ru_pcg: ||b-Ax|| = %g after %d iterations (tol %g)", res, it, tol);
+    return HGB_OK;
+}
+
 // ===================================================================== GMRES ===========
 // solve_gmres (hex/solvers/hala_solvers_gmres.hpp:127-230), device resident.  The reference
 // reads the projection coefficients back to the host in every inner iteration (:67-72) and
@@ -797,13 +989,16 @@ __global__ void f64_to_inner_kernel(long n, const double *__restrict__ a, float 
 }
 }  // namespace hgb
 
-extern "C" int hgb_mixed_ir_pcg_solve(hgb_ctx *c, int n, int nnz, const int *pntr_h, const int *indx_h,
-                                      const double *vals_h, hgb_ilu *Mi, const double *b_h, double *x_h,
-                                      double tol, double inner_rtol, int max_inner, int max_outer,
-                                      hgb_solve_info *info) {
+// Host-buffer mixed solves: pntr/indx/vals (FP64) and b/x are loaded into the context's arena, the
+// inner matrix is converted on the device to Mi's store precision, the solver runs on the device
+// copies and x is read back (also when the solve did not converge).
+template <typename Solve>
+static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const int *pntr_h, const int *indx_h,
+                            const double *vals_h, hgb_ilu *Mi, const double *b_h, double *x_h, hgb_solve_info *info,
+                            Solve solve) {
     if (!c || n <= 0 || nnz < 0 || !pntr_h || !indx_h || !vals_h || !b_h || !x_h || !Mi)
-        return fail(HGB_ERR_ARG, "mixed_ir_pcg: bad arguments");
-    if (ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "mixed_ir_pcg: the preconditioner must store F32 or BF16");
+        return fail(HGB_ERR_ARG, "%s: bad arguments", what);
+    if (ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "%s: the preconditioner must store F32 or BF16", what);
     DeviceGuard g(c->device);
     const bool bf16 = ilu_store(Mi) == HGB_BF16;
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -832,7 +1027,7 @@ extern "C" int hgb_mixed_ir_pcg_solve(hgb_ctx *c, int n, int nnz, const int *pnt
     hgb_csr *A64 = nullptr, *Ai = nullptr;
     HGB_TRY(hgb_csr_create(c, n, n, nnz, dp, di, dv, HGB_F64, &A64));
     int st = hgb_csr_create(c, n, n, nnz, dp, di, dw, bf16 ? HGB_BF16 : HGB_F32, &Ai);
-    if (!st) st = hgb_ir_pcg_solve(c, A64, Ai, Mi, db, dx, tol, inner_rtol, max_inner, max_outer, info);
+    if (!st) st = solve(A64, Ai, db, dx);
     hgb_csr_destroy(A64);
     hgb_csr_destroy(Ai);
     if (info) info->kernel_launches += 1;
@@ -840,4 +1035,24 @@ extern "C" int hgb_mixed_ir_pcg_solve(hgb_ctx *c, int n, int nnz, const int *pnt
     HGB_CUDA(cudaMemcpyAsync(x_h, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     HGB_CUDA(cudaStreamSynchronize(c->stream));
     return st;
+}
+
+extern "C" int hgb_mixed_ir_pcg_solve(hgb_ctx *c, int n, int nnz, const int *pntr_h, const int *indx_h,
+                                      const double *vals_h, hgb_ilu *Mi, const double *b_h, double *x_h,
+                                      double tol, double inner_rtol, int max_inner, int max_outer,
+                                      hgb_solve_info *info) {
+    return mixed_host_solve(c, "mixed_ir_pcg", n, nnz, pntr_h, indx_h, vals_h, Mi, b_h, x_h, info,
+                            [&](hgb_csr *A64, hgb_csr *Ai, const double *db, double *dx) {
+                                return hgb_ir_pcg_solve(c, A64, Ai, Mi, db, dx, tol, inner_rtol, max_inner, max_outer,
+                                                        info);
+                            });
+}
+
+extern "C" int hgb_mixed_ru_pcg_solve(hgb_ctx *c, int n, int nnz, const int *pntr_h, const int *indx_h,
+                                      const double *vals_h, hgb_ilu *Mi, const double *b_h, double *x_h,
+                                      double tol, double delta, int max_iter, hgb_solve_info *info) {
+    return mixed_host_solve(c, "mixed_ru_pcg", n, nnz, pntr_h, indx_h, vals_h, Mi, b_h, x_h, info,
+                            [&](hgb_csr *A64, hgb_csr *Ai, const double *db, double *dx) {
+                                return hgb_ru_pcg_solve(c, A64, Ai, Mi, db, dx, tol, delta, max_iter, info);
+                            });
 }

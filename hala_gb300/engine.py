@@ -398,6 +398,17 @@ def solve_ir_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, inner_rtol=1e-4, ma
     return info
 
 
+def solve_ru_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, delta=0.01, max_iter=100000):
+    """Mixed-precision ILU(0)-PCG with FP64 reliable updates: one FP32/BF16 PCG whose residual is
+    replaced by the FP64 b - A x whenever it has dropped by delta (no reference counterpart).
+    Returns SolveInfo (iterations; outer = reliable updates)."""
+    info = SolveInfo()
+    st = _h.lib().hgb_ru_pcg_solve(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, _p(b), _p(x),
+                                   float(tol), float(delta), int(max_iter), C.byref(info))
+    check(st, "solve_ru_pcg")
+    return info
+
+
 def solve_ir_gmres(engine, A64, A_inner, ilu_inner, restart, b, x, tol, inner_rtol=1e-4, max_inner=3000,
                    max_outer=50):
     """Mixed-precision ILU(0)-GMRES(restart): FP32/BF16 inner solves, FP64 refinement to
@@ -438,6 +449,18 @@ def solve_ir_pcg_mixed(engine, tol, pntr_h, indx_h, vals_h, ilu_inner, b_h, x_h,
                                           ilu_inner.h, b_h.ctypes.data_as(C.c_void_p),
                                           x_h.ctypes.data_as(C.c_void_p), float(tol), float(inner_rtol),
                                           int(max_inner), int(max_outer), C.byref(info)), "solve_ir_pcg (mixed)")
+    return info
+
+
+def solve_ru_pcg_mixed(engine, tol, pntr_h, indx_h, vals_h, ilu_inner, b_h, x_h, delta=0.01, max_iter=100000):
+    """Host-buffer mixed-precision PCG with reliable updates (hgb_mixed_ru_pcg_solve).  Returns SolveInfo."""
+    info = SolveInfo()
+    n = pntr_h.size - 1
+    check(_h.lib().hgb_mixed_ru_pcg_solve(engine.h, n, indx_h.size, pntr_h.ctypes.data_as(C.c_void_p),
+                                          indx_h.ctypes.data_as(C.c_void_p), vals_h.ctypes.data_as(C.c_void_p),
+                                          ilu_inner.h, b_h.ctypes.data_as(C.c_void_p),
+                                          x_h.ctypes.data_as(C.c_void_p), float(tol), float(delta), int(max_iter),
+                                          C.byref(info)), "solve_ru_pcg (mixed)")
     return info
 
 

@@ -208,6 +208,16 @@ int hgb_ir_pcg_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_in
 int hgb_ir_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, char trans,
                         const double *b, double *x, double tol, double inner_rtol, int max_inner,
                         int max_outer, hgb_solve_info *info);
+/* Mixed precision PCG with reliable updates (van der Vorst and Ye, SIAM J. Sci. Comput. 22,
+ * 2000): one ILU(0)-PCG on A_inner (F32 or BF16 values, FP32 vectors) with M_inner (store F32
+ * or BF16) on the correction d; when ||r|| drops below delta (0 < delta < 1) times its largest
+ * value since the last update, or below tol, or at max_iter, x += d in FP64 and r = b - A64 x
+ * in FP64, continuing with the same search direction.  Keeps the Krylov space (FP64 PCG's
+ * iteration count) where hgb_ir_pcg_solve restarts it per sweep.  Stops when the FP64
+ * ||b - A x||_2 < tol.  info->iterations: inner iterations, info->outer: reliable updates.
+ * No reference counterpart. */
+int hgb_ru_pcg_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, const double *b,
+                     double *x, double tol, double delta, int max_iter, hgb_solve_info *info);
 /* solve_gmres / solve_gmres_ilu over gpu_engine (hex/solvers/hala_solvers_gmres.hpp:127-267):
  * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations in
  * the reference's order.  The rotations and the back substitution run on the device and one
@@ -239,6 +249,10 @@ int hgb_mixed_ir_pcg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, c
                            const double *vals_host, hgb_ilu *M_inner, const double *b_host,
                            double *x_host, double tol, double inner_rtol, int max_inner,
                            int max_outer, hgb_solve_info *info);
+/* Host-buffer form of hgb_ru_pcg_solve, loaded and converted as hgb_mixed_ir_pcg_solve. */
+int hgb_mixed_ru_pcg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const int *indx_host,
+                           const double *vals_host, hgb_ilu *M_inner, const double *b_host,
+                           double *x_host, double tol, double delta, int max_iter, hgb_solve_info *info);
 
 /* ------------------------------------------ batched independent systems (no reference
  * counterpart: the reference's batch is one matrix with many right-hand sides) -------------- */

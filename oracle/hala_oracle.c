@@ -355,3 +355,66 @@ int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, con
     free(r); free(rf); free(d);
     return total;
 }
+
+/* Mixed-precision PCG with reliable updates (no reference counterpart): one FP32 ILU(0)-PCG
+ * (solve_cg_core's order, FP32 vectors, inner products in double) on the correction; whenever
+ * the iterated residual falls below delta times its largest value since the last update, the
+ * correction is added to x in FP64, the residual is recomputed as b - A x in FP64 and the
+ * iteration continues from it with the same search direction.  Stops when the FP64 residual
+ * after an update is below tol (an update is forced when the iterated residual is below tol and
+ * at the iteration limit).
+ * Returns the iterations; *updates_out gets the number of reliable updates. */
+int or_ru_pcg(int n, const int *pntr, const int *indx, const double *vals, const float *vals32,
+              const int *diag, const float *ilu32, const double *piv, const double *b, double *x,
+              double tol, double delta, int max_iter, int *updates_out) {
+    if (updates_out) *updates_out = 0;
+    if (n <= 0) return 0;
+    size_t nd = sizeof(double) * (size_t)n, nf = sizeof(float) * (size_t)n;
+    double *r64 = (double *)malloc(nd);
+    float *r = (float *)malloc(nf), *d = (float *)malloc(nf), *p = (float *)malloc(nf);
+    float *Ap = (float *)malloc(nf), *z = (float *)malloc(nf);
+    int it = 0, updates = 0;
+    or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r64);
+    for (int i = 0; i < n; i++) r64[i] = b[i] - r64[i];
+    double rn = dnorm(n, r64), rmax = rn;
+    if (rn < tol) { free(r64); free(r); free(d); free(p); free(Ap); free(z); if (updates_out) *updates_out = 0; return 0; }
+    for (int i = 0; i < n; i++) { r[i] = (float)r64[i]; d[i] = 0.0f; }
+    memcpy(z, r, nf);
+    ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, z);
+    memcpy(p, z, nf);
+    double zr = 0;
+    for (int i = 0; i < n; i++) zr += (double)r[i] * z[i];
+    while (it < max_iter) {
+        or_spmv_f('N', n, n, 1.0f, pntr, indx, vals32, p, 0.0f, Ap);
+        it++;
+        double pap = 0;
+        for (int i = 0; i < n; i++) pap += (double)p[i] * Ap[i];
+        float a = (float)(zr / pap);
+        for (int i = 0; i < n; i++) d[i] += a * p[i];
+        double s = 0;
+        for (int i = 0; i < n; i++) { r[i] -= a * Ap[i]; s += (double)r[i] * r[i]; }
+        rn = sqrt(s);
+        if (rn > rmax) rmax = rn;
+        if (rn < delta * rmax || rn < tol || !(rn == rn) || it >= max_iter) {
+            /* reliable update: x += d (FP64), r = b - A x (FP64) */
+            for (int i = 0; i < n; i++) { x[i] += (double)d[i]; d[i] = 0.0f; }
+            or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r64);
+            s = 0;
+            for (int i = 0; i < n; i++) { r64[i] = b[i] - r64[i]; s += r64[i] * r64[i]; r[i] = (float)r64[i]; }
+            rn = sqrt(s);
+            rmax = rn;
+            updates++;
+            if (rn < tol || !(rn == rn) || it >= max_iter) break;
+        }
+        memcpy(z, r, nf);
+        ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, z);
+        double nzr = 0;
+        for (int i = 0; i < n; i++) nzr += (double)r[i] * z[i];
+        float bt = (float)(nzr / zr);
+        for (int i = 0; i < n; i++) p[i] = bt * p[i] + z[i];
+        zr = nzr;
+    }
+    if (updates_out) *updates_out = updates;
+    free(r64); free(r); free(d); free(p); free(Ap); free(z);
+    return it;
+}

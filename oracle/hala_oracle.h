@@ -98,6 +98,15 @@ int or_ir_pcg(int n, const int *pntr, const int *indx, const double *vals, const
               const int *diag, const float *ilu32, const double *piv, const double *b, double *x,
               double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out);
 
+/* Mixed-precision PCG with reliable updates (no reference counterpart): one FP32 ILU(0)-PCG on
+ * the correction d (inner products in double); when ||r|| < delta * (its largest value since the
+ * last update), or ||r|| < tol, or at max_iter: x += d in FP64, r = b - A x in FP64, and the
+ * iteration continues with the same direction.  Stops when that FP64 residual is below tol.
+ * Returns the iterations; *updates_out gets the reliable updates. */
+int or_ru_pcg(int n, const int *pntr, const int *indx, const double *vals, const float *vals32,
+              const int *diag, const float *ilu32, const double *piv, const double *b, double *x,
+              double tol, double delta, int max_iter, int *updates_out);
+
 /* Mixed-precision GMRES (no reference counterpart): outer r = b - A x in FP64, inner
  * GMRES(restart) (solve_gmres's loop) in FP32 vectors with double inner products and rotations,
  * on (vals32, ilu32 with FP64 pivots piv), each sweep to a relative preconditioned tolerance,

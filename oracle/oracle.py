@@ -65,6 +65,9 @@ def _load():
     lib.or_ir_gmres.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, i, _f64p, _f64p,
                                 C.c_double, C.c_double, i, i, C.POINTER(i)]
     lib.or_ir_gmres.restype = i
+    lib.or_ru_pcg.argtypes = [i, _i32p, _i32p, _f64p, _f32p, _i32p, _f32p, _f64p, _f64p, _f64p,
+                              C.c_double, C.c_double, i, C.POINTER(i)]
+    lib.or_ru_pcg.restype = i
     return lib
 
 
@@ -242,6 +245,17 @@ def ir_pcg(pntr, indx, vals, vals32, diag, ilu32, piv, b, tol, inner_rtol=1e-4, 
     tot = lib().or_ir_pcg(n, pntr, indx, vals, vals32, diag, ilu32, piv, b, x, tol, inner_rtol,
                           max_inner, max_outer, C.byref(outer))
     return x, tot, outer.value
+
+
+def ru_pcg(pntr, indx, vals, vals32, diag, ilu32, piv, b, tol, delta=0.1, max_iter=100000, x0=None):
+    """Mixed FP32 ILU(0)-PCG with FP64 reliable updates (no reference counterpart).
+    Returns (x, iterations, reliable updates)."""
+    n = len(pntr) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    upd = C.c_int(0)
+    it = lib().or_ru_pcg(n, pntr, indx, vals, vals32, diag, ilu32, piv, b, x, tol, delta, max_iter,
+                         C.byref(upd))
+    return x, it, upd.value
 
 
 def ir_gmres(pntr, indx, vals, vals32, diag, ilu32, piv, restart, b, tol, inner_rtol=1e-4, max_inner=3000,

@@ -18,7 +18,7 @@ def declared_symbols():
 def test_header_declares_the_path():
     names = declared_symbols()
     for must in ("hgb_spmv_f64", "hgb_ilu0_create", "hgb_ilu0_apply", "hgb_tri_solve", "hgb_cg_solve",
-                 "hgb_gmres_solve", "hgb_ir_pcg_solve", "hgb_ir_gmres_solve", "hgb_dot_f64", "hgb_nrm2_f64", "hgb_axpy_f64"):
+                 "hgb_gmres_solve", "hgb_ir_pcg_solve", "hgb_ir_gmres_solve", "hgb_ru_pcg_solve", "hgb_dot_f64", "hgb_nrm2_f64", "hgb_axpy_f64"):
         assert must in names
 
 

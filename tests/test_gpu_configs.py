@@ -101,6 +101,22 @@ def test_pcg_aniso128_mixed(eng, aniso128, store):
     assert info.outer >= 2
 
 
+def test_ru_pcg_aniso128(eng, aniso128):
+    # mixed FP32 PCG with FP64 reliable updates: FP64 PCG's iteration count at 128^3
+    p, i, v, xt, b, tol, xo, ito = aniso128
+    n = len(p) - 1
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    A32 = E.make_sparse_matrix(eng, n, gp, gi, gv.to(torch.float32))
+    M32 = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    info = E.solve_ru_pcg(eng, A64, A32, M32, T(b), x, tol, delta=0.01)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
+    assert within5(info.iterations, ito - 1), (info.iterations, ito)
+
+
 @pytest.fixture(scope="module")
 def convdiff96(eng):
     p, i, v = P.convdiff3d(96)

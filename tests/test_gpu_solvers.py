@@ -245,3 +245,72 @@ def test_ir_gmres(eng, rng, inner):
                                     inner_rtol=rtol)
         assert info.outer == outer, (info.outer, outer)
         assert within5(info.iterations, tot), (info.iterations, tot)
+
+
+@pytest.mark.parametrize("store", [torch.float32, torch.bfloat16])
+def test_ru_pcg(eng, rng, store):
+    p, i, v = P.aniso3d(32)
+    n = len(p) - 1
+    xt = rng.standard_normal(n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    xo, ito, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    A32 = E.make_sparse_matrix(eng, n, gp, gi, gv.to(torch.float32))
+    M = E.make_ilu(eng, gp, gi, gv, store=store)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    info = E.solve_ru_pcg(eng, A64, A32, M, T(b), x, tol, delta=0.01)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
+    assert abs(info.true_residual - np.linalg.norm(b - P.csr_matvec(p, i, v, xs))) <= 1e-3 * tol
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
+    # the Krylov space is kept across updates: FP64 PCG's iterations (its count includes the
+    # initial residual), not a restarted refinement's
+    assert within5(info.iterations, ito - 1), (info.iterations, ito)
+    if store == torch.float32:
+        _, it_o, upd_o = O.ru_pcg(p, i, v, v.astype(np.float32), do, fo.astype(np.float32), fo[do], b, tol,
+                                  delta=0.01)
+        assert within5(info.iterations, it_o), (info.iterations, it_o)
+        assert abs(info.outer - upd_o) <= 1, (info.outer, upd_o)
+
+
+def test_ru_pcg_iteration_limit(eng, rng):
+    from hala_gb300.hgb import HgbError
+    p, i, v = P.aniso3d(16)
+    n = len(p) - 1
+    b = rng.standard_normal(n)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    A32 = E.make_sparse_matrix(eng, n, gp, gi, gv.to(torch.float32))
+    M = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    with pytest.raises(HgbError):
+        E.solve_ru_pcg(eng, A64, A32, M, T(b), x, 1e-12, max_iter=6)
+    # the correction of the six iterations is in x: the oracle's iterate after the same six
+    xo, it_o, _ = O.ru_pcg(p, i, v, v.astype(np.float32), do, fo.astype(np.float32), fo[do], b, 1e-12, max_iter=6)
+    assert it_o == 6
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-5 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("solver", ["ir", "ru"])
+def test_mixed_host_buffers(eng, rng, solver):
+    # host pntr/indx/vals/b/x in, x out: the end-to-end entry points of the mixed solves
+    p, i, v = P.aniso3d(20)
+    n = len(p) - 1
+    xt = rng.standard_normal(n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    M = E.make_ilu(eng, T(p), T(i), T(v), store=torch.float32)
+    x = np.zeros(n)
+    if solver == "ir":
+        info = E.solve_ir_pcg_mixed(eng, tol, p, i, v, M, b, x, inner_rtol=1e-4)
+    else:
+        info = E.solve_ru_pcg_mixed(eng, tol, p, i, v, M, b, x, delta=0.01)
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, x)) < tol
+    assert info.true_residual < tol
+    fo, do, _ = O.ilu_factor(p, i, v)
+    xo, _, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
+    assert np.linalg.norm(x - xo) <= 1e-7 * np.linalg.norm(xo)

@@ -132,6 +132,23 @@ def test_ir_pcg_reaches_tolerance(rng):
     assert outer >= 2
 
 
+def test_ru_pcg_keeps_fp64_iterations(rng):
+    p, i, v = P.aniso3d(12)
+    n = len(p) - 1
+    xt = rng.standard_normal(n)
+    b = P.csr_matvec(p, i, v, xt)
+    tol = 1e-10 * np.linalg.norm(b)
+    f, d, _ = O.ilu_factor(p, i, v)
+    _, it64, _ = O.cg(p, i, v, b, tol=tol, diag=d, ilu=f)
+    x, it, upd = O.ru_pcg(p, i, v, v.astype(np.float32), d, f.astype(np.float32), f[d], b, tol, delta=0.01)
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, x)) < tol
+    assert upd >= 2 and abs(it - (it64 - 1)) <= 2, (it, it64, upd)
+    # at the iteration limit the correction is folded into x and the FP64 residual reported
+    x5, it5, upd5 = O.ru_pcg(p, i, v, v.astype(np.float32), d, f.astype(np.float32), f[d], b, tol, max_iter=5)
+    assert it5 == 5 and upd5 >= 1
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, x5)) < 0.5 * np.linalg.norm(b)
+
+
 @pytest.mark.parametrize("restart", [5, 30])
 def test_ir_gmres_reaches_tolerance(rng, restart):
     p, i, v = P.convdiff3d(12)
