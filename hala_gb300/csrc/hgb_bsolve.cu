@@ -60,7 +60,7 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
 }
 
 inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
-constexpr int kBsMaxCluster = 8;   // portable thread-block cluster size
+constexpr int kBsMaxCluster = 16;  // largest thread-block cluster (above 8: non-portable sizes)
 
 // shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
 //                 remote-value ring kBsF x 128 | solution slice + zero slot]
@@ -322,6 +322,19 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 for (int q = 0; q < 4; q++)   // rows whose value the block before has not offered yet
                     if (jq[q] >= 0 && RingTag<X>::bits(vslot[32 * q]) == want) todo |= 1u << q;
                 spins = 0;
+                // one lane polls a single value of the step until it is produced, then the warp
+                // loads them all: one L2 load per round instead of one per row keeps the memory
+                // pipeline, which the solver threads' shared-memory accesses go through, free
+                const unsigned lanes = __ballot_sync(0xFFFFFFFFu, todo != 0);
+                if (lanes && l == __ffs(lanes) - 1) {
+                    const int q0 = __ffs(todo) - 1;
+                    const int jrep = q0 == 0 ? jq[0] : (q0 == 1 ? jq[1] : (q0 == 2 ? jq[2] : jq[3]));
+                    while (Pending<X>::is(ld_relaxed(out + jrep))) {
+                        if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) break;
+                        __nanosleep(32);
+                    }
+                }
+                __syncwarp();
                 while (todo) {
                     X v[4];
 #pragma unroll
@@ -572,7 +585,8 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
     if (c->device < 0 || c->device >= 64 || cl < 1 || cl > kBsMaxCluster) return 0;
     if (init[c->device][ri][cl]) return cache[c->device][ri][cl];
     auto fits = [&](auto kernel, size_t smem) {
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            (cl > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
             cudaGetLastError();
             return 0;
         }
@@ -603,15 +617,20 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
     return n;
 }
 
-// Cluster size: the largest of 8, 4, 2 at which a cluster fits.  Measured at 128^3 (128 blocks):
-// clusters of 8 (15 co-resident, so the last 8 blocks start when a cluster frees up) beat
-// clusters of 4 (all 128 co-resident, twice the hops through L2): 0.43 vs 0.51 ms per FP32-store
-// apply, 0.83 vs 0.93 ms FP64.  HGB_BS_CLUSTER caps the size (1: no clusters, for comparisons).
+// Cluster size.  Every hop between clusters goes through L2 and the fetcher warps, a hop inside a
+// cluster through distributed shared memory; and a block whose cluster is not co-resident starts
+// only when another cluster has finished all its blocks.  So: the largest size (up to 16, sizes
+// above 8 being non-portable) at which the clusters of all nblk blocks are co-resident; failing
+// that, the largest of 8, 4, 2 that fits.  On GB300 (one CTA per SM) 15 clusters of 8 are
+// co-resident, so for 128 blocks a size between 9 and 16 that still fits 128 CTAs at once removes
+// the wait for a free cluster.  HGB_BS_CLUSTER caps the size (1: no clusters, for comparisons).
 static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
     const char *e = getenv("HGB_BS_CLUSTER");
     const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
     if (nblk < 2) return 1;
-    for (int cl = cap; cl > 1; cl /= 2)
+    for (int cl = std::min(cap, nblk); cl > 1; cl--)
+        if ((long)bs_clusters_fit(c, R, cl) * cl >= nblk) return cl;
+    for (int cl = std::min(cap, 8); cl > 1; cl /= 2)
         if (bs_clusters_fit(c, R, cl) >= 1) return cl;
     return 1;
 }
@@ -842,6 +861,8 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
             return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem_max, mx);
         HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem_max));
+        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>,
+                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         attr_dev = c->device;
     }
     if (smem > smem_max) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %d rows per block", S.R);
