@@ -85,6 +85,31 @@ template <> struct Val<uint16_t> {   // bfloat16 bit pattern
     __device__ static float get(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
 };
 
+// Per-thread running sum of products for the grid reductions.  FP64 data: a double sum.  FP32
+// data: a float sum (FMA) flushed into a double every 16 terms.  The FP64 pipe of sm_103 is narrow
+// (a warp-wide FP64 instruction holds it for 64 cycles), so converting every FP32 term to double
+// and accumulating it with an FP64 FMA bounds an FP32 reduction by the FP64 pipe rather than by
+// memory; the float partials of 16 terms keep the per-thread error at the FP32 level of the data.
+template <typename X> struct DotAcc {
+    double d = 0.0;
+    __device__ __forceinline__ void add(X a, X b) { d += (double)a * (double)b; }
+    __device__ __forceinline__ double get() const { return d; }
+};
+template <> struct DotAcc<float> {
+    double d = 0.0;
+    float f = 0.0f;
+    int k = 0;
+    __device__ __forceinline__ void add(float a, float b) {
+        f = __fmaf_rn(a, b, f);
+        if (++k == 16) {
+            d += (double)f;
+            f = 0.0f;
+            k = 0;
+        }
+    }
+    __device__ __forceinline__ double get() const { return d + (double)f; }
+};
+
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }

@@ -25,9 +25,10 @@ template <typename X>
 __global__ void mr_dot_partial_kernel(long n, int nparts, const X *__restrict__ x, const X *__restrict__ y,
                                       double *__restrict__ partial) {
     const long off = (long)blockIdx.y * n;
-    double acc[1] = {0.0};
+    DotAcc<X> d;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        acc[0] += (double)x[off + i] * (double)y[off + i];
+        d.add(x[off + i], y[off + i]);
+    double acc[1] = {d.get()};
     block_sum<1>(acc);
     if (threadIdx.x == 0) partial[blockIdx.y * nparts + blockIdx.x] = acc[0];
 }

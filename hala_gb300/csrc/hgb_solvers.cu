@@ -27,13 +27,14 @@ __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in,
     // a = <r,z> / <p,Ap>; x += a p; r -= a Ap  (axpy(a,p,x), axpy(-a,Ap,r))
     const X a = (X)(s_in->zr / s_in->pap);
     const X ma = -a;
-    double acc[1] = {0.0};
+    DotAcc<X> rr;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         x[i] = add_rn(x[i], mul_rn(a, p[i]));
         X ri = add_rn(r[i], mul_rn(ma, Ap[i]));
         r[i] = ri;
-        acc[0] += (double)ri * (double)ri;
+        rr.add(ri, ri);
     }
+    double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
         s->rr = v[0];
         s->it += 1;
@@ -45,11 +46,13 @@ template <typename X>
 __global__ void cg_rz_kernel(long n, SolverScalars *s, const X *__restrict__ r, const X *__restrict__ z,
                              double *partials, unsigned *counter, int init) {
     if (!init && s->done) return;
-    double acc[2] = {0.0, 0.0};
+    DotAcc<X> rz, rr;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        acc[0] += (double)r[i] * (double)z[i];
-        if (init) acc[1] += (double)r[i] * (double)r[i];
+        const X ri = r[i];
+        rz.add(ri, z[i]);
+        if (init) rr.add(ri, ri);
     }
+    double acc[2] = {rz.get(), rr.get()};
     grid_sum<2>(acc, partials, counter, [&](double (&v)[2]) {
         s->nzr = s->zr;      // previous <r,z>, used by the p update
         s->zr = v[0];
@@ -376,13 +379,14 @@ __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict
     if (s->done) return;
     const float a = (float)(s->zr / s->pap);
     const float ma = -a;
-    double acc[1] = {0.0};
+    DotAcc<float> rr;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         d[i] = __fadd_rn(d[i], __fmul_rn(a, p[i]));
         const float ri = __fadd_rn(r[i], __fmul_rn(ma, Ap[i]));
         r[i] = ri;
-        acc[0] += (double)ri * (double)ri;
+        rr.add(ri, ri);
     }
+    double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
         const double rr = v[0];
         s->rr = rr;

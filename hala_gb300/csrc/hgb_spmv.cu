@@ -72,7 +72,7 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
     __syncthreads();
     const bool use_tma = tma != 0;
     const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    double dsum[1] = {0.0};
+    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
     if (tid >= kSpmvRows) {
         // producer warp
         const int lane = tid & 31;
@@ -155,13 +155,14 @@ spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *_
                 }
                 X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
                 y[r] = out;
-                if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
+                if (FUSE_DOT) dacc.add(__ldg(x + r), out);
             }
             named_bar_sync(1, kSpmvRows);   // every consumer is done with stage st
             if (tid == 0) mbar_arrive(&empty[st]);
         }
     }
     if (FUSE_DOT) {
+        double dsum[1] = {dacc.get()};
         grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
     }
 }
@@ -176,7 +177,7 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
                    double *dot_out, const int *skip) {
     using X = typename Val<V>::X;
     if (skip && *skip) return;
-    double dsum[1] = {0.0};
+    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
         const int ps = __ldg(pntr + r), pe = __ldg(pntr + r + 1);
         X acc = X(0);
@@ -194,9 +195,12 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
         }
         X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
         y[r] = out;
-        if (FUSE_DOT) dsum[0] += (double)__ldg(x + r) * (double)out;
+        if (FUSE_DOT) dacc.add(__ldg(x + r), out);
     }
-    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    if (FUSE_DOT) {
+        double dsum[1] = {dacc.get()};
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    }
 }
 
 // Warp-tiled SpMV: each warp owns a contiguous run of 32-row tiles.  For every tile it copies the
@@ -230,7 +234,7 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
     const long per = (ntiles + nwarps - 1) / nwarps;
     const long tb = ((long)blockIdx.x * (kWarpBlock / 32) + wib) * per;
     const long te = min(ntiles, tb + per);
-    double dsum[1] = {0.0};
+    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
 
     // lane's row pointers of tile k (loads only; nothing waits on them yet)
     auto load_ptrs = [&](long k, int &ps, int &pe) {
@@ -309,7 +313,7 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
                 }
                 const X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[row]));
                 y[row] = out;
-                if (FUSE_DOT) dsum[0] += (double)__ldg(x + row) * (double)out;
+                if (FUSE_DOT) dacc.add(__ldg(x + row), out);
             }
             __syncwarp();   // buffer buf is refilled by tile k+2
             ps0 = ps1;
@@ -321,7 +325,10 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
         }
     }
     cp_async_wait<0>();
-    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    if (FUSE_DOT) {
+        double dsum[1] = {dacc.get()};
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    }
 }
 
 // SpMV variant: warp-tiled (default), "direct" (thread per row, no staging) or "tma" (CTA-wide
@@ -368,7 +375,7 @@ __global__ void spmv_t_cached_kernel(int n_cols, const int *__restrict__ pntrT, 
                                      unsigned *counter, double *dot_out, const int *skip) {
     using X = typename Val<V>::X;
     if (skip && *skip) return;
-    double dsum[1] = {0.0};
+    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_cols; c += gridDim.x * blockDim.x) {
         X acc = (beta == X(0)) ? X(0) : mul_rn(beta, y[c]);
         for (int p = __ldg(pntrT + c); p < __ldg(pntrT + c + 1); p++) {
@@ -376,9 +383,12 @@ __global__ void spmv_t_cached_kernel(int n_cols, const int *__restrict__ pntrT, 
             acc = add_rn(acc, mul_rn(mul_rn(alpha, __ldg(x + i)), Val<V>::get(__ldg(vals + __ldg(mapT + p)))));
         }
         y[c] = acc;
-        if (FUSE_DOT) dsum[0] += (double)dot_x[c] * (double)acc;
+        if (FUSE_DOT) dacc.add(dot_x[c], acc);
     }
-    if (FUSE_DOT) grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    if (FUSE_DOT) {
+        double dsum[1] = {dacc.get()};
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    }
 }
 
 // ------------------------------------------------------------- CSR validation ----------
