@@ -13,10 +13,11 @@
 // streams its own row packets (three dependency codes and the row's slot, then the values and
 // diagonal terms, 16-byte pieces) D steps ahead into a private shared-memory ring with cp.async,
 // one commit group per step, so no handshake between warps sits on that path; a named barrier
-// ends each level.  Four fetcher warps poll the first dependency on an earlier block of every row
-// in the coming steps from L2 (many loads in flight, re-polled until produced) and deposit each
-// value in a shared-memory ring as soon as it is ready.  A solver thread therefore waits on
-// shared memory, not on an L2 round trip, when it needs a value from the block before.  The
+// ends each level.  Four fetcher warps take the coming steps in turn: a warp polls one value of
+// its step in L2 until it is produced, then loads the first dependency on an earlier block of
+// every row of the step (re-polling the few not yet produced) and deposits each value in a
+// shared-memory ring.  A solver thread therefore waits on shared memory, not on an L2 round trip,
+// when it needs a value from the block before.  The
 // launch groups the CTAs into thread-block clusters that take consecutive blocks: inside a
 // cluster, the CTA of block b also offers each value that block b+1 needs first straight to the
 // ring of block b+1's CTA (a compare-and-swap in distributed shared memory), so most hops between
