@@ -49,6 +49,8 @@ struct SolverScalars {
     // 0 while an update is due in the current iteration, updates so far
     double rmax2, delta2;
     int ru_skip, updates;
+    double last2;                // ||r||^2 after the previous update
+    int restart, pad2;           // 1: the next direction update restarts (beta = 0)
 };
 
 }  // namespace hgb

@@ -353,7 +353,8 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
 // strategies for Krylov subspace iterative methods for the convergence of true residuals",
 // SIAM J. Sci. Comput. 22 (2000)): when ||r|| falls below delta times its largest value since
 // the last update (or below tol, or at the iteration limit), x += d in FP64, r = b - A x in FP64
-// and the iteration continues from the new residual with the same search direction.  Unlike a
+// and the iteration continues from the new residual with the same search direction, or restarts
+// (beta = 0) when that update reduced the FP64 residual less than twice.  Unlike a
 // restarted refinement, the Krylov space is kept, so the iterations stay those of FP64 PCG.
 // No reference counterpart.  One iteration is nine launches, three of them (the update) no-ops
 // except in update iterations; kItersPerGraph iterations are one CUDA graph.
@@ -371,6 +372,8 @@ __global__ void ru_init_kernel(SolverScalars *s, double tol2, double delta2, dou
     s->delta2 = delta2;
     s->ru_skip = 1;
     s->updates = 0;
+    s->last2 = rr;
+    s->restart = 0;
 }
 
 // a = <r,z>/<p,Ap>; d += a p; r -= a Ap; ||r||^2; decide whether this iteration updates
@@ -394,6 +397,7 @@ __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict
         s->rmax2 = fmax(s->rmax2, rr);
         const bool upd = (rr < s->delta2 * s->rmax2) || (rr < s->tol2) || !(rr == rr) || (s->it >= s->max_iter);
         s->ru_skip = upd ? 0 : 1;
+        s->restart = 0;
     });
 }
 
@@ -425,23 +429,36 @@ __global__ void ru_replace_kernel(long n, SolverScalars *s, const double *__rest
         s->updates += 1;
         s->done = (rr < s->tol2) || !(rr == rr) || (s->it >= s->max_iter);
         s->ru_skip = 1;
+        // an update that reduced ||r|| less than twice: the kept directions are stale (FP32
+        // recurrences on an ill-conditioned operator), restart from the new residual
+        s->restart = rr > 0.25 * s->last2;
+        s->last2 = rr;
     });
+}
+
+// p = beta p + z with beta = <r,z> / <r,z>_old, or p = z after a restart
+__global__ void ru_p_kernel(long n, const SolverScalars *__restrict__ s, float *__restrict__ p,
+                            const float *__restrict__ z) {
+    if (s->done) return;
+    const float bta = s->restart ? 0.0f : (float)(s->zr / s->nzr);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        p[i] = __fadd_rn(__fmul_rn(bta, p[i]), z[i]);
 }
 
 template <typename V>
 static int ru_iteration(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, CgWork<float> &w, float *d, double *x,
-                        double *r64, const double *b, long n) {
+                        double *r64, const double *b, long n, bool trans) {
     SolverScalars *s = c->scal;
     const int *done = &s->done;
-    HGB_TRY(spmv_A<V, float>(c, Ai, 1.0f, w.p, 0.0f, w.Ap, &s->pap, done));
+    HGB_TRY(spmv_A<V, float>(c, Ai, 1.0f, w.p, 0.0f, w.Ap, &s->pap, done, trans));
     ru_step_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.p, w.Ap, d, w.r, c->partials, c->counter);
     ru_fold_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, b, d, x, r64);
-    HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r64, nullptr, &s->ru_skip));
+    HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r64, nullptr, &s->ru_skip, trans));
     ru_replace_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, r64, w.r, c->partials, c->counter);
     float *z = M ? w.z : w.r;
-    if (M) HGB_TRY(ilu_apply_internal(M, 'N', w.r, w.z, done));
+    if (M) HGB_TRY(ilu_apply_internal(M, trans ? 'T' : 'N', w.r, w.z, done));
     cg_rz_kernel<float><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
-    cg_p_kernel<float><<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, w.p, z);
+    ru_p_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, w.p, z);
     return launch_check("ru iteration");
 }
 
@@ -449,7 +466,8 @@ static int ru_launches_per_iter(bool precond) { return precond ? 9 : 7; }
 
 template <typename V>
 static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const double *b, double *x, double tol,
-                  double delta, int max_iter, int *iters, int *updates, double *res, long long *launches) {
+                  double delta, int max_iter, int *iters, int *updates, double *res, long long *launches,
+                  bool trans = false) {
     const long n = csr_rows(A64);
     CaptureStream cs(c);
     CgWork<float> w;
@@ -466,7 +484,8 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
             break;
         }
         double rn = 0.0;
-        if ((st = true_residual(c, A64, b, x, r64, &rn, launches))) break;
+        if (trans && (st = csr_ensure_transpose(Ai))) break;
+        if ((st = true_residual(c, A64, b, x, r64, &rn, launches, trans))) break;
         *iters = 0;
         *updates = 0;
         *res = rn;
@@ -476,14 +495,14 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
         f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, w.r);
         zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d);
         float *z = M ? w.z : w.r;
-        if (M && (st = ilu_apply_internal(M, 'N', w.r, w.z, nullptr))) break;
+        if (M && (st = ilu_apply_internal(M, trans ? 'T' : 'N', w.r, w.z, nullptr))) break;
         copy_kernel<float><<<ew_grid(c, n), 256, 0, c->stream>>>(n, z, w.p);
         // <r,z> of the first direction (the rr slot keeps the FP64 residual)
         cg_rz_kernel<float><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
         *launches += 5 + (M ? 2 : 0);
         if ((st = launch_check("ru init"))) break;
         if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)) { st = cuda_fail(cudaGetLastError(), "begin capture"); break; }
-        for (int k = 0; k < kItersPerGraph && !st; k++) st = ru_iteration<V>(c, A64, Ai, M, w, d, x, r64, b, n);
+        for (int k = 0; k < kItersPerGraph && !st; k++) st = ru_iteration<V>(c, A64, Ai, M, w, d, x, r64, b, n, trans);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
         if (st) break;
         if (ce != cudaSuccess) { st = cuda_fail(ce, "end capture"); break; }
@@ -513,7 +532,15 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
 
 extern "C" int hgb_ru_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, const double *b, double *x,
                                 double tol, double delta, int max_iter, hgb_solve_info *info) {
+    return hgb_ru_pcg_solve_op(c, A64, Ai, Mi, 'N', b, x, tol, delta, max_iter, info);
+}
+
+extern "C" int hgb_ru_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char trans, const double *b,
+                                   double *x, double tol, double delta, int max_iter, hgb_solve_info *info) {
     if (!c || !A64 || !Ai || !b || !x) return fail(HGB_ERR_ARG, "ru_pcg: bad arguments");
+    const bool tr = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
+    if (!tr && trans != 'N' && trans != 'n') return fail(HGB_ERR_ARG, "ru_pcg: trans '%c'", trans);
+    if (tr && csr_dtype(Ai) == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "ru_pcg: transposed solve with a bf16 matrix");
     if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the outer matrix must be F64");
     if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the inner matrix must be F32 or BF16");
     if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the preconditioner must store F32 or BF16");
@@ -526,7 +553,7 @@ extern "C" int hgb_ru_pcg_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *
     double res = 0.0;
     long long launches = 0;
     int st = (csr_dtype(Ai) == HGB_F32)
-                 ? ru_run<float>(c, A64, Ai, Mi, b, x, tol, delta, max_iter, &it, &upd, &res, &launches)
+                 ? ru_run<float>(c, A64, Ai, Mi, b, x, tol, delta, max_iter, &it, &upd, &res, &launches, tr)
                  : ru_run<uint16_t>(c, A64, Ai, Mi, b, x, tol, delta, max_iter, &it, &upd, &res, &launches);
     if (st) return st;
     if (info) {

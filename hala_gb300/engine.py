@@ -409,6 +409,15 @@ def solve_ru_pcg(engine, A64, A_inner, ilu_inner, b, x, tol, delta=0.01, max_ite
     return info
 
 
+def solve_ru_pcg_op(engine, A64, A_inner, ilu_inner, trans, b, x, tol, delta=0.01, max_iter=100000):
+    """solve_ru_pcg on op(A) ('N' or 'T'): the adjoint solve of the mixed forward solve."""
+    info = SolveInfo()
+    st = _h.lib().hgb_ru_pcg_solve_op(engine.h, A64.h, A_inner.h, ilu_inner.h if ilu_inner else None, ch_(trans),
+                                      _p(b), _p(x), float(tol), float(delta), int(max_iter), C.byref(info))
+    check(st, "solve_ru_pcg")
+    return info
+
+
 def solve_ir_gmres(engine, A64, A_inner, ilu_inner, restart, b, x, tol, inner_rtol=1e-4, max_inner=3000,
                    max_outer=50):
     """Mixed-precision ILU(0)-GMRES(restart): FP32/BF16 inner solves, FP64 refinement to

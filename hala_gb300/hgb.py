@@ -81,6 +81,7 @@ _SIGS = {
     "hgb_csr_pattern_grad": ([vp, f64, vp, vp, vp], i32),
     "hgb_gmres_solve": ([vp, vp, vp, i32, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_ru_pcg_solve": ([vp, vp, vp, vp, vp, vp, f64, f64, i32, C.POINTER(SolveInfo)], i32),
+    "hgb_ru_pcg_solve_op": ([vp, vp, vp, vp, ch, vp, vp, f64, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_ir_gmres_solve": ([vp, vp, vp, vp, i32, vp, vp, f64, f64, i32, i32, C.POINTER(SolveInfo)], i32),
     "hgb_mixed_cg_solve": ([vp, i32, i32, vp, vp, vp, vp, vp, vp, f64, i32, C.POINTER(SolveInfo)], i32),
     "hgb_mixed_ir_pcg_solve": ([vp, i32, i32, vp, vp, vp, vp, vp, vp, f64, f64, i32, i32, C.POINTER(SolveInfo)], i32),

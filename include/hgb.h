@@ -212,12 +212,18 @@ int hgb_ir_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M
  * 2000): one ILU(0)-PCG on A_inner (F32 or BF16 values, FP32 vectors) with M_inner (store F32
  * or BF16) on the correction d; when ||r|| drops below delta (0 < delta < 1) times its largest
  * value since the last update, or below tol, or at max_iter, x += d in FP64 and r = b - A64 x
- * in FP64, continuing with the same search direction.  Keeps the Krylov space (FP64 PCG's
- * iteration count) where hgb_ir_pcg_solve restarts it per sweep.  Stops when the FP64
+ * in FP64, continuing with the same search direction (restarted, beta = 0, when that update
+ * reduced the FP64 residual less than twice).  Keeps the Krylov space (FP64 PCG's iteration
+ * count) where hgb_ir_pcg_solve restarts it per sweep.  Stops when the FP64
  * ||b - A x||_2 < tol.  info->iterations: inner iterations, info->outer: reliable updates.
  * No reference counterpart. */
 int hgb_ru_pcg_solve(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, const double *b,
                      double *x, double tol, double delta, int max_iter, hgb_solve_info *info);
+/* hgb_ru_pcg_solve on op(A) (trans 'N' or 'T'; 'T' needs an F32 inner matrix): the adjoint of the
+ * mixed-precision forward solve, with the cached transposes and the transposed ILU apply. */
+int hgb_ru_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M_inner, char trans,
+                        const double *b, double *x, double tol, double delta, int max_iter,
+                        hgb_solve_info *info);
 /* solve_gmres / solve_gmres_ilu over gpu_engine (hex/solvers/hala_solvers_gmres.hpp:127-267):
  * left preconditioned restarted GMRES, one classical Gram-Schmidt pass, Givens rotations in
  * the reference's order.  The rotations and the back substitution run on the device and one

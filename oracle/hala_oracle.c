@@ -360,7 +360,8 @@ int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, con
  * (solve_cg_core's order, FP32 vectors, inner products in double) on the correction; whenever
  * the iterated residual falls below delta times its largest value since the last update, the
  * correction is added to x in FP64, the residual is recomputed as b - A x in FP64 and the
- * iteration continues from it with the same search direction.  Stops when the FP64 residual
+ * iteration continues from it with the same search direction (restarted, beta = 0, when the update
+ * reduced the FP64 residual less than twice).  Stops when the FP64 residual
  * after an update is below tol (an update is forced when the iterated residual is below tol and
  * at the iteration limit).
  * Returns the iterations; *updates_out gets the number of reliable updates. */
@@ -376,7 +377,8 @@ int or_ru_pcg(int n, const int *pntr, const int *indx, const double *vals, const
     int it = 0, updates = 0;
     or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r64);
     for (int i = 0; i < n; i++) r64[i] = b[i] - r64[i];
-    double rn = dnorm(n, r64), rmax = rn;
+    double rn = dnorm(n, r64), rmax = rn, last = rn;
+    int restart = 0;
     if (rn < tol) { free(r64); free(r); free(d); free(p); free(Ap); free(z); if (updates_out) *updates_out = 0; return 0; }
     for (int i = 0; i < n; i++) { r[i] = (float)r64[i]; d[i] = 0.0f; }
     memcpy(z, r, nf);
@@ -405,12 +407,17 @@ int or_ru_pcg(int n, const int *pntr, const int *indx, const double *vals, const
             rmax = rn;
             updates++;
             if (rn < tol || !(rn == rn) || it >= max_iter) break;
+            /* the update reduced the true residual less than twice: the kept directions are stale,
+             * restart the recurrence from the new residual */
+            restart = rn > 0.5 * last;
+            last = rn;
         }
         memcpy(z, r, nf);
         ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, z);
         double nzr = 0;
         for (int i = 0; i < n; i++) nzr += (double)r[i] * z[i];
-        float bt = (float)(nzr / zr);
+        float bt = restart ? 0.0f : (float)(nzr / zr);
+        restart = 0;
         for (int i = 0; i < n; i++) p[i] = bt * p[i] + z[i];
         zr = nzr;
     }

@@ -3,7 +3,7 @@
 -div(k grad u) = f on an n x n grid of unit cells (5-point finite volumes, face conductivity the
 harmonic mean of the two cells, Dirichlet faces 2 k_cell), k = exp(theta).  Loss
 L = ||u(theta) - u_target||^2.  The solve is a torch.autograd.Function: forward = mixed precision
-ILU(0)-PCG (FP32 inner, FP64 refinement) through the C ABI; backward = the hand-written adjoint:
+ILU(0)-PCG (FP32 PCG with FP64 reliable updates) through the C ABI; backward = the hand-written adjoint:
 A^T lam = dL/du by the same solver on the transposed operator, dL/df = lam and
 dL/dA_ij = -lam_i u_j on A's pattern (hgb_csr_pattern_grad).  dL/dtheta follows by autograd
 through the assembly below.
@@ -77,9 +77,10 @@ class Solver:
         A64, A32, M = ops[:3]
         x = torch.zeros_like(rhs)
         if sweeps is None:
+            # to the tolerance: FP32 PCG with FP64 reliable updates (one Krylov space; on this
+            # operator about 1.2x the FP64 iterations, where restarted refinement needs 1.5x and more)
             tol = self.tol * float(torch.linalg.vector_norm(rhs))
-            E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, tol, inner_rtol=self.inner_rtol,
-                              max_inner=self.max_inner, max_outer=200)
+            E.solve_ru_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, tol, delta=0.01, max_iter=20000)
         else:
             try:
                 E.solve_ir_pcg_op(self.eng, A64, A32, M, trans, rhs.contiguous(), x, 0.0, inner_rtol=self.inner_rtol,

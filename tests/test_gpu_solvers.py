@@ -314,3 +314,25 @@ def test_mixed_host_buffers(eng, rng, solver):
     fo, do, _ = O.ilu_factor(p, i, v)
     xo, _, _ = O.cg(p, i, v, b, tol=tol, diag=do, ilu=fo)
     assert np.linalg.norm(x - xo) <= 1e-7 * np.linalg.norm(xo)
+
+
+def test_ru_pcg_transposed(eng, rng):
+    # op(A) = A^T through the cached transpose and the transposed ILU apply (the adjoint form); the
+    # operator is symmetric (CG needs an SPD op(A)), so the 'T' solve must agree with the 'N' one
+    n = 48
+    p, i, v = P.vardiff2d(n, np.exp(P.grf2d(n, length=6.0, sigma=1.0, seed=3)))
+    N = len(p) - 1
+    b = rng.standard_normal(N)
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng, N, gp, gi, gv)
+    A32 = E.make_sparse_matrix(eng, N, gp, gi, gv.to(torch.float32))
+    M = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
+    tol = 1e-10 * np.linalg.norm(b)
+    xs = {}
+    for trans in "NT":
+        x = torch.zeros(N, dtype=torch.float64, device=dev)
+        info = E.solve_ru_pcg_op(eng, A64, A32, M, trans, T(b), x, tol, delta=0.01, max_iter=5000)
+        xs[trans] = x.cpu().numpy()
+        assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs[trans])) < tol * 1.0001
+        assert info.true_residual < tol
+    assert np.linalg.norm(xs["T"] - xs["N"]) <= 1e-7 * np.linalg.norm(xs["N"])
