@@ -377,23 +377,38 @@ int solve_batch_cg_ilu(gpu_engine const &e, stop_criteria<T> const &stop, gpu_ve
     return solve_batch_cg_ilu(e, stop, pntr, indx, vals, ilu, B, X);
 }
 
-/* solve_gmres_ilu(gpu_engine, stop, restart, pntr, indx, vals, ilu, b, x) */
-inline int solve_gmres_ilu(gpu_engine const &e, stop_criteria<double> const &stop, int restart,
-                           gpu_vector<int> const &pntr, gpu_vector<int> const &indx, gpu_vector<double> const &vals,
-                           gpu_ilu<double> const &ilu, gpu_vector<double> const &b, gpu_vector<double> &x) {
+/* solve_gmres_ilu(gpu_engine, stop, restart, pntr, indx, vals, ilu, b, x): double or float (the
+ * reference's template, hex/solvers/hala_solvers_gmres.hpp:252-267); returns the applications */
+template <typename T>
+int solve_gmres_ilu(gpu_engine const &e, stop_criteria<T> const &stop, int restart, gpu_vector<int> const &pntr,
+                    gpu_vector<int> const &indx, gpu_vector<T> const &vals, gpu_ilu<T> const &ilu,
+                    gpu_vector<T> const &b, gpu_vector<T> &x) {
     int n = (int)pntr.size() - 1;
     if (x.size() < (size_t)n) { x.resize(n); set_zero(e, x); }
     auto A = make_sparse_matrix(e, n, pntr, indx, vals);
     hgb_solve_info info{};
-    hgb_check(hgb_gmres_solve(e.handle(), A.handle(), ilu.handle(), restart, b.data(), x.data(), stop.tol,
+    hgb_check(hgb_gmres_solve(e.handle(), A.handle(), ilu.handle(), restart, b.data(), x.data(), (double)stop.tol,
                               stop.max_iter, &info), "solve_gmres_ilu");
     return info.iterations;
 }
-inline int solve_gmres_ilu(gpu_engine const &e, stop_criteria<double> const &stop, int restart,
-                           gpu_vector<int> const &pntr, gpu_vector<int> const &indx, gpu_vector<double> const &vals,
-                           gpu_vector<double> const &b, gpu_vector<double> &x, char policy = 'N') {
+template <typename T>
+int solve_gmres_ilu(gpu_engine const &e, stop_criteria<T> const &stop, int restart, gpu_vector<int> const &pntr,
+                    gpu_vector<int> const &indx, gpu_vector<T> const &vals, gpu_vector<T> const &b, gpu_vector<T> &x,
+                    char policy = 'N') {
     auto ilu = make_ilu(e, pntr, indx, vals, policy);
     return solve_gmres_ilu(e, stop, restart, pntr, indx, vals, ilu, b, x);
+}
+/* solve_gmres without preconditioner (solve_gmres(engine, stop, restart, A, no preconditioner, b, x)) */
+template <typename T>
+int solve_gmres(gpu_engine const &e, stop_criteria<T> const &stop, int restart, gpu_vector<int> const &pntr,
+                gpu_vector<int> const &indx, gpu_vector<T> const &vals, gpu_vector<T> const &b, gpu_vector<T> &x) {
+    int n = (int)pntr.size() - 1;
+    if (x.size() < (size_t)n) { x.resize(n); set_zero(e, x); }
+    auto A = make_sparse_matrix(e, n, pntr, indx, vals);
+    hgb_solve_info info{};
+    hgb_check(hgb_gmres_solve(e.handle(), A.handle(), nullptr, restart, b.data(), x.data(), (double)stop.tol,
+                              stop.max_iter, &info), "solve_gmres");
+    return info.iterations;
 }
 
 /* --------------------------------------------------------------- mixed engine ----------- */

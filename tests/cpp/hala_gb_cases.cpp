@@ -105,6 +105,15 @@ int main() {
         hala::solve_gmres_ilu(engine, hala::stop_criteria<double>(1e-9), 6, gp, gi, gv, hala::make_gpu_vector(b), gx);
         gx.unload(x);
         CHECK(testvec(x, xref), "gmres nonsymmetric");
+        // the same system in float (the reference's template over float): the float tolerance
+        std::vector<float> vf(vals.begin(), vals.end()), bf(b.begin(), b.end()), xf;
+        gpu_vector<float> gxf;
+        hala::solve_gmres_ilu(engine, hala::stop_criteria<float>(1e-5f), 6, gp, gi, hala::make_gpu_vector(vf),
+                              hala::make_gpu_vector(bf), gxf);
+        gxf.unload(xf);
+        double ef = 0;
+        for (size_t k = 0; k < xf.size(); k++) ef += std::fabs((double)xf[k] - xref[k]);
+        CHECK(xf.size() == xref.size() && ef < 1e-4, "gmres nonsymmetric float");
     }
     {   // test_cg_batch: three right-hand sides, exact tridiagonal then cyclic with (1e-9, 6)
         std::vector<double> xb(15);
