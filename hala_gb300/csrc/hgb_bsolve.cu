@@ -862,8 +862,11 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
             return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem_max, mx);
         HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem_max));
-        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>,
-                                      cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        // clusters above 8 CTAs are planned only where the occupancy query accepted them with this
+        // attribute set; a refusal here leaves the portable sizes working
+        if (cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                 1) != cudaSuccess)
+            cudaGetLastError();
         attr_dev = c->device;
     }
     if (smem > smem_max) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %d rows per block", S.R);
