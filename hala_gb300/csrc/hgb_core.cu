@@ -220,6 +220,17 @@ int hgb_ctx_create(int device, hgb_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->worker, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess) {
+        cudaMemPoolProps pp = {};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = device;
+        e = cudaMemPoolCreate(&c->pool, &pp);
+    }
+    if (e == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;   // never trim: the next solve of the same size reuses the memory
+        e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e == cudaSuccess) e = cudaMemset(c->counter, 0, sizeof(unsigned) * 8);
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(c->scal, 0, sizeof(SolverScalars));
@@ -244,6 +255,7 @@ int hgb_ctx_destroy(hgb_ctx *c) {
     if (c->worker) cudaStreamDestroy(c->worker);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
+    if (c->pool) cudaMemPoolDestroy(c->pool);   // released once the last stream-ordered free has run
     delete c;
     return HGB_OK;
 }

@@ -71,9 +71,21 @@ struct hgb_ctx {
     size_t arena_bytes = 0;
     cudaStream_t worker = nullptr;         // capturable stream used when the caller's is the NULL stream
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaMemPool_t pool = nullptr;          // solver workspaces: stream-ordered, memory kept between solves
 };
 
 namespace hgb {
+
+// Solver workspaces come from the context's memory pool in stream order: after the first solve of
+// a size the pool holds the memory, so a solve allocates without a device-wide cudaMalloc and frees
+// without the synchronising cudaFree.
+template <typename T>
+inline cudaError_t ws_alloc(hgb_ctx *c, T **p, size_t count) {
+    return cudaMallocFromPoolAsync((void **)p, sizeof(T) * (count ? count : 1), c->pool, c->stream);
+}
+inline void ws_free(hgb_ctx *c, void *p) {
+    if (p) cudaFreeAsync(p, c->stream);
+}
 
 struct DeviceGuard {
     int prev = -1;

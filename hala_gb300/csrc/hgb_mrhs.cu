@@ -133,13 +133,13 @@ static int mr_cg(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int nrhs, const typename Va
     };
     int st = HGB_OK;
     do {
-        if (cudaMallocAsync(&r, sizeof(X) * total, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&p, sizeof(X) * total, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&ap, sizeof(X) * total, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&z, sizeof(X) * total, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&sc, sizeof(X) * 3 * nrhs, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&partial, sizeof(double) * kMrMaxParts * nrhs, c->stream) != cudaSuccess ||
-            cudaMallocAsync(&norm, sizeof(double), c->stream) != cudaSuccess) {
+        if (cudaMallocFromPoolAsync((void **)&r, sizeof(X) * total, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&p, sizeof(X) * total, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&ap, sizeof(X) * total, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&z, sizeof(X) * total, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&sc, sizeof(X) * 3 * nrhs, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&partial, sizeof(double) * kMrMaxParts * nrhs, c->pool, c->stream) != cudaSuccess ||
+            cudaMallocFromPoolAsync((void **)&norm, sizeof(double), c->pool, c->stream) != cudaSuccess) {
             st = fail(HGB_ERR_ALLOC, "cg_solve_nrhs: device memory for %d columns of %ld rows", nrhs, n);
             break;
         }

@@ -122,17 +122,19 @@ static inline int ew_grid(hgb_ctx *c, long n) {
 template <typename X>
 struct CgWork {
     X *r = nullptr, *z = nullptr, *p = nullptr, *Ap = nullptr;
-    int alloc(long n, bool need_z) {
-        size_t b = sizeof(X) * (size_t)n;
-        if (cudaMalloc(&r, b) || cudaMalloc(&p, b) || cudaMalloc(&Ap, b) || (need_z && cudaMalloc(&z, b)))
+    hgb_ctx *c = nullptr;
+    int alloc(hgb_ctx *ctx, long n, bool need_z) {
+        c = ctx;
+        if (ws_alloc(c, &r, n) || ws_alloc(c, &p, n) || ws_alloc(c, &Ap, n) || (need_z && ws_alloc(c, &z, n)))
             return cuda_fail(cudaErrorMemoryAllocation, "cg workspace");
         return HGB_OK;
     }
     void release() {
-        cudaFree(r);
-        cudaFree(z);
-        cudaFree(p);
-        cudaFree(Ap);
+        if (!c) return;
+        ws_free(c, r);
+        ws_free(c, z);
+        ws_free(c, p);
+        ws_free(c, Ap);
     }
 };
 
@@ -175,7 +177,7 @@ static int cg_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const X *b, X *x, double t
     const long n = csr_rows(A);
     CaptureStream cs(c);
     CgWork<X> w;
-    int st = w.alloc(n, M != nullptr);
+    int st = w.alloc(c, n, M != nullptr);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     SolverScalars hs{};
@@ -304,7 +306,7 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
     double res = 0.0;
     long long launches = 0;
     do {
-        if (cudaMalloc(&r64, sizeof(double) * n) || cudaMalloc(&r32, sizeof(float) * n) || cudaMalloc(&d32, sizeof(float) * n)) {
+        if (ws_alloc(c, &r64, n) || ws_alloc(c, &r32, n) || ws_alloc(c, &d32, n)) {
             st = cuda_fail(cudaErrorMemoryAllocation, "ir_pcg workspace");
             break;
         }
@@ -330,9 +332,9 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
             outer++;
         }
     } while (0);
-    cudaFree(r64);
-    cudaFree(r32);
-    cudaFree(d32);
+    ws_free(c, r64);
+    ws_free(c, r32);
+    ws_free(c, d32);
     if (st) return st;
     if (info) {
         info->iterations = total;
@@ -476,10 +478,10 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     SolverScalars hs{};
-    int st = w.alloc(n, M != nullptr);
+    int st = w.alloc(c, n, M != nullptr);
     do {
         if (st) break;
-        if (cudaMalloc(&d, sizeof(float) * n) || cudaMalloc(&r64, sizeof(double) * n)) {
+        if (ws_alloc(c, &d, n) || ws_alloc(c, &r64, n)) {
             st = cuda_fail(cudaErrorMemoryAllocation, "ru_pcg workspace");
             break;
         }
@@ -522,8 +524,8 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     w.release();
-    cudaFree(d);
-    cudaFree(r64);
+    ws_free(c, d);
+    ws_free(c, r64);
     if (st) return st;
     return collect_dev_error(c);
 }
@@ -809,8 +811,8 @@ static int gmres_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int restart, const X *b
     const long long per_cycle = 6 + pre + (long long)restart * (4 + pre);
     int rc = HGB_OK;
     do {
-        if (cudaMalloc(&t, sizeof(X) * n) || cudaMalloc(&r, sizeof(X) * n) || cudaMalloc(&W, sizeof(X) * n * restart) ||
-            cudaMalloc(&cf, sizeof(double) * (kGmresMaxRestart + 1)) || cudaMalloc(&st, sizeof(GmresState))) {
+        if (ws_alloc(c, &t, n) || ws_alloc(c, &r, n) || ws_alloc(c, &W, (size_t)n * restart) ||
+            ws_alloc(c, &cf, kGmresMaxRestart + 1) || ws_alloc(c, &st, 1)) {
             rc = cuda_fail(cudaErrorMemoryAllocation, "gmres workspace");
             break;
         }
@@ -864,11 +866,11 @@ static int gmres_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int restart, const X *b
     } while (0);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    cudaFree(t);
-    cudaFree(r);
-    cudaFree(W);
-    cudaFree(cf);
-    cudaFree(st);
+    ws_free(c, t);
+    ws_free(c, r);
+    ws_free(c, W);
+    ws_free(c, cf);
+    ws_free(c, st);
     if (rc) return rc;
     return collect_dev_error(c);
 }
@@ -931,7 +933,7 @@ extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu
     long long launches = 0;
     const int cycles = (max_inner + restart - 1) / restart;
     do {
-        if (cudaMalloc(&r64, sizeof(double) * n) || cudaMalloc(&r32, sizeof(float) * n) || cudaMalloc(&d32, sizeof(float) * n)) {
+        if (ws_alloc(c, &r64, n) || ws_alloc(c, &r32, n) || ws_alloc(c, &d32, n)) {
             st = cuda_fail(cudaErrorMemoryAllocation, "ir_gmres workspace");
             break;
         }
@@ -957,9 +959,9 @@ extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu
             outer++;
         }
     } while (0);
-    cudaFree(r64);
-    cudaFree(r32);
-    cudaFree(d32);
+    ws_free(c, r64);
+    ws_free(c, r32);
+    ws_free(c, d32);
     if (st) return st;
     if (info) {
         info->iterations = total;
