@@ -312,7 +312,7 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
         }
         for (;;) {
             if ((st = true_residual(c, A64, b, x, r64, &res, &launches, tr))) break;
-            if (res < tol || outer >= max_outer || !(res == res)) break;
+            if (res < tol || res == 0.0 || outer >= max_outer || !(res == res)) break;   // 0: x is exact
             f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, r32);
             zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d32);
             int it = 0;
@@ -343,7 +343,7 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
         info->true_residual = res;
         info->kernel_launches = launches;
     }
-    if (!(res < tol)) return fail(HGB_ERR_NOT_CONVERGED, "ir_pcg: ||b-Ax|| = %g after %d sweeps (tol %g)", res, outer, tol);
+    if (!(res < tol || res == 0.0)) return fail(HGB_ERR_NOT_CONVERGED, "ir_pcg: ||b-Ax|| = %g after %d sweeps (tol %g)", res, outer, tol);
     return HGB_OK;
 }
 
@@ -491,7 +491,7 @@ static int ru_run(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, const doubl
         *iters = 0;
         *updates = 0;
         *res = rn;
-        if (rn < tol || !(rn == rn) || max_iter < 1) break;
+        if (rn < tol || rn == 0.0 || !(rn == rn) || max_iter < 1) break;   // 0: x is exact
         SolverScalars *s = c->scal;
         ru_init_kernel<<<1, 1, 0, c->stream>>>(s, tol * tol, delta * delta, rn * rn, max_iter);
         f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, w.r);
@@ -565,7 +565,7 @@ extern "C" int hgb_ru_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_il
         info->true_residual = res;
         info->kernel_launches = launches;
     }
-    if (!(res < tol)) return fail(HGB_ERR_NOT_CONVERGED, "ru_pcg: ||b-Ax|| = %g after %d iterations (tol %g)", res, it, tol);
+    if (!(res < tol || res == 0.0)) return fail(HGB_ERR_NOT_CONVERGED, "ru_pcg: ||b-Ax|| = %g after %d iterations (tol %g)", res, it, tol);
     return HGB_OK;
 }
 
@@ -939,7 +939,7 @@ extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu
         }
         for (;;) {
             if ((st = true_residual(c, A64, b, x, r64, &res, &launches))) break;
-            if (res < tol || outer >= max_outer || !(res == res)) break;
+            if (res < tol || res == 0.0 || outer >= max_outer || !(res == res)) break;   // 0: x is exact
             f64_to_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, r64, r32);
             zero_f32_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, d32);
             launches += 3;   // residual cast, zero, update
@@ -970,7 +970,7 @@ extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu
         info->true_residual = res;
         info->kernel_launches = launches;
     }
-    if (!(res < tol)) return fail(HGB_ERR_NOT_CONVERGED, "ir_gmres: ||b-Ax|| = %g after %d sweeps (tol %g)", res, outer, tol);
+    if (!(res < tol || res == 0.0)) return fail(HGB_ERR_NOT_CONVERGED, "ir_gmres: ||b-Ax|| = %g after %d sweeps (tol %g)", res, outer, tol);
     return HGB_OK;
 }
 

@@ -172,7 +172,7 @@ int or_ir_pcg(int n, const int *pntr, const int *indx, const double *vals, const
         or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r);
         for (int i = 0; i < n; i++) r[i] = b[i] - r[i];
         double res = dnorm(n, r);
-        if (res < tol || outer >= max_outer) break;
+        if (res < tol || res == 0 || outer >= max_outer) break;   /* 0: x is exact */
         for (int i = 0; i < n; i++) { rf[i] = (float)r[i]; d[i] = 0.0f; }
         /* inner PCG on A32 d = rf, x0 = 0 */
         double rn0 = 0;
@@ -342,7 +342,7 @@ int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, con
         or_spmv_d('N', n, n, 1.0, pntr, indx, vals, x, 0.0, r);
         for (int i = 0; i < n; i++) r[i] = b[i] - r[i];
         double res = dnorm(n, r);
-        if (res < tol || outer >= max_outer || res != res) break;
+        if (res < tol || res == 0 || outer >= max_outer || res != res) break;
         for (int i = 0; i < n; i++) { rf[i] = (float)r[i]; d[i] = 0.0f; }
         double rel = 0.5 * tol / res;
         if (rel < inner_rtol) rel = inner_rtol;
@@ -379,7 +379,7 @@ int or_ru_pcg(int n, const int *pntr, const int *indx, const double *vals, const
     for (int i = 0; i < n; i++) r64[i] = b[i] - r64[i];
     double rn = dnorm(n, r64), rmax = rn, last = rn;
     int restart = 0;
-    if (rn < tol) { free(r64); free(r); free(d); free(p); free(Ap); free(z); if (updates_out) *updates_out = 0; return 0; }
+    if (rn < tol || rn == 0) { free(r64); free(r); free(d); free(p); free(Ap); free(z); if (updates_out) *updates_out = 0; return 0; }
     for (int i = 0; i < n; i++) { r[i] = (float)r64[i]; d[i] = 0.0f; }
     memcpy(z, r, nf);
     ilu_apply_mixed(n, pntr, indx, diag, ilu32, piv, z);
