@@ -1,0 +1,213 @@
+// Library baseline: the reference's GPU path for ILU(0)-PCG restated with the library calls it makes
+// (gpu/hala_cuda_sparse_general.hpp:265-277 cusparseSpMV; gpu/hala_gpu_ilu.hpp:67-78 csrilu02 and
+// :150-164 two SpSV solves per apply; gpu/hala_gpu_blas1.hpp cuBLAS BLAS-1 in host pointer mode;
+// the loop of solve_cg_core, hex/solvers/hala_solvers_cg.hpp:92-156).  FP64 throughout.
+//
+// Input (raw little-endian files in argv[1]): n.i32, pntr.i32[n+1], indx.i32[nnz], vals.f64[nnz],
+// b.f64[n].  Output: one JSON line with the times.  Not part of the library: timing only.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusparse.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#define CK(x)                                                                                  \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess) { std::fprintf(stderr, "%s: %s\n", #x, cudaGetErrorString(e_)); std::exit(1); } \
+    } while (0)
+#define CS(x)                                                                                  \
+    do {                                                                                       \
+        cusparseStatus_t s_ = (x);                                                             \
+        if (s_ != CUSPARSE_STATUS_SUCCESS) { std::fprintf(stderr, "%s: %d\n", #x, (int)s_); std::exit(1); } \
+    } while (0)
+#define CB(x)                                                                                  \
+    do {                                                                                       \
+        cublasStatus_t s_ = (x);                                                               \
+        if (s_ != CUBLAS_STATUS_SUCCESS) { std::fprintf(stderr, "%s: %d\n", #x, (int)s_); std::exit(1); } \
+    } while (0)
+
+template <typename T>
+static std::vector<T> load(const std::string &path, size_t count) {
+    std::vector<T> v(count);
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f || std::fread(v.data(), sizeof(T), count, f) != count) { std::fprintf(stderr, "read %s\n", path.c_str()); std::exit(1); }
+    std::fclose(f);
+    return v;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) { std::fprintf(stderr, "usage: cusparse_pcg DIR\n"); return 1; }
+    const std::string dir = argv[1];
+    const int n = load<int>(dir + "/n.i32", 1)[0];
+    auto pntr = load<int>(dir + "/pntr.i32", n + 1);
+    const int nnz = pntr[n];
+    auto indx = load<int>(dir + "/indx.i32", nnz);
+    auto vals = load<double>(dir + "/vals.f64", nnz);
+    auto b = load<double>(dir + "/b.f64", n);
+    double bn = 0;
+    for (double v : b) bn += v * v;
+    const double tol = 1e-10 * std::sqrt(bn);
+
+    int *dp, *di;
+    double *dv, *dilu, *db, *dx, *dr, *dz, *dp_, *dAp, *dt;
+    CK(cudaMalloc(&dp, sizeof(int) * (n + 1)));
+    CK(cudaMalloc(&di, sizeof(int) * nnz));
+    CK(cudaMalloc(&dv, sizeof(double) * nnz));
+    CK(cudaMalloc(&dilu, sizeof(double) * nnz));
+    for (double **p : {&db, &dx, &dr, &dz, &dp_, &dAp, &dt}) CK(cudaMalloc(p, sizeof(double) * n));
+    CK(cudaMemcpy(dp, pntr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(di, indx.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dv, vals.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(db, b.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+
+    cusparseHandle_t sp;
+    cublasHandle_t bl;
+    CS(cusparseCreate(&sp));
+    CB(cublasCreate(&bl));
+    CB(cublasSetPointerMode(bl, CUBLAS_POINTER_MODE_HOST));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto elapsed = [&]() { float ms; CK(cudaEventSynchronize(e1)); CK(cudaEventElapsedTime(&ms, e0, e1)); return (double)ms; };
+
+    // ---- SpMV: y = A x
+    cusparseSpMatDescr_t A;
+    cusparseDnVecDescr_t vp, vAp, vr, vz, vt, vx, vb;
+    CS(cusparseCreateCsr(&A, n, n, nnz, dp, di, dv, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_BASE_ZERO, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vp, n, dp_, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vAp, n, dAp, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vr, n, dr, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vz, n, dz, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vt, n, dt, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vx, n, dx, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vb, n, db, CUDA_R_64F));
+    const double one = 1.0, zero = 0.0;
+    size_t sz = 0;
+    CS(cusparseSpMV_bufferSize(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, A, vb, &zero, vAp, CUDA_R_64F, CUSPARSE_SPMV_ALG_DEFAULT, &sz));
+    void *spbuf;
+    CK(cudaMalloc(&spbuf, std::max<size_t>(sz, 16)));
+    auto spmv = [&](cusparseDnVecDescr_t in, cusparseDnVecDescr_t out) {
+        CS(cusparseSpMV(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, A, in, &zero, out, CUDA_R_64F, CUSPARSE_SPMV_ALG_DEFAULT, spbuf));
+    };
+    for (int k = 0; k < 3; k++) spmv(vb, vAp);
+    CK(cudaEventRecord(e0));
+    for (int k = 0; k < 20; k++) spmv(vb, vAp);
+    CK(cudaEventRecord(e1));
+    const double spmv_ms = elapsed() / 20;
+
+    // ---- ILU(0): csrilu02 on a copy of the values
+    CK(cudaMemcpy(dilu, dv, sizeof(double) * nnz, cudaMemcpyDeviceToDevice));
+    cusparseMatDescr_t md;
+    CS(cusparseCreateMatDescr(&md));
+    CS(cusparseSetMatIndexBase(md, CUSPARSE_INDEX_BASE_ZERO));
+    CS(cusparseSetMatType(md, CUSPARSE_MATRIX_TYPE_GENERAL));
+    csrilu02Info_t info;
+    CS(cusparseCreateCsrilu02Info(&info));
+    int isz = 0;
+    CS(cusparseDcsrilu02_bufferSize(sp, n, nnz, md, dilu, dp, di, info, &isz));
+    void *ibuf;
+    CK(cudaMalloc(&ibuf, std::max(isz, 16)));
+    CK(cudaDeviceSynchronize());
+    CK(cudaEventRecord(e0));
+    CS(cusparseDcsrilu02_analysis(sp, n, nnz, md, dilu, dp, di, info, CUSPARSE_SOLVE_POLICY_USE_LEVEL, ibuf));
+    CS(cusparseDcsrilu02(sp, n, nnz, md, dilu, dp, di, info, CUSPARSE_SOLVE_POLICY_USE_LEVEL, ibuf));
+    CK(cudaEventRecord(e1));
+    const double factor_ms = elapsed();
+    int zp = -1;
+    if (cusparseXcsrilu02_zeroPivot(sp, info, &zp) == CUSPARSE_STATUS_ZERO_PIVOT) { std::fprintf(stderr, "zero pivot %d\n", zp); return 1; }
+
+    // ---- the two triangular solves of gpu_ilu::apply: L (unit) then U (non-unit) over the factor
+    cusparseSpMatDescr_t L, U;
+    CS(cusparseCreateCsr(&L, n, n, nnz, dp, di, dilu, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_BASE_ZERO, CUDA_R_64F));
+    CS(cusparseCreateCsr(&U, n, n, nnz, dp, di, dilu, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_32I, CUSPARSE_INDEX_BASE_ZERO, CUDA_R_64F));
+    cusparseFillMode_t fl = CUSPARSE_FILL_MODE_LOWER, fu = CUSPARSE_FILL_MODE_UPPER;
+    cusparseDiagType_t dl = CUSPARSE_DIAG_TYPE_UNIT, du = CUSPARSE_DIAG_TYPE_NON_UNIT;
+    CS(cusparseSpMatSetAttribute(L, CUSPARSE_SPMAT_FILL_MODE, &fl, sizeof(fl)));
+    CS(cusparseSpMatSetAttribute(L, CUSPARSE_SPMAT_DIAG_TYPE, &dl, sizeof(dl)));
+    CS(cusparseSpMatSetAttribute(U, CUSPARSE_SPMAT_FILL_MODE, &fu, sizeof(fu)));
+    CS(cusparseSpMatSetAttribute(U, CUSPARSE_SPMAT_DIAG_TYPE, &du, sizeof(du)));
+    cusparseSpSVDescr_t sl, su;
+    CS(cusparseSpSV_createDescr(&sl));
+    CS(cusparseSpSV_createDescr(&su));
+    size_t bl_sz = 0, bu_sz = 0;
+    CS(cusparseSpSV_bufferSize(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, L, vr, vt, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, sl, &bl_sz));
+    CS(cusparseSpSV_bufferSize(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, U, vt, vz, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, su, &bu_sz));
+    void *lbuf, *ubuf;
+    CK(cudaMalloc(&lbuf, std::max<size_t>(bl_sz, 16)));
+    CK(cudaMalloc(&ubuf, std::max<size_t>(bu_sz, 16)));
+    CK(cudaEventRecord(e0));
+    CS(cusparseSpSV_analysis(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, L, vr, vt, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, sl, lbuf));
+    CS(cusparseSpSV_analysis(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, U, vt, vz, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, su, ubuf));
+    CK(cudaEventRecord(e1));
+    const double analysis_ms = elapsed();
+    auto precond = [&]() {   // z = U^-1 L^-1 r
+        CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, L, vr, vt, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, sl));
+        CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, U, vt, vz, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, su));
+    };
+    CK(cudaMemcpy(dr, db, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+    for (int k = 0; k < 3; k++) precond();
+    CK(cudaEventRecord(e0));
+    for (int k = 0; k < 20; k++) precond();
+    CK(cudaEventRecord(e1));
+    const double apply_ms = elapsed() / 20;
+
+    // ---- PCG, solve_cg_core's loop with host-returned scalars (three synchronisations per iteration)
+    auto pcg = [&](int &iters, double &rnorm) {
+        CK(cudaMemset(dx, 0, sizeof(double) * n));
+        CK(cudaMemcpy(dr, db, sizeof(double) * n, cudaMemcpyDeviceToDevice));   // r = b - A 0
+        precond();
+        CK(cudaMemcpy(dp_, dz, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+        double rz = 0;
+        CB(cublasDdot(bl, n, dr, 1, dz, 1, &rz));
+        int it = 1;
+        for (;;) {
+            spmv(vp, vAp);
+            double pap = 0;
+            CB(cublasDdot(bl, n, dp_, 1, dAp, 1, &pap));
+            const double a = rz / pap, ma = -a;
+            CB(cublasDaxpy(bl, n, &a, dp_, 1, dx, 1));
+            CB(cublasDaxpy(bl, n, &ma, dAp, 1, dr, 1));
+            double rn = 0;
+            CB(cublasDnrm2(bl, n, dr, 1, &rn));
+            it++;
+            if (rn < tol || it > 100000) { rnorm = rn; break; }
+            precond();
+            double nrz = 0;
+            CB(cublasDdot(bl, n, dr, 1, dz, 1, &nrz));
+            const double bt = nrz / rz;
+            CB(cublasDscal(bl, n, &bt, dp_, 1));
+            CB(cublasDaxpy(bl, n, &one, dz, 1, dp_, 1));
+            rz = nrz;
+        }
+        iters = it;
+    };
+    int iters = 0;
+    double rn = 0;
+    pcg(iters, rn);   // warm-up
+    std::vector<double> ts;
+    for (int k = 0; k < 3; k++) {
+        CK(cudaDeviceSynchronize());
+        CK(cudaEventRecord(e0));
+        pcg(iters, rn);
+        CK(cudaEventRecord(e1));
+        ts.push_back(elapsed());
+    }
+    std::sort(ts.begin(), ts.end());
+    // true residual of the last solve
+    spmv(vx, vAp);
+    std::vector<double> ax(n), xs(n);
+    CK(cudaMemcpy(ax.data(), dAp, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    double tr = 0;
+    for (int i = 0; i < n; i++) tr += (b[i] - ax[i]) * (b[i] - ax[i]);
+    std::printf("{\"impl\": \"cusparse\", \"n\": %d, \"nnz\": %d, \"spmv_ms\": %.5f, \"ilu_factor_ms\": %.3f, "
+                "\"spsv_analysis_ms\": %.3f, \"ilu_apply_ms\": %.5f, \"pcg_ms\": %.3f, \"pcg_solves_per_s\": %.4f, "
+                "\"iterations\": %d, \"rel_residual\": %.3e}\n",
+                n, nnz, spmv_ms, factor_ms, analysis_ms, apply_ms, ts[1], 1e3 / ts[1], iters, std::sqrt(tr / bn));
+    return 0;
+}
