@@ -3,6 +3,11 @@
 // :150-164 two SpSV solves per apply; gpu/hala_gpu_blas1.hpp cuBLAS BLAS-1 in host pointer mode;
 // the loop of solve_cg_core, hex/solvers/hala_solvers_cg.hpp:92-156).  FP64 throughout.
 //
+// With argv[2] = "gmres": left-preconditioned GMRES(30) as solve_gmres
+// (hex/solvers/hala_solvers_gmres.hpp:127-230): cublasDgemv 'T' / 'N' for the projection
+// (krylov_project / krylov_combine, :47-77) with the coefficients read back to the host in every
+// inner iteration, Givens rotations and tpsv on the host.
+//
 // Input (raw little-endian files in argv[1]): n.i32, pntr.i32[n+1], indx.i32[nnz], vals.f64[nnz],
 // b.f64[n].  Output: one JSON line with the times.  Not part of the library: timing only.
 #include <cublas_v2.h>
@@ -42,8 +47,9 @@ static std::vector<T> load(const std::string &path, size_t count) {
 }
 
 int main(int argc, char **argv) {
-    if (argc < 2) { std::fprintf(stderr, "usage: cusparse_pcg DIR\n"); return 1; }
+    if (argc < 2) { std::fprintf(stderr, "usage: cusparse_pcg DIR [gmres]\n"); return 1; }
     const std::string dir = argv[1];
+    const bool gmres = argc > 2 && std::string(argv[2]) == "gmres";
     const int n = load<int>(dir + "/n.i32", 1)[0];
     auto pntr = load<int>(dir + "/pntr.i32", n + 1);
     const int nnz = pntr[n];
@@ -150,12 +156,136 @@ int main(int argc, char **argv) {
         CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, L, vr, vt, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, sl));
         CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, U, vt, vz, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, su));
     };
+    // out = U^-1 L^-1 in (through the work vector t)
+    cusparseDnVecDescr_t vin, vout;
+    CS(cusparseCreateDnVec(&vin, n, dr, CUDA_R_64F));
+    CS(cusparseCreateDnVec(&vout, n, dz, CUDA_R_64F));
+    auto precond_to = [&](double *in, double *out) {
+        CS(cusparseDnVecSetValues(vin, in));
+        CS(cusparseDnVecSetValues(vout, out));
+        CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, L, vin, vt, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, sl));
+        CS(cusparseSpSV_solve(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, U, vt, vout, CUDA_R_64F, CUSPARSE_SPSV_ALG_DEFAULT, su));
+    };
     CK(cudaMemcpy(dr, db, sizeof(double) * n, cudaMemcpyDeviceToDevice));
     for (int k = 0; k < 3; k++) precond();
     CK(cudaEventRecord(e0));
     for (int k = 0; k < 20; k++) precond();
     CK(cudaEventRecord(e1));
     const double apply_ms = elapsed() / 20;
+
+    if (gmres) {
+        const int m = 30;
+        double *W, *dcf, *dt2;
+        CK(cudaMalloc(&W, sizeof(double) * (size_t)n * m));
+        CK(cudaMalloc(&dcf, sizeof(double) * (m + 1)));
+        CK(cudaMalloc(&dt2, sizeof(double) * n));
+        cusparseDnVecDescr_t vt2;
+        CS(cusparseCreateDnVec(&vt2, n, dt2, CUDA_R_64F));
+        // tol = 1e-9 ||P^-1 b|| (the preconditioned residual the reference's loop tests)
+        precond_to(db, dz);
+        double pb = 0;
+        CB(cublasDnrm2(bl, n, dz, 1, &pb));
+        const double gtol = 1e-9 * pb;
+        auto rotg = [](double &a, double &b, double &c, double &s) {
+            double roe = (std::fabs(a) > std::fabs(b)) ? a : b, scale = std::fabs(a) + std::fabs(b), r, z;
+            if (scale == 0.0) { c = 1; s = 0; r = 0; z = 0; }
+            else {
+                r = scale * std::sqrt((a / scale) * (a / scale) + (b / scale) * (b / scale));
+                if (roe < 0) r = -r;
+                c = a / r; s = b / r; z = 1;
+                if (std::fabs(a) > std::fabs(b)) z = s;
+                if (std::fabs(b) >= std::fabs(a) && c != 0) z = 1 / c;
+            }
+            a = r; b = z;
+        };
+        auto rot = [](double &x, double &y, double c, double s) { double t = c * x + s * y; y = c * y - s * x; x = t; };
+        auto run = [&](int &total) {
+            CK(cudaMemset(dx, 0, sizeof(double) * n));
+            std::vector<double> H, S, C, Z, cf(m + 1);
+            double outer_res = gtol + 1, inner_res = 0;
+            int outer = 0;
+            total = 0;
+            const double mone = -1.0;
+            while (outer_res > gtol && outer < 10000) {
+                H.clear(); S.clear(); C.clear(); Z.clear();
+                CK(cudaMemcpy(dt2, db, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+                CS(cusparseSpMV(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &mone, A, vx, &one, vt2, CUDA_R_64F, CUSPARSE_SPMV_ALG_DEFAULT, spbuf));
+                precond_to(dt2, dr);
+                total++;
+                CB(cublasDnrm2(bl, n, dr, 1, &inner_res));
+                double sc = 1.0 / inner_res;
+                CB(cublasDscal(bl, n, &sc, dr, 1));
+                Z.push_back(inner_res);
+                CK(cudaMemcpy(W, dr, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+                int k = 0;
+                while (inner_res > gtol && k < m) {
+                    CS(cusparseDnVecSetValues(vin, dr));
+                    CS(cusparseSpMV(sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, A, vin, &zero, vt2, CUDA_R_64F, CUSPARSE_SPMV_ALG_DEFAULT, spbuf));
+                    precond_to(dt2, dr);
+                    total++;
+                    // krylov_project: cf = W^T r, r -= W cf (coefficients back to the host)
+                    CB(cublasDgemv(bl, CUBLAS_OP_T, n, k + 1, &one, W, n, dr, 1, &zero, dcf, 1));
+                    CB(cublasDgemv(bl, CUBLAS_OP_N, n, k + 1, &mone, W, n, dcf, 1, &one, dr, 1));
+                    CK(cudaMemcpy(cf.data(), dcf, sizeof(double) * (k + 1), cudaMemcpyDeviceToHost));
+                    double nrm = 0;
+                    CB(cublasDnrm2(bl, n, dr, 1, &nrm));
+                    sc = 1.0 / nrm;
+                    CB(cublasDscal(bl, n, &sc, dr, 1));
+                    for (int i = 0; i < k; i++) rot(cf[i], cf[i + 1], C[i], S[i]);
+                    double beta = nrm, ic, is;
+                    rotg(cf[k], beta, ic, is);
+                    H.insert(H.end(), cf.begin(), cf.begin() + k + 1);
+                    S.push_back(is);
+                    C.push_back(ic);
+                    inner_res = std::fabs(S.back() * Z.back());
+                    k++;
+                    if (inner_res > gtol && k < m) {
+                        CK(cudaMemcpy(W + (size_t)k * n, dr, sizeof(double) * n, cudaMemcpyDeviceToDevice));
+                        Z.push_back(0.0);
+                        rot(Z[k - 1], Z[k], C.back(), S.back());
+                    }
+                }
+                if (!H.empty()) {   // tpsv on the packed upper factor, then x += W Z
+                    int nz = (int)Z.size();
+                    long kk = (long)nz * (nz + 1) / 2 - 1;
+                    for (int j = nz - 1; j >= 0; j--) {
+                        if (Z[j] != 0.0) {
+                            Z[j] /= H[kk];
+                            double tt = Z[j];
+                            long q = kk - 1;
+                            for (int i = j - 1; i >= 0; i--, q--) Z[i] -= tt * H[q];
+                        }
+                        kk -= j + 1;
+                    }
+                    CK(cudaMemcpy(dcf, Z.data(), sizeof(double) * nz, cudaMemcpyHostToDevice));
+                    CB(cublasDgemv(bl, CUBLAS_OP_N, n, nz, &one, W, n, dcf, 1, &one, dx, 1));
+                }
+                outer++;
+                outer_res = inner_res;
+            }
+        };
+        int total = 0;
+        run(total);   // warm-up
+        std::vector<double> tg;
+        for (int k = 0; k < 3; k++) {
+            CK(cudaDeviceSynchronize());
+            CK(cudaEventRecord(e0));
+            run(total);
+            CK(cudaEventRecord(e1));
+            tg.push_back(elapsed());
+        }
+        std::sort(tg.begin(), tg.end());
+        spmv(vx, vAp);
+        std::vector<double> ax(n);
+        CK(cudaMemcpy(ax.data(), dAp, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        double tr = 0;
+        for (int i = 0; i < n; i++) tr += (b[i] - ax[i]) * (b[i] - ax[i]);
+        std::printf("{\"impl\": \"cusparse\", \"solver\": \"gmres30\", \"n\": %d, \"nnz\": %d, \"spmv_ms\": %.5f, "
+                    "\"ilu_factor_ms\": %.3f, \"spsv_analysis_ms\": %.3f, \"ilu_apply_ms\": %.5f, \"gmres_ms\": %.3f, "
+                    "\"applications\": %d, \"true_rel_residual\": %.3e}\n",
+                    n, nnz, spmv_ms, factor_ms, analysis_ms, apply_ms, tg[1], total, std::sqrt(tr / bn));
+        return 0;
+    }
 
     // ---- PCG, solve_cg_core's loop with host-returned scalars (three synchronisations per iteration)
     auto pcg = [&](int &iters, double &rnorm) {

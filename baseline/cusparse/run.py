@@ -1,6 +1,7 @@
-"""Builds and runs the cuSPARSE/cuBLAS restatement of the reference's GPU ILU(0)-PCG path on the
-128^3 anisotropic workload of bench.py (same matrix and right-hand side) and prints its JSON line.
-    python baseline/cusparse/run.py [--grid G]"""
+"""Builds and runs the cuSPARSE/cuBLAS restatement of the reference's GPU path and prints its JSON
+line: ILU(0)-PCG on the 128^3 anisotropic workload of bench.py (same matrix and right-hand side), or
+with --gmres ILU(0)-GMRES(30) on the 96^3 convection-diffusion operator (b ~ U[-1,1], seed 3).
+    python baseline/cusparse/run.py [--grid G] [--gmres]"""
 import argparse
 import os
 import subprocess
@@ -16,11 +17,17 @@ sys.path.insert(0, ROOT)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--grid", type=int, default=None)
+    ap.add_argument("--gmres", action="store_true")
     args = ap.parse_args()
-    import bench
-    bench.GRID = args.grid
-    p, i, v, xt, b = bench.workload()
+    if args.gmres:
+        from hala_gb300 import problems as P
+        p, i, v = P.convdiff3d(args.grid or 96)
+        b = np.random.default_rng(3).uniform(-1, 1, len(p) - 1)
+    else:
+        import bench
+        bench.GRID = args.grid or 128
+        p, i, v, xt, b = bench.workload()
     exe = os.path.join(tempfile.gettempdir(), "hgb_cusparse_pcg")
     subprocess.run(["nvcc", "-O3", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler",
                     "-Wno-deprecated-declarations", os.path.join(HERE, "cusparse_pcg.cu"),
@@ -31,7 +38,7 @@ def main():
         i.astype(np.int32).tofile(os.path.join(d, "indx.i32"))
         v.astype(np.float64).tofile(os.path.join(d, "vals.f64"))
         b.astype(np.float64).tofile(os.path.join(d, "b.f64"))
-        r = subprocess.run([exe, d], capture_output=True, text=True)
+        r = subprocess.run([exe, d] + (["gmres"] if args.gmres else []), capture_output=True, text=True)
         sys.stdout.write(r.stdout)
         sys.stderr.write(r.stderr)
         sys.exit(r.returncode)
