@@ -171,6 +171,21 @@ def run_reference(args, rank, world):
     }), flush=True)
 
 
+def max_over_ranks(times_ms, device):
+    """Replicas: each rank times its own solves; the job's time is the slowest rank's (barrier on
+    both sides of the timed region), so value = solves of all ranks / that time."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(times_ms, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def aggregate_rate(world, ms_per_solve):
+    """Whole-job solves/s of `world` replicas whose slowest rank took ms_per_solve per solve."""
+    return world * 1e3 / ms_per_solve
+
+
 def flush_l2(buf):
     buf.add_(1.0)   # writes 256 MB > the 129 MB L2
 
@@ -351,10 +366,9 @@ def main():
     t_mx = statistics.mean(msmx)
     t_64 = statistics.mean(ms64)
     t_e2e = statistics.mean(e2e_ms)
+    t_ir = statistics.mean(msir)
     if world > 1:
-        tt = torch.tensor([t_mx, t_64, t_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_mx, t_64, t_e2e = tt.tolist()
+        t_mx, t_64, t_e2e, t_ir = max_over_ranks([t_mx, t_64, t_e2e, t_ir], dev)
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -402,7 +416,7 @@ def main():
         except Exception as e:  # report, do not hide
             cpu = {"value": None, "error": str(e)}
     out = {
-        "metric": METRIC, "value": world * 1e3 / t_mx, "unit": "solves/s", "n_gpus": world,
+        "metric": METRIC, "value": aggregate_rate(world, t_mx), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mx, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
         "config": {"workload": f"ILU(0)-PCG, 3D 7-point anisotropic {GRID}^3 coef (1,1,0.01), b = A x_true "
@@ -411,22 +425,22 @@ def main():
                                                f"refinement by reliable updates (delta {RU_DELTA})",
                    "l2": "flushed between timed solves (256 MB write); matrix 217 MB > 129 MB L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "fp64": {"solves_per_s": world * 1e3 / t_64, "ms_per_solve": t_64, "iterations": it64,
+        "fp64": {"solves_per_s": aggregate_rate(world, t_64), "ms_per_solve": t_64, "iterations": it64,
                  "rel_residual": res64, "setup_ms": setup64 * 1e3},
-        "mixed": {"solves_per_s": world * 1e3 / t_mx, "ms_per_solve": t_mx, "inner_iterations": infmx[-1].iterations,
+        "mixed": {"solves_per_s": aggregate_rate(world, t_mx), "ms_per_solve": t_mx, "inner_iterations": infmx[-1].iterations,
                   "reliable_updates": infmx[-1].outer, "rel_residual": resmx,
                   "err_vs_fp64": float(np.linalg.norm(xm - xs) / np.linalg.norm(xs)),
                   "err_vs_xtrue": float(np.linalg.norm(xm - xt) / np.linalg.norm(xt)), "setup_ms": setup32 * 1e3},
         "mixed_over_fp64": t_64 / t_mx,
-        "mixed_restarted_ir": {"solves_per_s": world * 1e3 / statistics.mean(msir),
-                               "ms_per_solve": statistics.mean(msir), "inner_iterations": infir[-1].iterations,
+        "mixed_restarted_ir": {"solves_per_s": aggregate_rate(world, t_ir),
+                               "ms_per_solve": t_ir, "inner_iterations": infir[-1].iterations,
                                "sweeps": infir[-1].outer, "inner_rtol": IR_INNER_RTOL},
         "roofline": roof, "spmv": spmv,
         "ilu_apply": {"f64": {"ms": t_ilu64, "gbs": ib64 / (t_ilu64 * 1e-3) / 1e9, "bytes": ib64,
                               "traffic": prof.get("ilu_apply_f64_bytes")},
                       "f32": {"ms": t_ilu32, "gbs": ib32 / (t_ilu32 * 1e-3) / 1e9, "bytes": ib32,
                               "traffic": prof.get("ilu_apply_f32_bytes")}},
-        "e2e": {"value": world * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": aggregate_rate(world, t_e2e), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "entry": "hgb_mixed_ru_pcg_solve (host pntr/indx/vals/b/x)",
                 "rel_residual": e2e_err},
         "gpu_launches": launches,
