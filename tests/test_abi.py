@@ -40,3 +40,26 @@ def test_host_only_entry_points():
     # argument checks run before any device work
     assert L.hgb_ctx_create(0, None) == hgb.HGB_ERR_ARG
     assert b"null output" in L.hgb_last_error()
+
+
+def test_solver_argument_checks_need_no_device():
+    # null handles and out-of-range limits are rejected before any CUDA call, with a message
+    L = hgb.lib()
+    info = hgb.SolveInfo()
+    cases = [
+        (lambda: L.hgb_cg_solve(None, None, None, None, None, 1e-10, 10, C.byref(info)), b"cg_solve"),
+        (lambda: L.hgb_gmres_solve(None, None, None, 30, None, None, 1e-10, 10, C.byref(info)), b"gmres"),
+        (lambda: L.hgb_gmres_solve(None, None, None, 65, None, None, 1e-10, 10, C.byref(info)), b"restart"),
+        (lambda: L.hgb_ru_pcg_solve(None, None, None, None, None, None, 1e-10, 0.01, 10, C.byref(info)),
+         b"ru_pcg"),
+        (lambda: L.hgb_ru_pcg_solve_op(None, None, None, None, b"T", None, None, 1e-10, 0.01, 10, C.byref(info)),
+         b"ru_pcg"),
+        (lambda: L.hgb_ir_pcg_solve(None, None, None, None, None, None, 1e-10, 1e-4, 10, 5, C.byref(info)),
+         b"ir_pcg"),
+        (lambda: L.hgb_ir_gmres_solve(None, None, None, None, 30, None, None, 1e-10, 1e-4, 10, 5, C.byref(info)),
+         b"ir_gmres"),
+        (lambda: L.hgb_cg_solve_nrhs(None, None, None, 2, None, None, 1e-10, 10, C.byref(info)), b"cg_solve_nrhs"),
+    ]
+    for call, what in cases:
+        assert call() == hgb.HGB_ERR_ARG
+        assert what in L.hgb_last_error(), what
