@@ -31,6 +31,8 @@ RTOL = 1e-10
 IR_INNER_RTOL = 1e-5     # first refinement sweep; later sweeps stop at what the target needs
 RU_DELTA = 0.01          # reliable update when ||r|| has dropped 100x since the last one
 SEED = 2
+WORKLOAD = ("ILU(0)-PCG, 3D 7-point anisotropic {grid}^3 coef (1,1,0.01), b = A x_true (x_true ~ N(0,1), "
+            "seed 2), x0 = 0, ||b-Ax|| < 1e-10 ||b||")
 
 
 def workload():
@@ -114,28 +116,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(p, i, v, b, full_iters, target_s=12.0):
-    """FP64 ILU(0)-PCG of the oracle (the reference's algorithm, serial) on the host cores:
-    a bounded sample of iterations, extrapolated to one full solve."""
+def cpu_sample(p, i, v, b):
+    """FP64 ILU(0)-PCG of the oracle (the reference's algorithm, serial) on the host cores: one
+    complete solve to the 1e-10 relative residual from x0 = 0 (ILU factor excluded)."""
     from oracle import oracle as O
     tol = RTOL * float(np.linalg.norm(b))
     f, d, _ = O.ilu_factor(p, i, v)
     t0 = time.perf_counter()
-    O.cg(p, i, v, b, tol=tol, max_iter=4, diag=d, ilu=f)
-    per_it = (time.perf_counter() - t0) / 4
-    m = int(max(8, min(400, target_s / max(per_it, 1e-6))))
-    t0 = time.perf_counter()
-    _, it, _ = O.cg(p, i, v, b, tol=tol, max_iter=m, diag=d, ilu=f)
+    _, it, _ = O.cg(p, i, v, b, tol=tol, diag=d, ilu=f)
     dt = time.perf_counter() - t0
-    per_it = dt / max(it - 1, 1)
-    return {"value": 1.0 / (per_it * full_iters), "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"{it - 1} FP64 ILU(0)-PCG iterations of the 128^3 solve ({dt:.1f} s), extrapolated "
-                      f"to the {full_iters} iterations of a full solve; ILU factor excluded"}
+    return {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one complete FP64 ILU(0)-PCG solve of the {GRID}^3 system ({it} iterations, {dt:.1f} s), "
+                      "serial as the reference's sparse path; ILU factor excluded"}
 
 
 def run_reference(args, rank, world):
     """Reference arm: the reference's CPU algorithm for the path (the oracle port: the reference's
-    own sources are not on this machine), FP64 ILU(0)-PCG, timed on the host cores."""
+    own sources are not on this machine), FP64 ILU(0)-PCG, timed on the host cores.  Every step is
+    one complete solve to the 1e-10 relative residual from x0 = 0; the ILU factor is computed once,
+    outside the timed steps (the reference's own factorisation is O(n^2): about 37 min here)."""
     if rank != 0:
         return
     from oracle import oracle as O
@@ -143,32 +142,218 @@ def run_reference(args, rank, world):
     n = len(p) - 1
     tol = RTOL * float(np.linalg.norm(b))
     f, d, _ = O.ilu_factor(p, i, v)
-    # warm-up: one full solve gives the iteration count of the workload
-    t0 = time.perf_counter()
-    x, full_iters, _ = O.cg(p, i, v, b, tol=tol, diag=d, ilu=f) if args.warmup > 0 else (None, 0, 0)
-    t_full = time.perf_counter() - t0
-    if not full_iters:
-        full_iters = 300
-    per_step_iters = 10
-    times = []
+    for _ in range(args.warmup):
+        O.cg(p, i, v, b, tol=tol, diag=d, ilu=f)
+    times, its = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, it, _ = O.cg(p, i, v, b, tol=tol, max_iter=per_step_iters + 1, diag=d, ilu=f)
-        times.append((time.perf_counter() - t0) / (it - 1))
-    per_it = statistics.median(times)
-    val = 1.0 / (per_it * full_iters)
-    sample = (f"{args.steps} steps of {per_step_iters} FP64 ILU(0)-PCG iterations (serial, as the reference's "
-              f"sparse path), extrapolated to the {full_iters}-iteration full solve (one full solve in "
-              f"warm-up took {t_full:.1f} s)")
+        x, it, _ = O.cg(p, i, v, b, tol=tol, diag=d, ilu=f)
+        times.append(time.perf_counter() - t0)
+        its.append(it)
+    per = statistics.mean(times)
+    val = 1.0 / per
+    res = float(np.linalg.norm(b - __import__("hala_gb300.problems", fromlist=["x"]).csr_matvec(p, i, v, x))
+                / np.linalg.norm(b))
+    sample = (f"{args.steps} complete FP64 ILU(0)-PCG solves ({its[-1]} iterations each, rel. residual "
+              f"{res:.2e}) after {args.warmup} untimed ones; serial, as the reference's sparse path")
     print(json.dumps({
         "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": per_it * full_iters * 1e3, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"ILU(0)-PCG 3D 7-point anisotropic {GRID}^3 (1,1,0.01), rel res 1e-10",
-                   "n": n, "nnz": int(len(i))},
+        "config": {"workload": WORKLOAD.format(grid=GRID), "n": n, "nnz": int(len(i))},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def _events_ms(stream, fn, steps, warm, flush=None):
+    """Median CUDA-event time of fn on stream (after warm untimed calls); returns (ms, last result)."""
+    import torch
+    for _ in range(warm):
+        if flush is not None:
+            flush_l2(flush)
+        fn()
+    out, res = [], None
+    for _ in range(steps):
+        if flush is not None:
+            flush_l2(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = fn()
+        e1.record(stream)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return statistics.median(out), res
+
+
+def other_workloads(E, eng, dev, stream, flush, peak, steps=3, warm=2):
+    """The path's other workloads, timed on the device (CUDA events, setup excluded): CG on the 256^2
+    Poisson system, ILU(0)-GMRES(30) on the 96^3 convection-diffusion operator (FP64 and mixed),
+    the 4,096 independent systems in one persistent launch, and the 512^2 differentiable solve
+    (forward and adjoint).  Each entry reports its time, iterations and residual."""
+    import torch
+    from hala_gb300 import problems as P
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)   # noqa: E731
+    out = {}
+    launches = 0
+
+    # 256^2 2D Poisson, unpreconditioned CG to 1e-10 (5 MB of matrix: L2-resident, not flushed)
+    p, i, v = P.poisson2d(256)
+    n = len(p) - 1
+    b = P.csr_matvec(p, i, v, np.random.default_rng(1).uniform(-1, 1, n))
+    tol = 1e-10 * float(np.linalg.norm(b))
+    A = E.make_sparse_matrix(eng, n, T(p), T(i), T(v))
+    gb, x = T(b), torch.zeros(n, dtype=torch.float64, device=dev)
+
+    def cg():
+        x.zero_()
+        return E.solve_cg_info(eng, A, None, gb, x, tol)
+    ms, info = _events_ms(stream, cg, steps, warm)
+    launches += (steps + warm) * int(info.kernel_launches)
+    res = float(np.linalg.norm(b - P.csr_matvec(p, i, v, x.cpu().numpy())) / np.linalg.norm(b))
+    out["cg_poisson256"] = {"ms_per_solve": ms, "iterations": info.iterations, "rel_residual": res,
+                            "us_per_iteration": 1e3 * ms / max(info.iterations, 1), "n": n, "nnz": len(i),
+                            "l2": "not flushed (5 MB system)"}
+
+    # 96^3 convection-diffusion, ILU(0)-GMRES(30): FP64 to 1e-9 of ||P^-1 b|| (the reference's test on
+    # the preconditioned residual), and mixed FP32-inner GMRES with FP64 refinement to a 1e-9 true residual
+    p, i, v = P.convdiff3d(96)
+    n = len(p) - 1
+    b = np.random.default_rng(3).uniform(-1, 1, n)
+    gp, gi, gv, gb = T(p), T(i), T(v), T(b)
+    A64 = E.make_sparse_matrix(eng, n, gp, gi, gv)
+    M64 = E.make_ilu(eng, gp, gi, gv)
+    pb = torch.empty(n, dtype=torch.float64, device=dev)
+    M64.apply(gb, pb)
+    ptol = 1e-9 * float(torch.linalg.vector_norm(pb))
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+
+    def gm64():
+        x.zero_()
+        return E.solve_gmres(eng, E.stop_criteria(ptol), 30, gp, gi, gv, gb, x, ilu=M64, matrix=A64)
+    ms64, apps = _events_ms(stream, gm64, steps, warm, flush)
+    r64 = float(np.linalg.norm(b - P.csr_matvec(p, i, v, x.cpu().numpy())) / np.linalg.norm(b))
+    A32 = E.make_sparse_matrix(eng, n, gp, gi, gv.float())
+    M32 = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
+    ttol = 1e-9 * float(np.linalg.norm(b))
+
+    def gmmx():
+        x.zero_()
+        return E.solve_ir_gmres(eng, A64, A32, M32, 30, gb, x, ttol, inner_rtol=1e-4)
+    msmx, infmx = _events_ms(stream, gmmx, steps, warm, flush)
+    launches += (steps + warm) * int(infmx.kernel_launches)
+    rmx = float(np.linalg.norm(b - P.csr_matvec(p, i, v, x.cpu().numpy())) / np.linalg.norm(b))
+    out["gmres30_convdiff96"] = {
+        "n": n, "nnz": len(i),
+        "fp64": {"ms_per_solve": ms64, "applications": apps, "true_rel_residual": r64,
+                 "stop": "preconditioned residual < 1e-9 ||P^-1 b||"},
+        "mixed": {"ms_per_solve": msmx, "inner_iterations": infmx.iterations, "sweeps": infmx.outer,
+                  "true_rel_residual": rmx, "stop": "||b - Ax|| < 1e-9 ||b||"}}
+    del A64, M64, A32, M32
+
+    # 4,096 independent Erdos-Renyi Laplacians (n_i log-uniform in [64, 4096]), FP32 CG with FP64
+    # refinement to 1e-8 per system, one persistent launch replayed from a CUDA graph
+    S = 4096
+    sp_, p, i, v = P.er_laplacian_batch(S, 64, 4096, seed=4)
+    nt = len(p) - 1
+    b = np.random.default_rng(5).uniform(-1, 1, nt)
+    B = E.gpu_batch(eng, T(sp_), T(p), T(i), T(v))
+    gb = T(b)
+    x = torch.zeros(nt, dtype=torch.float64, device=dev)
+    iters = torch.zeros(S, dtype=torch.int32, device=dev)
+    rel = torch.zeros(S, dtype=torch.float64, device=dev)
+
+    def batch():
+        x.zero_()
+        return B.solve(gb, x, rtol=1e-8, iters=iters, relres=rel)
+    msb, _ = _events_ms(stream, batch, steps, warm, flush)
+    launches += 2 * (steps + warm)
+    it = iters.cpu().numpy().astype(np.int64)
+    ni = np.diff(sp_).astype(np.int64)
+    nnz_i = (p[sp_[1:]] - p[sp_[:-1]]).astype(np.int64)
+    # algorithmic bytes: every inner iteration streams its system's matrix (FP32 values, int32
+    # columns and row pointers) and touches x and b once per system in FP64
+    mat_bytes = float(np.sum(it * (8 * nnz_i + 4 * (ni + 1)))) + float(np.sum(16 * ni))
+    gbs = mat_bytes / (msb * 1e-3) / 1e9
+    out["batch_4096"] = {"ms_per_batch": msb, "systems_per_s": S * 1e3 / msb, "rows": nt, "nnz": len(i),
+                         "max_rel_residual": float(rel.max()), "iterations_total": int(it.sum()),
+                         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                      "frac": gbs / peak, "algorithmic_bytes": mat_bytes,
+                                      "bytes": "sum over systems of inner iterations x (8 nnz_i + 4 (n_i + 1)) + 16 n_i"}}
+    del B
+
+    # 512^2 variable-coefficient diffusion: forward mixed ILU(0)-PCG (FP32 PCG, FP64 reliable updates)
+    # to 3e-11 and the adjoint solve A^T lam = 2 (u - u_target) with dL/dA on the pattern
+    nn = 512
+    k1, k2 = np.exp(P.grf2d(nn, 16.0, 1.0, seed=1)), np.exp(P.grf2d(nn, 16.0, 1.0, seed=2))
+    p, i, v = P.vardiff2d(nn, k1)
+    v2 = P.vardiff2d(nn, k2)[2]
+    n = len(p) - 1
+    gp, gi = T(p), T(i)
+    f = torch.ones(n, dtype=torch.float64, device=dev)
+    tol = 3e-11 * float(torch.linalg.vector_norm(f))
+
+    def ops(vals):
+        gv = T(vals)
+        return (E.make_sparse_matrix(eng, n, gp, gi, gv), E.make_sparse_matrix(eng, n, gp, gi, gv.float()),
+                E.make_ilu(eng, gp, gi, gv, store=torch.float32), gv)
+    A64, A32, M32, gv = ops(v)
+    ut = torch.zeros(n, dtype=torch.float64, device=dev)
+    t2 = ops(v2)
+    E.solve_ru_pcg(eng, t2[0], t2[1], t2[2], f, ut, tol, delta=0.01, max_iter=20000)
+    del t2
+    u = torch.zeros(n, dtype=torch.float64, device=dev)
+    lam = torch.zeros(n, dtype=torch.float64, device=dev)
+    gvals = torch.empty_like(gv)
+    fw = {}
+
+    def forward_adjoint():
+        u.zero_()
+        lam.zero_()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        fi = E.solve_ru_pcg(eng, A64, A32, M32, f, u, tol, delta=0.01, max_iter=20000)
+        e1.record(stream)
+        g = 2.0 * (u - ut)
+        ai = E.solve_ru_pcg_op(eng, A64, A32, M32, "T", g, lam, 3e-11 * float(torch.linalg.vector_norm(g)),
+                               delta=0.01, max_iter=20000)
+        E.pattern_grad(A64, -1.0, lam, u, gvals)
+        e2.record(stream)
+        e2.synchronize()
+        fw.setdefault("fwd", []).append(e0.elapsed_time(e1))
+        fw.setdefault("adj", []).append(e1.elapsed_time(e2))
+        return fi, ai
+    msfa, (fi, ai) = _events_ms(stream, forward_adjoint, 2, 1)
+    launches += 3 * (int(fi.kernel_launches) + int(ai.kernel_launches))
+    res = float(np.linalg.norm(1.0 - P.csr_matvec(p, i, v, u.cpu().numpy())) / np.sqrt(n))
+    out["adjoint_vardiff512"] = {"ms_forward_plus_adjoint": msfa, "ms_forward": statistics.median(fw["fwd"][1:]),
+                                 "ms_adjoint": statistics.median(fw["adj"][1:]), "forward_iterations": fi.iterations,
+                                 "adjoint_iterations": ai.iterations, "forward_rel_residual": res, "n": n,
+                                 "loss": float(torch.sum((u - ut) ** 2))}
+    return out, launches
+
+
+LIBRARY_EXE = os.path.join(ROOT, "baseline", "cusparse", "_build", "cusparse_pcg")
+
+
+def library_baseline(p, i, v, b, tmpdir, gmres=False):
+    """The reference's GPU path (cuSPARSE SpMV / csrilu02 / SpSV and cuBLAS BLAS-1 in host pointer
+    mode, the loop of solve_cg_core, or with gmres=True the GMRES(30) of solve_gmres with its
+    per-iteration host read-back) restated in baseline/cusparse and built by the package build, run
+    on the given system outside this arm's timed region.  Returns its JSON line, or why it did not run."""
+    exe = LIBRARY_EXE
+    if not os.path.exists(exe):
+        return {"unavailable": "baseline/cusparse was not built (nvcc or cuSPARSE missing at build time)"}
+    n = len(p) - 1
+    np.array([n], np.int32).tofile(os.path.join(tmpdir, "n.i32"))
+    p.astype(np.int32).tofile(os.path.join(tmpdir, "pntr.i32"))
+    i.astype(np.int32).tofile(os.path.join(tmpdir, "indx.i32"))
+    v.astype(np.float64).tofile(os.path.join(tmpdir, "vals.f64"))
+    b.astype(np.float64).tofile(os.path.join(tmpdir, "b.f64"))
+    r = subprocess.run([exe, tmpdir] + (["gmres"] if gmres else []), capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": f"cusparse_pcg exited {r.returncode}: {r.stderr.strip()[-300:]}"}
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 def max_over_ranks(times_ms, device):
@@ -200,6 +385,8 @@ def main():
     ap.add_argument("--grid", type=int, default=None, help="grid edge (default 128: the headline workload)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the SpMV and ILU-apply launches (for profiling captures)")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="skip the other workloads and the library baseline (reported beside the headline)")
     args = ap.parse_args()
     if args.grid:
         global GRID
@@ -320,27 +507,32 @@ def main():
     y64 = torch.empty(n, dtype=torch.float64, device=dev)
     y32 = torch.empty(n, dtype=torch.float32, device=dev)
     xs32 = gb.float()
+    # two copies of the BF16 matrix (2 x 112 MB > the 129 MB L2), alternated launch by launch
     gvb = gv.to(torch.bfloat16)
-    Ab = E.make_sparse_matrix(eng, n, gp, gi, gvb)
+    gp2, gi2, gvb2 = gp.clone(), gi.clone(), gvb.clone()
+    Ab = [E.make_sparse_matrix(eng, n, gp, gi, gvb), E.make_sparse_matrix(eng, n, gp2, gi2, gvb2)]
     # SpMV: 20 launches back to back per timing (the FP64 and FP32 matrices, 217 / 142 MB, exceed the
     # 129 MB L2, so each launch streams from HBM; a single launch would also time the launch gap).
-    # The BF16 matrix (112 MB) fits in L2: one launch after a flush.
     def spmv_ms(fn, batch=20, reps=5):
         out = []
         for _ in range(reps):
             flush_l2(flush)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            for _ in range(batch):
-                fn()
+            for k in range(batch):
+                fn(k)
             e1.record(stream)
             e1.synchronize()
             out.append(e0.elapsed_time(e1) / batch)
         return statistics.median(out)
 
-    t_spmv64 = spmv_ms(lambda: A64.gemv("N", 1.0, gb, 0.0, y64))
-    t_spmv32 = spmv_ms(lambda: A32.gemv("N", 1.0, xs32, 0.0, y32))
-    t_spmvbf = kernel_ms(lambda: Ab.gemv("N", 1.0, xs32, 0.0, y32))
+    t_spmv64 = spmv_ms(lambda k: A64.gemv("N", 1.0, gb, 0.0, y64))
+    t_spmv32 = spmv_ms(lambda k: A32.gemv("N", 1.0, xs32, 0.0, y32))
+    t_spmvbf = spmv_ms(lambda k: Ab[k & 1].gemv("N", 1.0, xs32, 0.0, y32))
+    eng.set_spmv_mode("exact")      # the reference's rounding: separately rounded multiply and add
+    t_spmv64x = spmv_ms(lambda k: A64.gemv("N", 1.0, gb, 0.0, y64))
+    t_spmv32x = spmv_ms(lambda k: A32.gemv("N", 1.0, xs32, 0.0, y32))
+    eng.set_spmv_mode("fused")
     t_ilu64 = kernel_ms(lambda: M64.apply(gb, y64))
     t_ilu32 = kernel_ms(lambda: M32.apply(xs32, y32))
     clk = clocks.stop()
@@ -361,6 +553,23 @@ def main():
     d2h = 8 * n
     e2e_err = float(np.linalg.norm(b - __import__("hala_gb300.problems", fromlist=["x"]).csr_matvec(p, i, v, hx))
                     / np.linalg.norm(b))
+
+    # ---- the path's other workloads and the library baseline (outside the timed headline region)
+    others, other_launches, lib = None, 0, None
+    if not args.no_other_workloads:
+        others, other_launches = other_workloads(E, eng, dev, stream, flush, peaks()[0])
+        if rank == 0:
+            import tempfile
+            from hala_gb300 import problems as P
+            lib = {}
+            pc, ic, vc = P.convdiff3d(96)
+            bc = np.random.default_rng(3).uniform(-1, 1, len(pc) - 1)
+            for key, args_ in (("pcg_aniso128", (p, i, v, b, False)), ("gmres30_convdiff96", (pc, ic, vc, bc, True))):
+                with tempfile.TemporaryDirectory() as tdir:
+                    try:
+                        lib[key] = library_baseline(*args_[:4], tdir, gmres=args_[4])
+                    except Exception as e:  # report, do not hide
+                        lib[key] = {"unavailable": f"library baseline failed: {e}"}
 
     # ---- aggregate (replicas): solves of all ranks / max time
     t_mx = statistics.mean(msmx)
@@ -385,7 +594,7 @@ def main():
     it64 = inf64[-1].iterations
     launches = (sum(int(q.kernel_launches) for q in inf64) + sum(int(q.kernel_launches) for q in infmx)
                 + sum(int(q.kernel_launches) for q in infir))
-    launches += 2 * 20 * 5 + 10 + 4 * 10   # kernel timing: 2 x 100 SpMV, 10 BF16 SpMV, 2 x 10 ILU applies (2 launches each)
+    launches += 5 * 20 * 5 + 4 * 10   # kernel timing: 5 x 100 SpMV, 2 x 10 ILU applies (2 launches each)
     # dominant kernel of the headline (mixed) solve: the FP32-store triangular sweeps (ILU apply)
     ach_ilu = ib32 / (t_ilu32 * 1e-3) / 1e9
     prof = {}
@@ -406,21 +615,28 @@ def main():
                     "frac": spmv_bytes(n, nnz, 4, 4) / (t_spmv32 * 1e-3) / 1e9 / peak,
                     "bytes": spmv_bytes(n, nnz, 4, 4), "traffic": prof.get("spmv_f32_bytes")},
             "bf16f32": {"ms": t_spmvbf, "gbs": spmv_bytes(n, nnz, 2, 4) / (t_spmvbf * 1e-3) / 1e9,
+                        "frac": spmv_bytes(n, nnz, 2, 4) / (t_spmvbf * 1e-3) / 1e9 / peak,
                         "bytes": spmv_bytes(n, nnz, 2, 4)},
+            "f64_exact": {"ms": t_spmv64x, "gbs": vb64 / (t_spmv64x * 1e-3) / 1e9,
+                          "frac": vb64 / (t_spmv64x * 1e-3) / 1e9 / peak},
+            "f32_exact": {"ms": t_spmv32x, "gbs": spmv_bytes(n, nnz, 4, 4) / (t_spmv32x * 1e-3) / 1e9,
+                          "frac": spmv_bytes(n, nnz, 4, 4) / (t_spmv32x * 1e-3) / 1e9 / peak},
             "peak": peak, "unit": "GB/s",
-            "timing": "f64/f32: 20 launches back to back (matrix > L2), median of 5; bf16: one launch after an L2 flush"}
+            "mode": "f64/f32/bf16: fused multiply-add (the default, used by the solves); *_exact: separately "
+                    "rounded multiply and add (bit-identical to the reference's CPU product)",
+            "timing": "20 launches back to back, median of 5; f64/f32 matrices (217 / 142 MB) exceed the 129 MB L2, "
+                      "bf16 alternates two copies of its 112 MB matrix"}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
-            cpu = cpu_sample(p, i, v, b, it64)
+            cpu = cpu_sample(p, i, v, b)
         except Exception as e:  # report, do not hide
             cpu = {"value": None, "error": str(e)}
     out = {
         "metric": METRIC, "value": aggregate_rate(world, t_mx), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mx, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
-        "config": {"workload": f"ILU(0)-PCG, 3D 7-point anisotropic {GRID}^3 coef (1,1,0.01), b = A x_true "
-                               f"(x_true ~ N(0,1), seed {SEED}), x0 = 0, ||b-Ax|| < 1e-10 ||b||",
+        "config": {"workload": WORKLOAD.format(grid=GRID),
                    "n": n, "nnz": nnz, "form": "mixed: FP32 values/vectors/ILU (FP64 pivots) PCG, FP64 "
                                                f"refinement by reliable updates (delta {RU_DELTA})",
                    "l2": "flushed between timed solves (256 MB write); matrix 217 MB > 129 MB L2",
@@ -444,6 +660,9 @@ def main():
                 "d2h_bytes_per_step": d2h, "entry": "hgb_mixed_ru_pcg_solve (host pntr/indx/vals/b/x)",
                 "rel_residual": e2e_err},
         "gpu_launches": launches,
+        "other_workloads": others,
+        "gpu_launches_other_workloads": other_launches,
+        "library_baseline": lib,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <vector>
 
 namespace hgb {
@@ -624,14 +625,12 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
 // above 8 being non-portable) at which the clusters of all nblk blocks are co-resident; failing
 // that, the largest of 8, 4, 2 that fits.  On GB300 (one CTA per SM) 15 clusters of 8 are
 // co-resident, so for 128 blocks a size between 9 and 16 that still fits 128 CTAs at once removes
-// the wait for a free cluster.  HGB_BS_CLUSTER caps the size (1: no clusters, for comparisons).
+// the wait for a free cluster.
 static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
-    const char *e = getenv("HGB_BS_CLUSTER");
-    const int cap = (e && atoi(e) >= 1) ? std::min(atoi(e), kBsMaxCluster) : kBsMaxCluster;
     if (nblk < 2) return 1;
-    for (int cl = std::min(cap, nblk); cl > 1; cl--)
+    for (int cl = std::min(kBsMaxCluster, nblk); cl > 1; cl--)
         if ((long)bs_clusters_fit(c, R, cl) * cl >= nblk) return cl;
-    for (int cl = std::min(cap, 8); cl > 1; cl /= 2)
+    for (int cl = 8; cl > 1; cl /= 2)
         if (bs_clusters_fit(c, R, cl) >= 1) return cl;
     return 1;
 }
@@ -639,13 +638,10 @@ static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
 // Rows per block: 16384 (the FP64 slice fills 128 KB).  For natural-ordered grids whose planes
 // hold 16384 rows this puts one plane in a block; blocks that cut planes make a block's first
 // local levels wait for the previous block's last ones, which serialises the wavefront.
-// HGB_BS_ROWS32 sets the FP32 / BF16 block rows (up to 32768) for comparisons.
 int bsolve_rows(hgb_ctx *c, int xsize, int n) {
     (void)c;
+    (void)xsize;
     (void)n;
-    if (xsize == 8) return 16384;
-    const char *e = getenv("HGB_BS_ROWS32");
-    if (e && atoi(e) >= 1024) return std::min(32768, atoi(e) / 128 * 128);
     return 16384;
 }
 
@@ -876,9 +872,12 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
         return launch_check("bsolve_kernel");
     }
     // thread-block clusters of S.cl CTAs (the push targets were planned for that size); as many
-    // clusters as are co-resident, at most one per run of S.cl blocks
-    static int clusters_dev[kBsMaxCluster + 1] = {};
-    static int clusters_max[kBsMaxCluster + 1] = {};
+    // clusters as are co-resident with this launch's shared memory, at most one per run of S.cl
+    // blocks.  The occupancy query is cached per (device, cluster size, shared memory).
+    struct FitKey { int dev, cl; size_t smem; int n; };
+    static std::vector<FitKey> fit_cache;
+    static std::mutex fit_mu;
+    std::lock_guard<std::mutex> lock(fit_mu);
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -890,16 +889,17 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
     cfg.stream = c->stream;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (clusters_dev[S.cl] != c->device + 1) {
+    int clusters_max = 0;
+    for (const FitKey &k : fit_cache)
+        if (k.dev == c->device && k.cl == S.cl && k.smem == smem) clusters_max = k.n;
+    if (clusters_max == 0) {
         cfg.gridDim = dim3(S.cl * 16);
-        int n = 0;
-        HGB_CUDA(cudaOccupancyMaxActiveClusters(&n, bsolve_kernel<V, X, MODE, UNIT, RECIP>, &cfg));
-        if (n < 1) return fail(HGB_ERR_UNSUPPORTED, "bsolve: no cluster of %d CTAs fits", S.cl);
-        clusters_max[S.cl] = n;
-        clusters_dev[S.cl] = c->device + 1;
+        HGB_CUDA(cudaOccupancyMaxActiveClusters(&clusters_max, bsolve_kernel<V, X, MODE, UNIT, RECIP>, &cfg));
+        if (clusters_max < 1) return fail(HGB_ERR_UNSUPPORTED, "bsolve: no cluster of %d CTAs fits", S.cl);
+        fit_cache.push_back(FitKey{c->device, S.cl, smem, clusters_max});
     }
     const int runs = (S.nblk + S.cl - 1) / S.cl;
-    cfg.gridDim = dim3(S.cl * std::max(1, std::min(runs, clusters_max[S.cl])));
+    cfg.gridDim = dim3(S.cl * std::max(1, std::min(runs, clusters_max)));
     HGB_CUDA(cudaLaunchKernelEx(&cfg, bsolve_kernel<V, X, MODE, UNIT, RECIP>, A, alpha, in, out, pend));
     return launch_check("bsolve_kernel");
 }

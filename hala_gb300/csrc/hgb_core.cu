@@ -216,7 +216,6 @@ int hgb_ctx_create(int device, hgb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&c->scal, sizeof(SolverScalars));
     if (e == cudaSuccess) e = cudaMallocHost(&c->host_result, sizeof(double) * 64);
-    if (e == cudaSuccess) e = (cudaError_t)(spmv_init_attributes() == HGB_OK ? cudaSuccess : cudaErrorUnknown);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->worker, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
@@ -263,6 +262,19 @@ int hgb_ctx_destroy(hgb_ctx *c) {
 int hgb_ctx_set_stream(hgb_ctx *c, void *stream) {
     if (!c) return fail(HGB_ERR_ARG, "null context");
     c->stream = (cudaStream_t)stream;
+    return HGB_OK;
+}
+
+int hgb_ctx_set_spmv_mode(hgb_ctx *c, int mode) {
+    if (!c) return fail(HGB_ERR_ARG, "set_spmv_mode: null context");
+    if (mode != HGB_SPMV_FUSED && mode != HGB_SPMV_EXACT) return fail(HGB_ERR_ARG, "set_spmv_mode: mode %d", mode);
+    c->spmv_mode = mode;
+    return HGB_OK;
+}
+
+int hgb_ctx_get_spmv_mode(hgb_ctx *c, int *mode) {
+    if (!c || !mode) return fail(HGB_ERR_ARG, "get_spmv_mode: bad arguments");
+    *mode = c->spmv_mode;
     return HGB_OK;
 }
 

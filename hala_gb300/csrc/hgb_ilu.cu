@@ -413,25 +413,9 @@ static int fill_pending(hgb_ctx *c, long n, X *p) {
     return launch_check("fill_pending_kernel");
 }
 
-// 0: block-local level schedule (default); 1: global level tasks (HGB_ILU_SOLVER=levels)
-static int ilu_solver_kind() {
-    static int v = [] {
-        const char *e = getenv("HGB_ILU_SOLVER");
-        return (e && std::string(e) == "levels") ? 1 : 0;
-    }();
-    return v;
-}
-
-// CTAs (of 8 warps) per SM for the sync-free solves.  More warps hold tasks further ahead of
-// the wavefront, all of them polling L2; HGB_TRSV_BLOCKS_PER_SM overrides the default.
-static int trsv_blocks_per_sm() {
-    static int v = [] {
-        const char *e = getenv("HGB_TRSV_BLOCKS_PER_SM");
-        int k = e ? atoi(e) : 4;
-        return (k >= 1 && k <= 8) ? k : 4;
-    }();
-    return v;
-}
+// CTAs (of 8 warps) per SM for the global-level sync-free solves: more warps hold tasks further
+// ahead of the wavefront, all of them polling L2.
+constexpr int kTrsvBlocksPerSm = 4;
 
 template <typename V, typename X>
 static int launch_solve(hgb_ctx *c, const Schedule &S, SolveArgs A, const V *vals, X alpha, const X *in, X *out,
@@ -442,7 +426,7 @@ static int launch_solve(hgb_ctx *c, const Schedule &S, SolveArgs A, const V *val
     A.perm = S.perm;
     A.ticket = S.ticket;
     A.err = c->err;
-    int blocks = std::max(1, std::min((S.ntasks + 7) / 8, c->num_sms * trsv_blocks_per_sm()));
+    int blocks = std::max(1, std::min((S.ntasks + 7) / 8, c->num_sms * kTrsvBlocksPerSm));
     trsv_kernel<V, X><<<blocks, 256, 0, c->stream>>>(A, vals, alpha, in, out, pend_a, pend_b);
     return launch_check("trsv_kernel");
 }
@@ -705,7 +689,7 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
             if ((st = launch_check("ilu store conversion"))) break;
         }
         if (cudaMalloc(&M->tmp, xsize(store) * n) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
-        if (ilu_solver_kind() == 0) {
+        {   // block-local schedules; patterns they cannot hold fall back to the global-level solve
             const int R = bsolve_rows(c, (int)xsize(store), n);
             int bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 1, 0, R, (int)xsize(store), M->BL);
             if (!bs) bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 0, 0, R, (int)xsize(store), M->BU);

@@ -72,6 +72,7 @@ struct hgb_ctx {
     cudaStream_t worker = nullptr;         // capturable stream used when the caller's is the NULL stream
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaMemPool_t pool = nullptr;          // solver workspaces: stream-ordered, memory kept between solves
+    int spmv_mode = HGB_SPMV_FUSED;        // arithmetic of the 'N' products (hgb_ctx_set_spmv_mode)
 };
 
 namespace hgb {

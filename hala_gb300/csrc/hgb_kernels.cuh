@@ -128,9 +128,6 @@ struct Transpose {
     void release();
 };
 
-// opt the SpMV kernels into their dynamic shared memory size (once per process, before capture)
-int spmv_init_attributes();
-
 int exclusive_scan(hgb_ctx *c, const int *in, int *out, int n, int *total_dev, int *scratch);
 int csr_check(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx);
 int build_transpose(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,

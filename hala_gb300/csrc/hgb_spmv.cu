@@ -1,8 +1,19 @@
-// CSR SpMV for sm_103a: row tiles staged into shared memory by the TMA bulk-copy engine
-// (cp.async.bulk + mbarrier, double-buffered, persistent CTAs), one thread per row summing its
-// entries sequentially with separately rounded multiply and add.  That is the arithmetic of the
-// reference's sparse_gemv_array<T,'N'> (sparse/hala_sparse_utils.hpp:104-112), so FP64 results
-// are bit-identical to the reference CPU path while the DRAM stream stays fully coalesced.
+// CSR SpMV for sm_103a.  One warp takes 32 consecutive rows at a time: it copies the tile's whole
+// vals / indx range into its own shared-memory buffer with coalesced 16-byte cp.async (no
+// handshake between warps), then every lane sums its row from shared memory, gathering x from
+// global memory (L2) kGW entries at a time.  The warp double-buffers: the copy of tile k+1 and the
+// row pointers of tile k+2 are in flight while tile k is summed.  Tiles of more than kWarpCap
+// entries read their rows directly.
+//
+// Two arithmetic modes, chosen per context (hgb_ctx_set_spmv_mode):
+//  - exact: each row summed in column order with separately rounded multiply and add, the
+//    arithmetic of the reference's sparse_gemv_array<T,'N'> (sparse/hala_sparse_utils.hpp:104-112),
+//    so FP64 results are bit-identical to the reference CPU path.  That is two FP64 operations per
+//    entry; sm_103's FP64 pipe is narrow (a warp-wide FP64 instruction holds an SMSP's FP64 unit
+//    for 64 cycles), so the exact FP64 product is bound by the FP64 pipe, not by HBM.
+//  - fused (the default): the same column order with one fused multiply-add per entry; a product
+//    with alpha = 1 and beta = 0 skips the scaling.  Results differ from the reference's by the
+//    rounding of the individual products (a few ulps of the row sum).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
 
@@ -13,209 +24,31 @@
 
 namespace hgb {
 
-constexpr int kSpmvRows = 256;              // rows per tile = consumer threads (8 warps)
-constexpr int kSpmvStages = 4;              // TMA ring depth
-constexpr int kSpmvStageBytes = 27 * 1024;  // one tile: row pointers, header, vals, indx
-constexpr int kSpmvHdr = kSpmvRows * 4 + 16;  // pntr[r0, r0+256) and {s, e, k} of the tile
-constexpr int kSpmvSmem = kSpmvStages * kSpmvStageBytes;   // 108 KB: 2 CTAs per SM
-
-template <typename V>
-__host__ __device__ constexpr int spmv_cap() {
-    // entries per stage, with 16 entries of slack for the 16-byte rounding of the staged range
-    return ((kSpmvStageBytes - kSpmvHdr) / (int)(sizeof(V) + sizeof(int))) / 16 * 16 - 16;
-}
-
-template <typename V>
-struct TileGeom {
-    int s, e;           // nnz range of the tile
-    int sv, ev;         // staged range of vals (aligned to 16 bytes), ev == sv when not staged
-    int si, ei;         // staged range of indx
-};
-
-template <typename V>
-__device__ __forceinline__ TileGeom<V> tile_geom_se(int s, int e, bool tma) {
-    constexpr int VA = 16 / sizeof(V);
-    TileGeom<V> g;
-    g.s = s;
-    g.e = e;
-    bool staged = tma && (e - s) <= spmv_cap<V>();
-    g.sv = s & ~(VA - 1);
-    g.ev = staged ? (e & ~(VA - 1)) : g.sv;
-    g.si = s & ~3;
-    g.ei = staged ? (e & ~3) : g.si;
-    return g;
-}
-
-// Warp-specialized SpMV: warp 8 streams tile data into a kSpmvStages-deep shared ring with TMA
-// bulk copies (boundaries of the next 32 tiles fetched by its 32 lanes at once); warps 0-7 take
-// one row each per tile, issue up to 8 x-gathers at a time and sum in column order.
-// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A).
-template <typename V, bool FUSE_DOT>
-__global__ void __launch_bounds__(kSpmvRows + 32, 2)
-spmv_n_kernel(int n_rows, int ntiles, const int *__restrict__ pntr, const int *__restrict__ indx,
-              const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
-              typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, int tma, double *partials,
-              unsigned *counter, double *dot_out, int *err, const int *skip) {
-    using X = typename Val<V>::X;
-    if (skip && *skip) return;   // converged solver iteration replayed from a graph
-    constexpr int CAP = spmv_cap<V>() + 16;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t full[kSpmvStages], empty[kSpmvStages];
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        for (int k = 0; k < kSpmvStages; k++) {
-            mbar_init(&full[k], 1);
-            mbar_init(&empty[k], 1);
-        }
-        fence_mbar_init();
-    }
-    __syncthreads();
-    const bool use_tma = tma != 0;
-    const int my_tiles = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
-    if (tid >= kSpmvRows) {
-        // producer warp
-        const int lane = tid & 31;
-        for (int base = 0; base < my_tiles; base += 32) {
-            int s = 0, e = 0;
-            const int mine = base + lane;
-            if (mine < my_tiles) {
-                const int tile = blockIdx.x + mine * gridDim.x;
-                s = __ldg(pntr + tile * kSpmvRows);
-                e = __ldg(pntr + min(tile * kSpmvRows + kSpmvRows, n_rows));
-            }
-            const int cnt = min(32, my_tiles - base);
-            for (int k = 0; k < cnt; k++) {
-                const int sk = __shfl_sync(0xffffffffu, s, k), ek = __shfl_sync(0xffffffffu, e, k);
-                if (lane == 0) {
-                    const int j = base + k;
-                    const int st = j % kSpmvStages;
-                    if (j >= kSpmvStages) mbar_wait(&empty[st], ((j / kSpmvStages) - 1) & 1, err);
-                    const int tile = blockIdx.x + j * gridDim.x;
-                    const int r0 = tile * kSpmvRows, r1 = min(r0 + kSpmvRows, n_rows);
-                    // row pointers [r0, r0 + kp) by bulk copy (kp a multiple of 4 so the size is a
-                    // multiple of 16 bytes and no copy reads past pntr[n_rows]); the rest from global
-                    const int kp = use_tma ? ((r1 - r0 + 1) & ~3) : 0;
-                    unsigned char *stg = smem + st * kSpmvStageBytes;
-                    int *hdr = (int *)(stg + kSpmvRows * 4);
-                    hdr[0] = sk;
-                    hdr[1] = ek;
-                    hdr[2] = kp;
-                    TileGeom<V> g = tile_geom_se<V>(sk, ek, use_tma);
-                    V *sv = (V *)(stg + kSpmvHdr);
-                    int *si = (int *)(stg + kSpmvHdr + CAP * sizeof(V));
-                    uint32_t bp = (uint32_t)kp * 4;
-                    uint32_t bv = (uint32_t)(g.ev - g.sv) * sizeof(V);
-                    uint32_t bi = (uint32_t)(g.ei - g.si) * sizeof(int);
-                    if (bp + bv + bi == 0) {
-                        mbar_arrive(&full[st]);
-                    } else {
-                        mbar_arrive_tx(&full[st], bp + bv + bi);
-                        if (bp) bulk_g2s(stg, pntr + r0, bp, &full[st]);
-                        if (bv) bulk_g2s(sv, vals + g.sv, bv, &full[st]);
-                        if (bi) bulk_g2s(si, indx + g.si, bi, &full[st]);
-                    }
-                }
-            }
-        }
-    } else {
-        for (int j = 0; j < my_tiles; j++) {
-            const int tile = blockIdx.x + j * gridDim.x;
-            const int st = j % kSpmvStages;
-            const int r = tile * kSpmvRows + tid;
-            mbar_wait(&full[st], (uint32_t)((j / kSpmvStages) & 1), err);
-            const unsigned char *stg = smem + st * kSpmvStageBytes;
-            const int *sp = (const int *)stg;
-            const int *hdr = (const int *)(stg + kSpmvRows * 4);
-            const int kp = hdr[2];
-            const TileGeom<V> g = tile_geom_se<V>(hdr[0], hdr[1], use_tma);
-            if (r < n_rows) {
-                const int ps = (tid < kp) ? sp[tid] : __ldg(pntr + r);
-                const int pe = (tid + 1 < kp) ? sp[tid + 1] : ((tid + 1 == kSpmvRows) ? hdr[1] : __ldg(pntr + r + 1));
-                const V *svs = (const V *)(stg + kSpmvHdr);
-                const int *sis = (const int *)(stg + kSpmvHdr + CAP * sizeof(V));
-                X acc = X(0);
-                // up to 8 entries at a time: all x gathers in flight together, then the sum in
-                // column order (the reference's sequential order, so the result keeps its bits)
-                for (int j0 = ps; j0 < pe; j0 += 8) {
-                    X xv[8], vv[8];
-#pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const int jj = j0 + k;
-                        if (jj < pe) {
-                            V v = (jj < g.ev) ? svs[jj - g.sv] : __ldg(vals + jj);
-                            int c = (jj < g.ei) ? sis[jj - g.si] : __ldg(indx + jj);
-                            vv[k] = Val<V>::get(v);
-                            xv[k] = __ldg(x + c);
-                        }
-                    }
-#pragma unroll
-                    for (int k = 0; k < 8; k++)
-                        if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
-                }
-                X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
-                y[r] = out;
-                if (FUSE_DOT) dacc.add(__ldg(x + r), out);
-            }
-            named_bar_sync(1, kSpmvRows);   // every consumer is done with stage st
-            if (tid == 0) mbar_arrive(&empty[st]);
-        }
-    }
-    if (FUSE_DOT) {
-        double dsum[1] = {dacc.get()};
-        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
-    }
-}
-
-// Full-occupancy variant without shared memory: one row per thread, grid-stride, the row's
-// vals/indx and x gathers (8 at a time) straight from global through L1.  Same arithmetic.
-template <typename V, bool FUSE_DOT>
-__global__ void __launch_bounds__(256)
-spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
-                   const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
-                   typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter,
-                   double *dot_out, const int *skip) {
-    using X = typename Val<V>::X;
-    if (skip && *skip) return;
-    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
-        const int ps = __ldg(pntr + r), pe = __ldg(pntr + r + 1);
-        X acc = X(0);
-        for (int j0 = ps; j0 < pe; j0 += 8) {
-            X xv[8], vv[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++)
-                if (j0 + k < pe) {
-                    vv[k] = Val<V>::get(__ldg(vals + j0 + k));
-                    xv[k] = __ldg(x + __ldg(indx + j0 + k));
-                }
-#pragma unroll
-            for (int k = 0; k < 8; k++)
-                if (j0 + k < pe) acc = add_rn(acc, mul_rn(vv[k], xv[k]));
-        }
-        X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[r]));
-        y[r] = out;
-        if (FUSE_DOT) dacc.add(__ldg(x + r), out);
-    }
-    if (FUSE_DOT) {
-        double dsum[1] = {dacc.get()};
-        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
-    }
-}
-
-// Warp-tiled SpMV: each warp owns a contiguous run of 32-row tiles.  For every tile it copies the
-// tile's whole vals / indx range into its own shared-memory buffer with 16-byte cp.async
-// (coalesced, no cross-warp handshake); every lane then sums its row from shared memory, gathering
-// x from global memory kGW entries at a time.  The warp double-buffers: the copy of tile k+1 and
-// the row pointers of tile k+2 are in flight while tile k is summed.  Tiles of more than kWarpCap
-// entries read their rows directly.
 static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 constexpr int kWarpCap = 256;
 constexpr int kWarpBlock = 256;   // 8 warps per CTA
 constexpr int kGW = 4;            // x gathers in flight per lane
 
-template <typename V, bool FUSE_DOT>
+// acc += v * x in the mode's rounding
+template <bool EXACT>
+__device__ __forceinline__ double spmv_acc(double acc, double v, double x) {
+    return EXACT ? add_rn(acc, mul_rn(v, x)) : __fma_rn(v, x, acc);
+}
+template <bool EXACT>
+__device__ __forceinline__ float spmv_acc(float acc, float v, float x) {
+    return EXACT ? add_rn(acc, mul_rn(v, x)) : __fmaf_rn(v, x, acc);
+}
+// alpha * acc + beta * y (y read only when beta != 0)
+template <bool EXACT, typename X>
+__device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
+    if (EXACT) return (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, *yp));
+    if (beta == X(0)) return (alpha == X(1)) ? acc : mul_rn(alpha, acc);
+    return spmv_acc<false>(mul_rn(beta, *yp), alpha, acc);
+}
+
+// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A)
+template <typename V, bool FUSE_DOT, bool EXACT>
 __global__ void __launch_bounds__(kWarpBlock)
 spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
                  typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, typename Val<V>::X beta,
@@ -295,7 +128,7 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
                             }
 #pragma unroll
                         for (int q = 0; q < kGW; q++)
-                            if (j0 + q < pe0) acc = add_rn(acc, mul_rn(vv[q], xv[q]));
+                            if (j0 + q < pe0) acc = spmv_acc<EXACT>(acc, vv[q], xv[q]);
                     }
                 } else {
                     for (int j0 = ps0; j0 < pe0; j0 += kGW) {
@@ -308,10 +141,10 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
                             }
 #pragma unroll
                         for (int q = 0; q < kGW; q++)
-                            if (j0 + q < pe0) acc = add_rn(acc, mul_rn(vv[q], xv[q]));
+                            if (j0 + q < pe0) acc = spmv_acc<EXACT>(acc, vv[q], xv[q]);
                     }
                 }
-                const X out = (beta == X(0)) ? mul_rn(alpha, acc) : add_rn(mul_rn(alpha, acc), mul_rn(beta, y[row]));
+                const X out = spmv_out<EXACT>(alpha, acc, beta, y + row);
                 y[row] = out;
                 if (FUSE_DOT) dacc.add(__ldg(x + row), out);
             }
@@ -331,17 +164,43 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
     }
 }
 
-// SpMV variant: warp-tiled (default), "direct" (thread per row, no staging) or "tma" (CTA-wide
-// bulk-copy ring), selected by HGB_SPMV for comparisons
-static int spmv_variant() {
-    static int v = [] {
-        const char *e = getenv("HGB_SPMV");
-        if (e && std::string(e) == "direct") return 1;
-        if (e && std::string(e) == "tma") return 2;
-        return 0;
-    }();
-    return v;
+// Arrays that are not 16-byte aligned cannot be staged with cp.async: one row per thread,
+// grid-stride, the row's vals/indx and x gathers (8 at a time) straight from global memory
+// through L1.  Same arithmetic as spmv_warp_kernel.
+template <typename V, bool FUSE_DOT, bool EXACT>
+__global__ void __launch_bounds__(256)
+spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
+                   const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
+                   typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter,
+                   double *dot_out, const int *skip) {
+    using X = typename Val<V>::X;
+    if (skip && *skip) return;
+    DotAcc<X> dacc;   // fused <x, y> (per-thread partial)
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+        const int ps = __ldg(pntr + r), pe = __ldg(pntr + r + 1);
+        X acc = X(0);
+        for (int j0 = ps; j0 < pe; j0 += 8) {
+            X xv[8], vv[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (j0 + k < pe) {
+                    vv[k] = Val<V>::get(__ldg(vals + j0 + k));
+                    xv[k] = __ldg(x + __ldg(indx + j0 + k));
+                }
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (j0 + k < pe) acc = spmv_acc<EXACT>(acc, vv[k], xv[k]);
+        }
+        const X out = spmv_out<EXACT>(alpha, acc, beta, y + r);
+        y[r] = out;
+        if (FUSE_DOT) dacc.add(__ldg(x + r), out);
+    }
+    if (FUSE_DOT) {
+        double dsum[1] = {dacc.get()};
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    }
 }
+
 
 // transposed product by atomic scatter (stateless path): y[c] += (alpha * x[i]) * v_ic
 template <typename V>
@@ -530,65 +389,42 @@ void Transpose::release() {
     pntr = row = map = nullptr;
 }
 
+template <typename V, bool FUSE_DOT, bool EXACT>
+static int spmv_n_launch_mode(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
+                              typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
+                              typename Val<V>::X *y, double *dot_out, const int *skip) {
+    double *partials = FUSE_DOT ? c->partials : nullptr;
+    unsigned *counter = FUSE_DOT ? c->counter : nullptr;
+    if (aligned16(vals) && aligned16(indx)) {
+        // persistent grid: the resident CTAs of every SM (occupancy queried once per kernel)
+        static int occ = 0;
+        if (!occ) {
+            HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmv_warp_kernel<V, FUSE_DOT, EXACT>, kWarpBlock, 0));
+            occ = std::max(occ, 1);
+        }
+        const long tiles = ((long)n_rows + 31) / 32;
+        const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, std::min(c->num_sms * occ, kMaxReduceBlocks)));
+        spmv_warp_kernel<V, FUSE_DOT, EXACT><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
+                                                                            partials, counter, dot_out, skip);
+        return launch_check("spmv_warp_kernel");
+    }
+    const int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
+    spmv_direct_kernel<V, FUSE_DOT, EXACT><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, partials,
+                                                                   counter, dot_out, skip);
+    return launch_check("spmv_direct_kernel");
+}
 
 template <typename V>
 int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
                   typename Val<V>::X *y, double *dot_out, const int *skip) {
     if (n_rows <= 0) return HGB_OK;
-    const int variant = spmv_variant();
-    if (variant == 0 && aligned16(vals) && aligned16(indx)) {
-        // persistent grid: the resident CTAs of every SM (occupancy queried once per kernel)
-        static int occ[2] = {0, 0};
-        int &o = occ[dot_out ? 1 : 0];
-        if (!o) {
-            if (dot_out) HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmv_warp_kernel<V, true>, kWarpBlock, 0));
-            else HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, spmv_warp_kernel<V, false>, kWarpBlock, 0));
-            o = std::max(o, 1);
-        }
-        const long tiles = ((long)n_rows + 31) / 32;
-        const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, std::min(c->num_sms * o, kMaxReduceBlocks)));
-        if (dot_out)
-            spmv_warp_kernel<V, true><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
-                                                                     c->partials, c->counter, dot_out, skip);
-        else
-            spmv_warp_kernel<V, false><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
-                                                                      nullptr, nullptr, nullptr, skip);
-        return launch_check("spmv_warp_kernel");
-    }
-    if (variant != 2) {
-        int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
-        if (dot_out)
-            spmv_direct_kernel<V, true><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, c->partials,
-                                                                 c->counter, dot_out, skip);
-        else
-            spmv_direct_kernel<V, false><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr,
-                                                                  nullptr, nullptr, skip);
-        return launch_check("spmv_direct_kernel");
-    }
-    int ntiles = (n_rows + kSpmvRows - 1) / kSpmvRows;
-    int grid = std::min(ntiles, c->num_sms * 2);
-    int tma = (aligned16(vals) && aligned16(indx) && aligned16(pntr)) ? 1 : 0;
-    if (dot_out) {
-        grid = std::min(grid, kMaxReduceBlocks);
-        spmv_n_kernel<V, true><<<grid, kSpmvRows + 32, kSpmvSmem, c->stream>>>(
-            n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, c->partials, c->counter, dot_out, c->err, skip);
-    } else {
-        spmv_n_kernel<V, false><<<grid, kSpmvRows + 32, kSpmvSmem, c->stream>>>(
-            n_rows, ntiles, pntr, indx, vals, alpha, x, beta, y, tma, nullptr, nullptr, nullptr, c->err, skip);
-    }
-    return launch_check("spmv_n_kernel");
-}
-
-int spmv_init_attributes() {
-    // cudaFuncSetAttribute is per device; the context creation calls this on its device
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<uint16_t, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    HGB_CUDA(cudaFuncSetAttribute(spmv_n_kernel<uint16_t, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpmvSmem));
-    return HGB_OK;
+    const bool exact = c->spmv_mode == HGB_SPMV_EXACT;
+    if (dot_out)
+        return exact ? spmv_n_launch_mode<V, true, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip)
+                     : spmv_n_launch_mode<V, true, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip);
+    return exact ? spmv_n_launch_mode<V, false, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip)
+                 : spmv_n_launch_mode<V, false, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip);
 }
 
 template int spmv_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, double,

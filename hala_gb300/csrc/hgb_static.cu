@@ -1,20 +1,28 @@
 // Dot product that allocates nothing: its scratch is a file-scope device array.
 //
 // Who needs it: a caller that may not allocate device memory at the point it needs a reduction:
-// code that runs while another component owns the allocator (a pool that must not grow), code
-// inside a stream callback or a host function node where cudaMalloc is not allowed, or a host
-// integration that forbids creating a context object (hgb_ctx_create allocates its scratch with
-// cudaMalloc).  hgb_dot_f64_noalloc takes only the inputs, a device result pointer and a stream.
+// code that runs while another component owns the allocator (a memory pool that must not grow, a
+// budget fixed at start-up), or a host integration that may not create a context object
+// (hgb_ctx_create allocates its scratch with cudaMalloc).  hgb_dot_f64_noalloc takes only the
+// inputs, a device result pointer and a stream, and calls no cudaMalloc, cudaFree or allocating
+// library routine.  It does call the CUDA runtime (a device query, a symbol lookup and a kernel
+// launch), so it must not be called from a stream callback or a host function node, where CUDA
+// API calls are not allowed.
 //
-// The scratch (one partial sum per block of kSpan entries plus an arrival counter) lives in
-// g_noalloc_scratch below, which every GPU that loads libhgb holds until the process exits.
-// Host code cannot use the array's name as a device address (in host code it names a host-side
-// stand-in), so the first call on each device looks the address up with cudaGetSymbolAddress,
-// with that device current, and passes it to the kernel.  That first call also clears the
-// counter; make it before any stream capture.  All calls share the array: two calls whose
-// kernels overlap on the GPU (different streams, or concurrent host threads) race on it and
-// must be ordered by the caller.
+// The scratch (one partial sum per block of kNoAllocSpan entries plus an arrival counter) lives
+// in g_noalloc_scratch below, which every GPU that loads libhgb holds until the process exits.
+// Device memory of a static __device__ array starts at zero when the module loads, and the last
+// block of every launch sets the counter back to zero, so no call clears it.  Host code cannot use
+// the array's name as a device address (in host code it names a host-side stand-in), so the first
+// call on each device, with that device current, looks the address up with cudaGetSymbolAddress
+// and passes it to the kernel; that first call should come before any stream capture.  The address
+// is kept per device and per CUDA context, so a new context on the device (after
+// cudaDeviceReset, or a driver-API context made current) is looked up again.  All calls share the
+// array: two calls whose kernels overlap on the GPU (different streams, or concurrent host
+// threads) race on it and must be ordered by the caller.
 #include "hgb_internal.cuh"
+
+#include <cuda.h>
 
 #include <mutex>
 
@@ -38,25 +46,42 @@ __global__ void dot_noalloc_kernel(long n, const double *__restrict__ x, const d
 }
 
 struct NoAllocDevice {
-    bool ready = false;
+    void *context = nullptr;   // CUDA context the address was looked up in
     double *scratch = nullptr;
 };
 static NoAllocDevice g_dev[64];
 static std::mutex g_mu;
 
-// Once per device, with that device current: the device address of the array, counter cleared.
+// The current CUDA context, through the driver entry point the runtime exposes (libhgb does not
+// link the driver library); null when the lookup is unavailable.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+static void *current_context() {
+    static CtxGetCurrentFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        cudaGetLastError();
+        return (CtxGetCurrentFn)p;
+    }();
+    CUcontext ctx = nullptr;
+    if (fn && fn(&ctx) == CUDA_SUCCESS) return (void *)ctx;
+    return nullptr;
+}
+
+// Set-up, once per device and context, with that device current: the device address of the array.
 static int noalloc_setup(int dev, double **scratch) {
     std::lock_guard<std::mutex> lock(g_mu);
     if (dev < 0 || dev >= 64) return fail(HGB_ERR_ARG, "dot_f64_noalloc: device %d", dev);
     NoAllocDevice &d = g_dev[dev];
-    if (!d.ready) {
+    void *ctx = current_context();
+    if (!d.scratch || !ctx || ctx != d.context) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        e = cudaMemset((double *)p + kNoAllocMaxParts, 0, 2 * sizeof(double));
-        if (e != cudaSuccess) return cuda_fail(e, "dot_f64_noalloc setup");
         d.scratch = (double *)p;
-        d.ready = true;
+        d.context = ctx;
     }
     *scratch = d.scratch;
     return HGB_OK;

@@ -62,6 +62,17 @@ class gpu_engine:
     def synchronize(self):
         check(_h.lib().hgb_ctx_synchronize(self.h))
 
+    def set_spmv_mode(self, mode):
+        """'exact' (separately rounded multiply and add: bit-identical to the reference's CPU
+        product) or 'fused' (one fused multiply-add per entry, the default)."""
+        m = {"fused": _h.HGB_SPMV_FUSED, "exact": _h.HGB_SPMV_EXACT}[mode]
+        check(_h.lib().hgb_ctx_set_spmv_mode(self.h, m), "set_spmv_mode")
+
+    def spmv_mode(self):
+        m = C.c_int()
+        check(_h.lib().hgb_ctx_get_spmv_mode(self.h, C.byref(m)), "spmv_mode")
+        return "exact" if m.value == _h.HGB_SPMV_EXACT else "fused"
+
     def __del__(self):
         try:
             if getattr(self, "h", None):

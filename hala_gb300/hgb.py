@@ -13,6 +13,7 @@ from . import build as _build
 HGB_OK, HGB_ERR_ARG, HGB_ERR_CSR, HGB_ERR_ZERO_PIVOT, HGB_ERR_TIMEOUT = 0, 1, 2, 3, 4
 HGB_ERR_NOT_CONVERGED, HGB_ERR_CUDA, HGB_ERR_ALLOC, HGB_ERR_UNSUPPORTED = 5, 6, 7, 8
 HGB_F64, HGB_F32, HGB_BF16 = 0, 1, 2
+HGB_SPMV_FUSED, HGB_SPMV_EXACT = 0, 1
 
 
 class HgbError(RuntimeError):
@@ -43,6 +44,8 @@ _SIGS = {
     "hgb_ctx_destroy": ([vp], i32),
     "hgb_ctx_set_stream": ([vp, vp], i32),
     "hgb_ctx_synchronize": ([vp], i32),
+    "hgb_ctx_set_spmv_mode": ([vp, i32], i32),
+    "hgb_ctx_get_spmv_mode": ([vp, C.POINTER(i32)], i32),
     "hgb_dot_f64": ([vp, i32, vp, vp, vp, i32], i32),
     "hgb_dot_f32": ([vp, i32, vp, vp, vp, i32], i32),
     "hgb_nrm2_f64": ([vp, i32, vp, vp, i32], i32),

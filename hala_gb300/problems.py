@@ -124,6 +124,12 @@ def vardiff2d_faces(n, kcell):
 def vardiff2d(n, kcell):
     """5-point finite-volume -div(k grad u) on n x n unit cells (h = 1)."""
     kx, ky = vardiff2d_faces(n, kcell)
+    return vardiff2d_from_faces(n, kx, ky)
+
+
+def vardiff2d_from_faces(n, kx, ky):
+    """The 5-point operator's CSR for given face conductivities kx (n, n+1) and ky (n+1, n),
+    [y][x] arrays.  Linear in the faces, so face changes give the operator's change."""
     west = kx[:, :-1].reshape(-1)
     east = kx[:, 1:].reshape(-1)
     south = ky[:-1, :].reshape(-1)

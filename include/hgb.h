@@ -42,6 +42,15 @@ typedef enum hgb_status {
 
 typedef enum hgb_dtype { HGB_F64 = 0, HGB_F32 = 1, HGB_BF16 = 2 } hgb_dtype;
 
+/* Arithmetic of the non-transposed SpMV (and of every solver product built on it).
+ * HGB_SPMV_FUSED: one fused multiply-add per entry in column order (the default; within a few
+ *   ulps of the row sum of the reference's loop; the FP64 product is about twice as fast on
+ *   sm_103, whose FP64 pipe is narrow).
+ * HGB_SPMV_EXACT: separately rounded multiply and add in column order, the arithmetic of
+ *   sparse_gemv_array (sparse/hala_sparse_utils.hpp:104-112): bit-identical to the reference's
+ *   CPU product. */
+typedef enum hgb_spmv_mode { HGB_SPMV_FUSED = 0, HGB_SPMV_EXACT = 1 } hgb_spmv_mode;
+
 typedef struct hgb_ctx hgb_ctx;
 typedef struct hgb_csr hgb_csr;
 typedef struct hgb_ilu hgb_ilu;
@@ -71,6 +80,9 @@ int hgb_ctx_destroy(hgb_ctx *ctx);
 /* gpu_engine::set_stream, gpu/hala_gpu_engine.hpp:86-90 (stream is a cudaStream_t) */
 int hgb_ctx_set_stream(hgb_ctx *ctx, void *stream);
 int hgb_ctx_synchronize(hgb_ctx *ctx);
+/* SpMV arithmetic of this context (hgb_spmv_mode); applies to products issued after the call. */
+int hgb_ctx_set_spmv_mode(hgb_ctx *ctx, int mode);
+int hgb_ctx_get_spmv_mode(hgb_ctx *ctx, int *mode);
 
 /* ------------------------------------------------------- BLAS-1 (gpu/hala_gpu_blas1.hpp) --- */
 /* result: host pointer (synchronises) when result_on_device == 0, else device pointer.
@@ -99,9 +111,10 @@ int hgb_gemv_f64(hgb_ctx *ctx, char trans, int m, int k, double alpha, const dou
 
 /* ------------------------------------------ SpMV (sparse_gemv(gpu_engine,...), :408-419) --- */
 /* y = alpha * op(A) x + beta * y; A is n_rows x n_cols CSR.  trans 'N', 'T' or 'C' (real: C==T).
- * beta == 0 does not read y.  'N' rows are summed sequentially in column order without fused
- * multiply-add, the arithmetic of sparse_gemv_array (sparse/hala_sparse_utils.hpp:104-112).
- * 'T' without a matrix handle scatters with atomics (order not fixed). */
+ * beta == 0 does not read y.  'N' rows are summed sequentially in column order, with the context's
+ * hgb_spmv_mode (HGB_SPMV_EXACT: no fused multiply-add, the arithmetic of sparse_gemv_array,
+ * sparse/hala_sparse_utils.hpp:104-112).  'T' without a matrix handle scatters with atomics
+ * (order not fixed). */
 int hgb_spmv_f64(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
                  const int *indx, const double *vals, double alpha, const double *x, double beta,
                  double *y);
@@ -138,8 +151,9 @@ int hgb_diag_index(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *ind
  * order of factorize_ilu_array (sparse/hala_sparse_utils.hpp:229-255) and no fused multiply-add,
  * so the F64 factor is bit-identical to the reference CPU factor.  vals_dtype F64 or F32 selects
  * the factorisation precision; store selects the precision the triangular solves read:
- * F64 (vectors double), F32 or BF16 (vectors float; pivots kept in FP64, the division by the
- * pivot done in FP64).  policy 'L'/'N' is accepted for signature parity; level scheduling is
+ * F64 (vectors double), F32 or BF16 (vectors float; the pivots stay FP64: each pivot's reciprocal
+ * is computed in FP64 and rounded once to FP32, and the FP32 backward sweep multiplies by it).
+ * policy 'L'/'N' is accepted for signature parity; level scheduling is
  * always used.  Returns HGB_ERR_ZERO_PIVOT (with a valid handle) when a pivot is exactly 0. */
 int hgb_ilu0_create(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx,
                     const void *vals, hgb_dtype vals_dtype, hgb_dtype store, char policy,
@@ -286,13 +300,15 @@ int hgb_batch_destroy(hgb_batch *batch);
 
 /* ------------------------------------------------------- allocation-free reduction ---- */
 /* No counterpart in the reference.  *result_device = <x, y> for callers that may not allocate
- * device memory where they need the reduction (an allocator owned by someone else, a stream
- * callback, a host integration that cannot create an hgb_ctx, which allocates).  Needs no
- * context: the partial sums live in a static device array (one per 2048 entries), so
- * n <= 33,554,432; larger n returns HGB_ERR_ARG before any launch.  The first call on a device
- * looks the array up (cudaGetSymbolAddress) and clears its counter: make it before any stream
- * capture.  Calls share the array, so calls whose kernels overlap on the GPU race.  Runs on the
- * current device, on the given stream (cudaStream_t, may be NULL); does not synchronise. */
+ * device memory where they need the reduction (an allocator or memory budget owned by another
+ * component, or a host integration that may not create an hgb_ctx, which allocates).  Needs no
+ * context and calls no allocating routine: the partial sums live in a static device array (one per
+ * 2048 entries), so n <= 33,554,432; larger n returns HGB_ERR_ARG before any launch.  The first
+ * call on a device (and in each new CUDA context on it) looks the array's address up with
+ * cudaGetSymbolAddress: make it before any stream capture.  It makes CUDA runtime calls, so it
+ * must not be called from a stream callback or host function node.  Calls share the array, so
+ * calls whose kernels overlap on the GPU race.  Runs on the current device, on the given stream
+ * (cudaStream_t, may be NULL); does not synchronise. */
 int hgb_dot_f64_noalloc(int n, const double *x, const double *y, double *result_device,
                         void *stream);
 

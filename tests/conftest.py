@@ -22,7 +22,19 @@ def eng():
     from hala_gb300 import build
     build.build()
     from hala_gb300 import engine as E
-    return E.gpu_engine(0)
+    e = E.gpu_engine(0)
+    # parity tests compare products bit for bit with the reference's separately rounded loop
+    e.set_spmv_mode("exact")
+    return e
+
+
+@pytest.fixture(scope="session")
+def eng_fused(eng):
+    """An engine in the default SpMV mode (one fused multiply-add per entry)."""
+    from hala_gb300 import engine as E
+    e = E.gpu_engine(0)
+    assert e.spmv_mode() == "fused"
+    return e
 
 
 @pytest.fixture

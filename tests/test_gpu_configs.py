@@ -117,6 +117,30 @@ def test_ru_pcg_aniso128(eng, aniso128):
     assert within5(info.iterations, ito - 1), (info.iterations, ito)
 
 
+def test_pcg_aniso128_fused_spmv(eng_fused, aniso128):
+    # the benchmark's forms in the default SpMV mode (one FMA per entry): FP64 PCG and the mixed
+    # reliable-update PCG, against the FP64 oracle's iteration count and solution
+    p, i, v, xt, b, tol, xo, ito = aniso128
+    n = len(p) - 1
+    gp, gi, gv = T(p), T(i), T(v)
+    A64 = E.make_sparse_matrix(eng_fused, n, gp, gi, gv)
+    M64 = E.make_ilu(eng_fused, gp, gi, gv)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    info = E.solve_cg_info(eng_fused, A64, M64, T(b), x, tol)
+    assert within5(info.iterations, ito), (info.iterations, ito)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < 2 * tol
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
+    A32 = E.make_sparse_matrix(eng_fused, n, gp, gi, gv.to(torch.float32))
+    M32 = E.make_ilu(eng_fused, gp, gi, gv, store=torch.float32)
+    x.zero_()
+    info = E.solve_ru_pcg(eng_fused, A64, A32, M32, T(b), x, tol, delta=0.01)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < tol
+    assert np.linalg.norm(xs - xo) <= 1e-7 * np.linalg.norm(xo)
+    assert within5(info.iterations, ito - 1), (info.iterations, ito)
+
+
 @pytest.fixture(scope="module")
 def convdiff96(eng):
     p, i, v = P.convdiff3d(96)

@@ -1,7 +1,9 @@
 """SpMV and BLAS-1 on the GPU, through the C ABI, against the CPU oracle.
 
-Tolerances: 'N' products (and the cached transpose) are compared BIT-EXACTLY with the oracle's
-sequential row loop; the atomic transpose and the reductions (dot, nrm2, fused dot) within 1e-13
+Tolerances: in the exact SpMV mode 'N' products (and the cached transpose) are compared
+BIT-EXACTLY with the oracle's sequential row loop; in the default fused mode (one FMA per entry)
+within 1e-14 relative (norm-wise, and per row within the rounding bound of the row's sum) in FP64
+and 1e-6 in FP32; the atomic transpose and the reductions (dot, nrm2, fused dot) within 1e-13
 relative in FP64 and 1e-6 in FP32."""
 import numpy as np
 import pytest
@@ -62,7 +64,53 @@ def test_spmv_n_f64_bit_exact(eng, rng, name, ab):
     assert np.array_equal(gy.cpu().numpy(), ref)
 
 
-def test_spmv_unaligned_pointers_take_plain_path(eng, rng):
+def _row_bound(p, i, v, x, alpha, beta, y0, eps):
+    """Per-row bound on the difference of two roundings of alpha * sum_j a_ij x_j + beta * y_i
+    (each within gamma_k * sum of |terms|, k = row length + 3)."""
+    n = len(p) - 1
+    s = np.zeros(n)
+    lens = np.diff(p)
+    rows = np.repeat(np.arange(n), lens)
+    np.add.at(s, rows, np.abs(v * x[i]))
+    k = lens + 3
+    mag = np.abs(alpha) * s + (np.abs(beta * y0) if beta != 0 else 0.0)
+    return 2 * k * eps * mag
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("ab", [(1.0, 0.0), (2.0, 0.0), (-1.0, 1.0), (0.5, -0.25)])
+def test_spmv_n_fused_f64_within_1e14(eng_fused, rng, name, ab):
+    p, i, v = CASES[name](rng)
+    m = len(p) - 1
+    ncols = int(i.max()) + 1 if len(i) else 1
+    x = rng.standard_normal(ncols)
+    y0 = rng.standard_normal(m)
+    alpha, beta = ab
+    ref = O.spmv("N", m, ncols, alpha, p, i, v, x, beta, y0)
+    gy = T(y0)
+    E.sparse_gemv(eng_fused, "N", m, ncols, alpha, T(p), T(i), T(v), T(x), beta, gy)
+    y = gy.cpu().numpy()
+    assert np.linalg.norm(y - ref) <= 1e-14 * np.linalg.norm(ref)
+    assert np.all(np.abs(y - ref) <= _row_bound(p, i, v, x, alpha, beta, y0, 2.0**-53))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_spmv_n_fused_f32_within_1e6(eng_fused, rng, name):
+    p, i, v = CASES[name](rng)
+    m = len(p) - 1
+    ncols = int(i.max()) + 1 if len(i) else 1
+    x = rng.standard_normal(ncols).astype(np.float32)
+    v32 = v.astype(np.float32)
+    ref = O.spmv("N", m, ncols, 1.0, p, i, v32, x, 0.0)
+    gy = torch.zeros(m, dtype=torch.float32, device=dev)
+    E.sparse_gemv(eng_fused, "N", m, ncols, 1.0, T(p), T(i), T(v32), T(x), 0.0, gy)
+    y = gy.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(y - ref) <= 1e-6 * np.linalg.norm(ref)
+    bound = _row_bound(p, i, v32.astype(np.float64), x.astype(np.float64), 1.0, 0.0, None, 2.0**-24)
+    assert np.all(np.abs(y - ref) <= bound)
+
+
+def test_spmv_unaligned_pointers_take_plain_path(eng, eng_fused, rng):
     p, i, v = P.aniso3d(20)
     n = len(p) - 1
     x = rng.standard_normal(n)
@@ -74,6 +122,11 @@ def test_spmv_unaligned_pointers_take_plain_path(eng, rng):
     gy = torch.zeros(n, dtype=torch.float64, device=dev)
     E.sparse_gemv(eng, "N", n, n, 1.0, T(p), gi, gv, T(x), 0.0, gy)
     assert np.array_equal(gy.cpu().numpy(), ref)
+    # the fused mode takes the same plain path
+    gy.zero_()
+    E.sparse_gemv(eng_fused, "N", n, n, 1.0, T(p), gi, gv, T(x), 0.0, gy)
+    y = gy.cpu().numpy()
+    assert np.linalg.norm(y - ref) <= 1e-14 * np.linalg.norm(ref)
 
 
 @pytest.mark.parametrize("name", ["aniso3d_24", "irregular"])
