@@ -2,6 +2,7 @@
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -80,36 +81,44 @@ __global__ void scal_kernel(long n, T alpha, T *__restrict__ x) {
         x[i] *= alpha;
 }
 
-// Tall-skinny gemv for the Krylov basis: W is m x k column-major (k <= 64).
-// 'T': y[j] = alpha * <W[:,j], x> + beta * y[j]   (one grid reduction over k values)
-template <int KMAX>
-__global__ void gemv_t_kernel(int m, int k, double alpha, const double *__restrict__ W,
-                              const double *__restrict__ x, double beta, double *y,
+// Tall-skinny gemv for the Krylov basis: W is m x k column-major.
+// 'T': y[j] = alpha * <W[:,j], x> + beta * y[j] for the KMAX columns j0.. j0+KMAX (one grid
+// reduction, double accumulation); wider W takes one launch per group of 64 columns.
+template <int KMAX, typename T>
+__global__ void gemv_t_kernel(int m, int k, T alpha, const T *__restrict__ W, const T *__restrict__ x, T beta, T *y,
                               double *partials, unsigned *counter) {
-    // reduce in chunks of kReduceSlots columns per launch slot; k <= KMAX handled by looping
-    // over column groups inside the kernel with one grid_sum per group would need k passes of
-    // arrival counters, so partials are laid out [block][KMAX] and summed by the last CTA.
     double acc[KMAX];
 #pragma unroll
     for (int j = 0; j < KMAX; j++) acc[j] = 0.0;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += (long)gridDim.x * blockDim.x) {
-        double xi = x[i];
+        const double xi = (double)x[i];
 #pragma unroll
         for (int j = 0; j < KMAX; j++)
-            if (j < k) acc[j] += W[(long)j * m + i] * xi;
+            if (j < k) acc[j] += (double)W[(long)j * m + i] * xi;
     }
     grid_sum<KMAX>(acc, partials, counter, [&](double (&s)[KMAX]) {
-        for (int j = 0; j < k; j++) y[j] = (beta == 0.0) ? alpha * s[j] : alpha * s[j] + beta * y[j];
+        for (int j = 0; j < k; j++) y[j] = (beta == T(0)) ? (T)(alpha * s[j]) : (T)(alpha * s[j] + beta * y[j]);
     });
 }
 
 // 'N': y[i] = alpha * sum_j W[i,j] * c[j] + beta * y[i]
-__global__ void gemv_n_kernel(int m, int k, double alpha, const double *__restrict__ W,
-                              const double *__restrict__ c, double beta, double *__restrict__ y) {
+template <typename T>
+__global__ void gemv_n_kernel(int m, int k, T alpha, const T *__restrict__ W, const T *__restrict__ c, T beta,
+                              T *__restrict__ y) {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += (long)gridDim.x * blockDim.x) {
-        double s = 0.0;
+        T s = T(0);
         for (int j = 0; j < k; j++) s += W[(long)j * m + i] * c[j];
-        y[i] = (beta == 0.0) ? alpha * s : alpha * s + beta * y[i];
+        y[i] = (beta == T(0)) ? alpha * s : alpha * s + beta * y[i];
+    }
+}
+
+// C = diag(x) A (side 'L': row i scaled by x[i]) or A diag(x) (side 'R': column j by x[j]);
+// A, C m x k column-major, packed
+template <typename T>
+__global__ void dgmm_kernel(long m, long k, int left, const T *__restrict__ A, const T *__restrict__ x, T *C) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m * k; e += (long)gridDim.x * blockDim.x) {
+        const long i = e % m, j = e / m;
+        C[e] = A[e] * x[left ? i : j];
     }
 }
 
@@ -318,22 +327,60 @@ int hgb_set_zero(hgb_ctx *c, size_t bytes, void *x) {
     return HGB_OK;
 }
 
-int hgb_gemv_f64(hgb_ctx *c, char trans, int m, int k, double alpha, const double *W,
-                 const double *x, double beta, double *y) {
-    if (!c || m < 0 || k < 0 || k > 64) return fail(HGB_ERR_ARG, "gemv: m=%d k=%d (k <= 64)", m, k);
+}  // extern "C"
+
+namespace hgb {
+template <typename T>
+static int gemv_impl(hgb_ctx *c, char trans, int m, int k, T alpha, const T *W, const T *x, T beta, T *y) {
+    if (!c || m < 0 || k < 0) return fail(HGB_ERR_ARG, "gemv: m=%d k=%d", m, k);
     if (m == 0 || k == 0) return HGB_OK;
     DeviceGuard g(c->device);
     if (trans == 'N' || trans == 'n') {
-        gemv_n_kernel<<<reduce_grid(c, m, 256 * 2), 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y);
+        gemv_n_kernel<T><<<reduce_grid(c, m, 256 * 2), 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y);
         return launch_check("gemv_n_kernel");
     }
     if (trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') return fail(HGB_ERR_ARG, "gemv: trans '%c'", trans);
-    int grid = reduce_grid(c, m, 256 * 8);
-    if (k <= 8) gemv_t_kernel<8><<<grid, 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y, c->partials, c->counter);
-    else if (k <= 16) gemv_t_kernel<16><<<grid, 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y, c->partials, c->counter);
-    else if (k <= 32) gemv_t_kernel<32><<<grid, 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y, c->partials, c->counter);
-    else gemv_t_kernel<64><<<grid, 256, 0, c->stream>>>(m, k, alpha, W, x, beta, y, c->partials, c->counter);
-    return launch_check("gemv_t_kernel");
+    const int grid = reduce_grid(c, m, 256 * 8);
+    for (int j0 = 0; j0 < k; j0 += 64) {   // groups of up to 64 columns, one grid reduction each
+        const int kk = std::min(64, k - j0);
+        const T *Wj = W + (long)j0 * m;
+        T *yj = y + j0;
+        if (kk <= 8) gemv_t_kernel<8, T><<<grid, 256, 0, c->stream>>>(m, kk, alpha, Wj, x, beta, yj, c->partials, c->counter);
+        else if (kk <= 16) gemv_t_kernel<16, T><<<grid, 256, 0, c->stream>>>(m, kk, alpha, Wj, x, beta, yj, c->partials, c->counter);
+        else if (kk <= 32) gemv_t_kernel<32, T><<<grid, 256, 0, c->stream>>>(m, kk, alpha, Wj, x, beta, yj, c->partials, c->counter);
+        else gemv_t_kernel<64, T><<<grid, 256, 0, c->stream>>>(m, kk, alpha, Wj, x, beta, yj, c->partials, c->counter);
+        HGB_TRY(launch_check("gemv_t_kernel"));
+    }
+    return HGB_OK;
+}
+
+template <typename T>
+static int dgmm_impl(hgb_ctx *c, char side, int m, int k, const T *A, const T *x, T *C) {
+    if (!c || m < 0 || k < 0) return fail(HGB_ERR_ARG, "dgmm: m=%d k=%d", m, k);
+    if (side != 'L' && side != 'l' && side != 'R' && side != 'r') return fail(HGB_ERR_ARG, "dgmm: side '%c'", side);
+    if ((long)m * k == 0) return HGB_OK;
+    DeviceGuard g(c->device);
+    dgmm_kernel<T><<<reduce_grid(c, (long)m * k, 256 * 4), 256, 0, c->stream>>>(m, k, (side == 'L' || side == 'l') ? 1 : 0,
+                                                                                 A, x, C);
+    return launch_check("dgmm_kernel");
+}
+}  // namespace hgb
+
+extern "C" {
+
+int hgb_gemv_f64(hgb_ctx *c, char trans, int m, int k, double alpha, const double *W, const double *x, double beta,
+                 double *y) {
+    return gemv_impl<double>(c, trans, m, k, alpha, W, x, beta, y);
+}
+int hgb_gemv_f32(hgb_ctx *c, char trans, int m, int k, float alpha, const float *W, const float *x, float beta,
+                 float *y) {
+    return gemv_impl<float>(c, trans, m, k, alpha, W, x, beta, y);
+}
+int hgb_dgmm_f64(hgb_ctx *c, char side, int m, int k, const double *A, const double *x, double *C) {
+    return dgmm_impl<double>(c, side, m, k, A, x, C);
+}
+int hgb_dgmm_f32(hgb_ctx *c, char side, int m, int k, const float *A, const float *x, float *C) {
+    return dgmm_impl<float>(c, side, m, k, A, x, C);
 }
 
 int hgb_diag_index(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, int *diag) {

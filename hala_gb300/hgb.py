@@ -58,6 +58,9 @@ _SIGS = {
     "hgb_copy_f32": ([vp, i32, vp, vp], i32),
     "hgb_set_zero": ([vp, C.c_size_t, vp], i32),
     "hgb_gemv_f64": ([vp, ch, i32, i32, f64, vp, vp, f64, vp], i32),
+    "hgb_gemv_f32": ([vp, ch, i32, i32, f32, vp, vp, f32, vp], i32),
+    "hgb_dgmm_f64": ([vp, ch, i32, i32, vp, vp, vp], i32),
+    "hgb_dgmm_f32": ([vp, ch, i32, i32, vp, vp, vp], i32),
     "hgb_spmv_f64": ([vp, ch, i32, i32, i32, vp, vp, vp, f64, vp, f64, vp], i32),
     "hgb_spmv_f32": ([vp, ch, i32, i32, i32, vp, vp, vp, f32, vp, f32, vp], i32),
     "hgb_spmv_bf16f32": ([vp, ch, i32, i32, i32, vp, vp, vp, f32, vp, f32, vp], i32),

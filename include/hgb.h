@@ -104,10 +104,18 @@ int hgb_copy_f32(hgb_ctx *ctx, int n, const float *x, float *y);
 int hgb_set_zero(hgb_ctx *ctx, size_t bytes, void *x);
 
 /* ------------------------------------------------ dense gemv (gpu/hala_gpu_blas2.hpp:40) --- */
-/* y = alpha * op(W) x + beta * y, W column-major m x k (ld = m): the GMRES Krylov project and
- * combine, hex/solvers/hala_solvers_gmres.hpp:67-77 (tall-skinny, k <= 64). */
+/* y = alpha * op(W) x + beta * y, W column-major m x k (ld = m), tall and skinny: the GMRES Krylov
+ * project and combine, hex/solvers/hala_solvers_gmres.hpp:67-77, and the column sums of the batch
+ * reductions (wax/hala_blas_extensions.hpp:246).  'T' accumulates in double. */
 int hgb_gemv_f64(hgb_ctx *ctx, char trans, int m, int k, double alpha, const double *W,
                  const double *x, double beta, double *y);
+int hgb_gemv_f32(hgb_ctx *ctx, char trans, int m, int k, float alpha, const float *W,
+                 const float *x, float beta, float *y);
+/* C = diag(x) A (side 'L') or A diag(x) (side 'R'), A and C m x k column-major, packed: the column
+ * scalings of batch_axpy / batch_scal / batch_dot (dgmm(gpu_engine,...), gpu/hala_gpu_overloads.hpp,
+ * called from wax/hala_blas_extensions.hpp:211-265).  C may alias A. */
+int hgb_dgmm_f64(hgb_ctx *ctx, char side, int m, int k, const double *A, const double *x, double *C);
+int hgb_dgmm_f32(hgb_ctx *ctx, char side, int m, int k, const float *A, const float *x, float *C);
 
 /* ------------------------------------------ SpMV (sparse_gemv(gpu_engine,...), :408-419) --- */
 /* y = alpha * op(A) x + beta * y; A is n_rows x n_cols CSR.  trans 'N', 'T' or 'C' (real: C==T).
