@@ -34,24 +34,35 @@
 #include <algorithm>
 #include <climits>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 namespace hgb {
 
-constexpr int kBsThreads = 128;   // solver threads: one row per thread per step
+// Solver threads per CTA (NT, one row per thread per step): 128 for FP64 stores, whose 128 KB
+// slice holds one 16384-row block; 256 for FP32 / BF16 stores of patterns whose blocks hold two or
+// more planes of the wavefront (32768 rows): two solver warps per scheduler interleave the
+// latency-bound steps, and half as many blocks halve the hops between blocks.
+constexpr int kBsThreads = 128;
+constexpr int kBsThreadsWide = 256;
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
-constexpr int kBsCta = kBsThreads + 32 * kBsFetchWarps;
+template <int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * kBsFetchWarps; }
 constexpr int kBsF = 32;          // steps in the remote-value ring
 constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on its ring entry before
                                              // reading the value from L2 itself
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
-// value pieces per packet (NV) and packet-ring depth in steps (D, a power of two)
+// value pieces per packet (NV) and packet-ring depth in steps (bs_depth, a power of two; the wide
+// layout's slice leaves room for 4)
 template <typename V> struct BsCfg;
-template <> struct BsCfg<double> { static constexpr int NV = 3, D = 4; };
-template <> struct BsCfg<float> { static constexpr int NV = 2, D = 8; };
-template <> struct BsCfg<uint16_t> { static constexpr int NV = 1, D = 8; };
+template <> struct BsCfg<double> { static constexpr int NV = 3; };
+template <> struct BsCfg<float> { static constexpr int NV = 2; };
+template <> struct BsCfg<uint16_t> { static constexpr int NV = 1; };
+template <typename V, int NT> __host__ __device__ constexpr int bs_depth() {
+    return (sizeof(V) == 8 || NT != kBsThreads) ? 4 : 8;
+}
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
 // dependencies (kBsIdle: no row for this thread in this step), bit 31 set on the last step of a
@@ -64,27 +75,27 @@ __host__ __device__ constexpr int bs_word(int slot, int nd, int bar) {
 inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
 constexpr int kBsMaxCluster = 16;  // largest thread-block cluster (above 8: non-portable sizes)
 
-// shared memory: [packet ring D x (1 + NV) x 128 pieces | step descriptors |
-//                 remote-value ring kBsF x 128 | solution slice + zero slot]
-template <typename V, typename X>
+// shared memory: [packet ring D x (1 + NV) x NT pieces | step descriptors |
+//                 remote-value ring kBsF x NT | solution slice + zero slot]
+template <typename V, typename X, int NT>
 constexpr size_t bs_smem_bytes(int R) {
-    return (size_t)BsCfg<V>::D * (1 + BsCfg<V>::NV) * kBsThreads * 16 + (size_t)kBsStepCap * 16 +
-           (size_t)kBsF * kBsThreads * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
+    return (size_t)bs_depth<V, NT>() * (1 + BsCfg<V>::NV) * NT * 16 + (size_t)kBsStepCap * 16 +
+           (size_t)kBsF * NT * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
 }
 
-// One row's values, unpacked from its value pieces (pieces are kBsThreads int4 apart):
+// One row's values, unpacked from its value pieces (pieces are NT int4 apart in the ring):
 //   FP64 {v0, v1} {v2, RN(1/d)} {d, push, 0};  FP32 {v0, v1, v2, dv} {push, 0, 0, 0};
 //   BF16 {v0 | v1 << 16, v2, dv, push}
 // dv is the FP32 diagonal (divided by) or the FP32 reciprocal of an FP64 pivot (multiplied by).
-// push: where the row's value goes in the next block's remote ring (consumer step << 7 | thread),
+// push: where the row's value goes in the next block's remote ring (consumer step << 8 | thread),
 // or -1.
 template <typename V> struct BsRow;
 template <> struct BsRow<double> {
     double v[3], d, dinv;
     int push;
-    __device__ __forceinline__ void load(const int4 *p) {
-        const double2 a = *(const double2 *)p, b = *(const double2 *)(p + kBsThreads);
-        const int4 c = p[2 * kBsThreads];
+    template <int NT> __device__ __forceinline__ void load(const int4 *p) {
+        const double2 a = *(const double2 *)p, b = *(const double2 *)(p + NT);
+        const int4 c = p[2 * NT];
         v[0] = a.x;
         v[1] = a.y;
         v[2] = b.x;
@@ -96,19 +107,19 @@ template <> struct BsRow<double> {
 template <> struct BsRow<float> {
     float v[3], d;
     int push;
-    __device__ __forceinline__ void load(const int4 *p) {
+    template <int NT> __device__ __forceinline__ void load(const int4 *p) {
         const float4 a = *(const float4 *)p;
         v[0] = a.x;
         v[1] = a.y;
         v[2] = a.z;
         d = a.w;
-        push = p[kBsThreads].x;
+        push = p[NT].x;
     }
 };
 template <> struct BsRow<uint16_t> {
     float v[3], d;
     int push;
-    __device__ __forceinline__ void load(const int4 *p) {
+    template <int NT> __device__ __forceinline__ void load(const int4 *p) {
         const int4 a = *p;
         v[0] = __uint_as_float((unsigned)a.x << 16);
         v[1] = __uint_as_float((unsigned)a.x & 0xFFFF0000u);
@@ -231,18 +242,20 @@ __device__ __forceinline__ unsigned bs_peer_cas(uint32_t a, unsigned expect, uns
 // MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
 // UNIT: no division; RECIP: multiply by the stored FP32 reciprocal instead of dividing.
-template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
-__global__ void __launch_bounds__(kBsCta, 1)
+template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
+__global__ void __launch_bounds__(bs_cta<NT>(), 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
-    constexpr int NV = BsCfg<V>::NV, D = BsCfg<V>::D, NP = 1 + NV;
+    constexpr int NV = BsCfg<V>::NV, D = bs_depth<V, NT>(), NP = 1 + NV;
+    constexpr int CTA = bs_cta<NT>(), RPL = NT / 32;   // fetcher rows per lane
+    static_assert(NT == 128 || NT == 256, "solver threads");
     static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
     static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps, "remote ring shape");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
-    int4 *ring = (int4 *)smem;                          // [D][NP][kBsThreads]
-    int4 *sdesc = ring + D * NP * kBsThreads;           // [kBsStepCap]
-    X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][kBsThreads] remote values
-    X *xsbuf = rbuf + kBsF * kBsThreads;                // [R + 16 / sizeof(X) + 1]
+    int4 *ring = (int4 *)smem;                          // [D][NP][NT]
+    int4 *sdesc = ring + D * NP * NT;                   // [kBsStepCap]
+    X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][NT] remote values
+    X *xsbuf = rbuf + kBsF * NT;                        // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
     const int t = threadIdx.x;
     const unsigned rank = bs_cluster_rank(), ncl = bs_cluster_size();
@@ -250,7 +263,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         if (t == 0) atomicOr(A.err, DEV_ERR_CSR);
         return;
     }
-    const bool solver = t < kBsThreads;
+    const bool solver = t < NT;
     int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
     volatile X *vrbuf = rbuf;
     for (;;) {
@@ -263,7 +276,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             for (unsigned r = 0; r < ncl; r++) bs_peer_store(bs_peer(&blk_sh, r), q);
         }
         if (t == 0) done_step = -1;
-        for (int i = t; i < kBsF * kBsThreads; i += kBsCta) rbuf[i] = RingTag<X>::val(RingTag<X>::tag(i / kBsThreads));
+        for (int i = t; i < kBsF * NT; i += CTA) rbuf[i] = RingTag<X>::val(RingTag<X>::tag(i / NT));
         bs_cluster_sync();
         const int q = blk_sh;
         if (q * (int)ncl >= A.nblk) break;   // the same for the whole cluster
@@ -273,15 +286,15 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         const int ns = bi.y - bi.x, row_lo = bi.z, cnt = bi.w;
 
         // the block's step descriptors and its right-hand side slice, in one commit group
-        for (int i = t; i < ns; i += kBsCta) bs_copy16(sdesc + i, A.desc + bi.x + i);
+        for (int i = t; i < ns; i += CTA) bs_copy16(sdesc + i, A.desc + bi.x + i);
         constexpr int E = 16 / (int)sizeof(X);
         const X *src = in + row_lo;
         const int mis = (int)(((size_t)src & 15) / sizeof(X));
         X *xs = xsbuf + mis;   // xs[i] and src[i] sit at the same offset modulo 16 bytes
         const int head = min(cnt, (E - mis) % E);
         const int body = (cnt - head) / E;
-        for (int i = t; i < body; i += kBsCta) bs_copy16(xs + head + i * E, src + head + i * E);
-        for (int i = head + body * E + t; i < cnt; i += kBsCta) xs[i] = src[i];
+        for (int i = t; i < body; i += CTA) bs_copy16(xs + head + i * E, src + head + i * E);
+        for (int i = head + body * E + t; i < cnt; i += CTA) xs[i] = src[i];
         if (t < head) xs[t] = src[t];
         if (t == 0) xs[A.R] = X(0);
         bs_commit();
@@ -290,14 +303,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 
         if (!solver) {
             // ---- fetcher warps: warp w takes steps w, w+4, w+8, ... one at a time, polling the
-            // step's remote values (four rows per lane) until all are deposited; the remote rows of
+            // step's remote values (RPL rows per lane) until all are deposited; the remote rows of
             // its next step are loaded meanwhile
-            const int w = (t - kBsThreads) >> 5, l = t & 31;
-            int jq[4], jn[4];
-            auto load_rj = [&](int s, int (&jr)[4]) {
+            const int w = (t - NT) >> 5, l = t & 31;
+            int jq[RPL], jn[RPL];
+            auto load_rj = [&](int s, int (&jr)[RPL]) {
                 const int4 d = (s < ns) ? sdesc[s] : make_int4(0, 0, 0, 0);
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < RPL; q++) {
                     const int r = l + 32 * q;
                     jr[q] = (r < d.y) ? __ldg(A.rj + d.x + r) : -1;
                 }
@@ -315,13 +328,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     }
                     __nanosleep(128);
                 }
-                X *slot = rbuf + (s & (kBsF - 1)) * kBsThreads + l;
+                X *slot = rbuf + (s & (kBsF - 1)) * NT + l;
                 volatile X *vslot = slot;
                 using U = typename RingTag<X>::U;
                 const U want = RingTag<X>::tag(s);
                 unsigned todo = 0;
 #pragma unroll
-                for (int q = 0; q < 4; q++)   // rows whose value the block before has not offered yet
+                for (int q = 0; q < RPL; q++)   // rows whose value the block before has not offered yet
                     if (jq[q] >= 0 && RingTag<X>::bits(vslot[32 * q]) == want) todo |= 1u << q;
                 spins = 0;
                 // one lane polls a single value of the step until it is produced, then the warp
@@ -330,7 +343,10 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 const unsigned lanes = __ballot_sync(0xFFFFFFFFu, todo != 0);
                 if (lanes && l == __ffs(lanes) - 1) {
                     const int q0 = __ffs(todo) - 1;
-                    const int jrep = q0 == 0 ? jq[0] : (q0 == 1 ? jq[1] : (q0 == 2 ? jq[2] : jq[3]));
+                    int jrep = jq[0];
+#pragma unroll
+                    for (int q = 1; q < RPL; q++)
+                        if (q == q0) jrep = jq[q];
                     while (Pending<X>::is(ld_relaxed(out + jrep))) {
                         if (bs_give_up(++spins, A.err) || spins > kBsSpinLimitSleeping) break;
                         __nanosleep(32);
@@ -338,13 +354,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 }
                 __syncwarp();
                 while (todo) {
-                    X v[4];
+                    X v[RPL];
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
+                    for (int q = 0; q < RPL; q++)
                         if (todo & (1u << q)) v[q] = ld_relaxed(out + jq[q]);
                     const unsigned before = todo;
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
+                    for (int q = 0; q < RPL; q++)
                         if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
                             atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(v[q]));
                             todo &= ~(1u << q);
@@ -355,14 +371,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                         // give up: deposit NaN so that the solver threads terminate too
                         atomicOr(A.err, DEV_ERR_TIMEOUT);
 #pragma unroll
-                        for (int q = 0; q < 4; q++)
+                        for (int q = 0; q < RPL; q++)
                             if (todo & (1u << q))
                                 atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(Pending<X>::canon(Pending<X>::value())));
                         todo = 0;
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 4; q++) jq[q] = jn[q];
+                for (int q = 0; q < RPL; q++) jq[q] = jn[q];
             }
             continue;   // to the block-end barrier
         }
@@ -375,12 +391,12 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         auto issue = [&](int s) {
             if (s < ns) {
                 const int4 d = sdesc[s];
-                int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
+                int4 *slot = myring + (s & (D - 1)) * (NP * NT);
                 if (t < d.y) {
                     bs_copy16(slot, A.pk0 + d.x + t);
 #pragma unroll
                     for (int p = 0; p < NV; p++)
-                        bs_copy16(slot + (1 + p) * kBsThreads, A.pkv + (long)p * A.npk + d.x + t);
+                        bs_copy16(slot + (1 + p) * NT, A.pkv + (long)p * A.npk + d.x + t);
                 } else {
                     *slot = make_int4(A.R, A.R, A.R, bs_word(0, kBsIdle, (d.w >> 16) & 1));
                 }
@@ -408,11 +424,11 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         for (int s = 0; s < ns; s++) {
             issue(s + D - 1);
             cp_async_wait<D - 1>();   // step s has landed
-            const int4 *slot = myring + (s & (D - 1)) * (NP * kBsThreads);
+            const int4 *slot = myring + (s & (D - 1)) * (NP * NT);
             const int4 p0 = slot[0];
             const int w = p0.w, nd = (w >> 15) & 0xFFFF, sl = w & 0x7FFF;
             BsRow<V> rw;
-            rw.load(slot + kBsThreads);
+            rw.template load<NT>(slot + NT);
             const int code[kBsInline] = {p0.x, p0.y, p0.z};
             const X xin = xs[sl];
             // padding entries read the zero slot and the zero value: 0 * 0 leaves the sum unchanged
@@ -424,7 +440,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             // is polled directly
             {
                 const int k0 = code[0] < 0 ? 0 : (code[1] < 0 ? 1 : (code[2] < 0 ? 2 : -1));
-                volatile X *e = vrbuf + (s & (kBsF - 1)) * kBsThreads + t;
+                volatile X *e = vrbuf + (s & (kBsF - 1)) * NT + t;
                 X rv = *e;
                 if (k0 >= 0) {
                     const int c0 = (k0 == 0) ? code[0] : (k0 == 1 ? code[1] : code[2]);
@@ -465,14 +481,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
                     // if the entry awaits exactly that step; the result is not read, which measured
                     // faster than reading it a step later)
-                    const int ps = rw.push >> 7, pt = rw.push & 127;
-                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * kBsThreads + pt) * sizeof(X)),
+                    const int ps = rw.push >> 8, pt = rw.push & 255;
+                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * NT + pt) * sizeof(X)),
                                 RingTag<X>::tag(ps), RingTag<X>::bits(acc));
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
                            // to the fetchers when 8 steps have passed (they lag by < 24 < kBsF steps)
-                named_bar_sync(1, kBsThreads);
+                named_bar_sync(1, NT);
                 if (t == 0 && s - last_pub >= 8) {
                     bs_st_release(&done_step, s);
                     last_pub = s;
@@ -577,13 +593,15 @@ void BlockSolve::release() {
     *this = BlockSolve();
 }
 
-// Co-resident thread-block clusters of cl block-solve CTAs for blocks of R rows (queried once per
-// device, cluster size and block-size class).  On GB300 one CTA per SM fits, and 15 clusters of 8,
-// 36 of 4 or 76 of 2 are co-resident.
-static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
+// Co-resident thread-block clusters of cl block-solve CTAs of nt solver threads (queried once per
+// device, cluster size and layout, with the layout's largest shared memory).  On GB300 one CTA per
+// SM fits, and 15 clusters of 8, 36 of 4 or 76 of 2 are co-resident.
+static int bs_clusters_fit(hgb_ctx *c, int nt, int cl) {
     static int cache[64][2][kBsMaxCluster + 1];
     static bool init[64][2][kBsMaxCluster + 1];
-    const int ri = R <= 16384 ? 0 : 1;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    const int ri = nt == kBsThreads ? 0 : 1;
     if (c->device < 0 || c->device >= 64 || cl < 1 || cl > kBsMaxCluster) return 0;
     if (init[c->device][ri][cl]) return cache[c->device][ri][cl];
     auto fits = [&](auto kernel, size_t smem) {
@@ -594,7 +612,7 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cl * 16);
-        cfg.blockDim = dim3(kBsCta);
+        cfg.blockDim = dim3(ri == 0 ? bs_cta<kBsThreads>() : bs_cta<kBsThreadsWide>());
         cfg.dynamicSmemBytes = smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -611,9 +629,12 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
         return n;
     };
     DeviceGuard g(c->device);
-    // the largest shared-memory layout of the class (FP64 / FP32 store; BF16 needs less)
-    const int n = (ri == 0) ? fits(bsolve_kernel<double, double, 0, true, false>, bs_smem_bytes<double, double>(16384))
-                            : fits(bsolve_kernel<float, float, 0, true, false>, bs_smem_bytes<float, float>(32768));
+    // the largest shared-memory layout of the class (narrow: FP64 store; wide: FP32 store)
+    const int n = (ri == 0)
+                      ? fits(bsolve_kernel<double, double, 0, true, false, kBsThreads>,
+                             bs_smem_bytes<double, double, kBsThreads>(16384))
+                      : fits(bsolve_kernel<float, float, 0, true, false, kBsThreadsWide>,
+                             bs_smem_bytes<float, float, kBsThreadsWide>(32768));
     cache[c->device][ri][cl] = n;
     init[c->device][ri][cl] = true;
     return n;
@@ -626,12 +647,12 @@ static int bs_clusters_fit(hgb_ctx *c, int R, int cl) {
 // that, the largest of 8, 4, 2 that fits.  On GB300 (one CTA per SM) 15 clusters of 8 are
 // co-resident, so for 128 blocks a size between 9 and 16 that still fits 128 CTAs at once removes
 // the wait for a free cluster.
-static int bs_cluster_plan(hgb_ctx *c, int R, int nblk) {
+static int bs_cluster_plan(hgb_ctx *c, int nt, int nblk) {
     if (nblk < 2) return 1;
     for (int cl = std::min(kBsMaxCluster, nblk); cl > 1; cl--)
-        if ((long)bs_clusters_fit(c, R, cl) * cl >= nblk) return cl;
+        if ((long)bs_clusters_fit(c, nt, cl) * cl >= nblk) return cl;
     for (int cl = 8; cl > 1; cl /= 2)
-        if (bs_clusters_fit(c, R, cl) >= 1) return cl;
+        if (bs_clusters_fit(c, nt, cl) >= 1) return cl;
     return 1;
 }
 
@@ -652,26 +673,30 @@ static int upload(T **dst, const std::vector<T> &src) {
     return HGB_OK;
 }
 
-// Host-side analysis: blocks, local levels, steps and the packets (structure only; the values are
-// gathered on the device through map3 / dv_map / dv_row / ovf_map).
-int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
-                   int rev, int R, int xsize, BlockSolve &S) {
-    std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(std::max(n, 1));
-    HGB_CUDA(cudaMemcpyAsync(pntr.data(), pntr_d, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
-    if (nnz > 0)
-        HGB_CUDA(cudaMemcpyAsync(indx.data(), indx_d, sizeof(int) * nnz, cudaMemcpyDeviceToHost, c->stream));
-    if (n > 0) HGB_CUDA(cudaMemcpyAsync(diag.data(), diag_d, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
-    HGB_CUDA(cudaStreamSynchronize(c->stream));
+// The schedule on the host (structure only; the values are gathered on the device through map3 /
+// dv_map / dv_row / ovf_map), before its upload.
+struct BsPlan {
+    int n = 0, R = 0, nt = kBsThreads, cl = 1;
     std::vector<int4> blk, desc, pk0;
-    std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj;
-    std::vector<int> lev(R), cnt, start, cur, order;
+    std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj, push;
+};
+
+// Host-side analysis from host arrays: blocks, local levels, steps and the packets.  Pure host
+// work apart from the (cached) occupancy query of the cluster plan, so the lower and upper
+// schedules can be planned in parallel threads.
+static int bsolve_plan(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const int *diag, int lower,
+                       int rev, int R, int xsize, BsPlan &P) {
+    (void)nnz;
+    std::vector<int4> &blk = P.blk, &desc = P.desc, &pk0 = P.pk0;
+    std::vector<int> &map3 = P.map3, &dv_map = P.dv_map, &dv_row = P.dv_row, &ovf_codes = P.ovf_codes,
+                     &ovf_map = P.ovf_map, &rj = P.rj;
+    std::vector<int> lev, cnt, start, cur, order;
     auto row_of = [&](int pos) { return lower ? pos : n - 1 - pos; };
     auto pos_of = [&](int row) { return lower ? row : n - 1 - row; };
     auto deps = [&](int row, int &a, int &e) {
         a = lower ? pntr[row] : diag[row] + 1;
         e = lower ? diag[row] : pntr[row + 1];
     };
-    (void)xsize;   // the block layout is the same for every solution type
     // Blocks hold a whole multiple of the bandwidth (in solve order), so that every dependency
     // reaches at most one block back and block b+1 trails block b by a few steps.  Other sizes
     // break the wavefront: on the 96^3 7-point pattern (bandwidth 9216), 16384-row blocks put the
@@ -683,8 +708,17 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         deps(row, a, e);
         if (e > a) bw = std::max(bw, lower ? row - indx[a] : indx[e - 1] - row);
     }
-    if (bw >= 1 && bw <= R) R = R / bw * bw;
+    // FP32 / BF16 solutions of patterns with a wide wavefront (bandwidth of at least 4096 rows, two
+    // or more bands in 32768 rows) take the wide layout: 256 solver threads, blocks of 32768 rows
+    int NT = kBsThreads;
+    if (xsize == 4 && bw >= 4096 && bw <= 16384) {
+        NT = kBsThreadsWide;
+        R = 32768 / bw * bw;
+    } else if (bw >= 1 && bw <= R) {
+        R = R / bw * bw;
+    }
     const int Rmax = R;
+    lev.assign(R, 0);
     for (int p0 = 0; p0 < n;) {
         // grow the block in solve order while it fits R rows and kBsStepCap steps
         cnt.clear();
@@ -699,7 +733,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                 if (pj >= p0) lv = std::max(lv, lev[pj - p0] + 1);
             }
             if ((int)cnt.size() <= lv) cnt.resize(lv + 1, 0);
-            const int add = (cnt[lv] % kBsThreads == 0) ? 1 : 0;
+            const int add = (cnt[lv] % NT == 0) ? 1 : 0;
             if (steps + add > kBsStepCap) break;
             steps += add;
             cnt[lv]++;
@@ -714,8 +748,8 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
         for (int pos = p0; pos < p1; pos++) order[cur[lev[pos - p0]]++] = pos;
         const int s_first = (int)desc.size();
         for (int l = 0; l < nl; l++) {
-            for (int k = start[l]; k < start[l + 1]; k += kBsThreads) {
-                const int nr = std::min(kBsThreads, start[l + 1] - k);
+            for (int k = start[l]; k < start[l + 1]; k += NT) {
+                const int nr = std::min(NT, start[l + 1] - k);
                 int kx = 0;
                 for (int i = 0; i < nr; i++) {
                     int a, e;
@@ -727,7 +761,7 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     return fail(HGB_ERR_UNSUPPORTED, "block solve: packed arrays exceed 2^31 entries");
                 // a barrier ends every level, and every 16th step inside a long level, so that the
                 // solver threads' progress reaches the fetchers at least every 16 steps
-                const int bar = (k + nr == start[l + 1] || ((k - start[l]) / kBsThreads) % 16 == 15) ? 1 : 0;
+                const int bar = (k + nr == start[l + 1] || ((k - start[l]) / NT) % 16 == 15) ? 1 : 0;
                 desc.push_back(make_int4((int)pk0.size(), nr, (int)ob, kx | (bar << 16)));
                 ovf_codes.resize(ob + (size_t)kx * nr, 0);
                 ovf_map.resize(ob + (size_t)kx * nr, -1);
@@ -765,11 +799,12 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
     }
     // Push targets.  Blocks are grouped in runs of cl (one thread-block cluster each); inside a
     // run, the value that a row of block b+1 needs first from block b is offered by block b's CTA
-    // straight to block b+1's ring (consumer step << 7 | consumer thread).  A producer row offers
+    // straight to block b+1's ring (consumer step << 8 | consumer thread).  A producer row offers
     // to at most one consumer row.  Offered rows leave the fetchers' lists; an offer that is dropped
     // (the consumer more than a ring's length behind) is read from L2 by the consumer itself.
-    const int cl = bs_cluster_plan(c, R, (int)blk.size());
-    std::vector<int> push(pk0.size(), -1);
+    const int cl = bs_cluster_plan(c, NT, (int)blk.size());
+    std::vector<int> &push = P.push;
+    push.assign(pk0.size(), -1);
     if (cl > 1) {
         std::vector<int> pk_of_row(n, -1), blk_of_row(n, -1);
         for (int bb = 0; bb < (int)blk.size(); bb++)
@@ -788,34 +823,90 @@ int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *ind
                     if (j < 0 || blk_of_row[j] != bb - 1) continue;
                     const int pp = pk_of_row[j];
                     if (push[pp] < 0) {
-                        push[pp] = ((st - blk[bb].x) << 7) | t;
+                        push[pp] = ((st - blk[bb].x) << 8) | t;
                         rj[cp] = -1;
                     }
                 }
         }
     }
+    P.n = n;
+    P.R = Rmax;
+    P.nt = NT;
+    P.cl = cl;
+    return HGB_OK;
+}
+
+static int bsolve_upload(const BsPlan &P, BlockSolve &S) {
     S.release();
-    S.n = n;
-    S.nblk = (int)blk.size();
-    S.nsteps = (int)desc.size();
-    S.R = Rmax;
-    S.cl = cl;
-    S.npk = (long)pk0.size();
-    S.novf = (long)ovf_codes.size();
-    HGB_TRY(upload(&S.blk, blk));
-    HGB_TRY(upload(&S.desc, desc));
-    HGB_TRY(upload(&S.pk0, pk0));
-    HGB_TRY(upload(&S.rj, rj));
-    HGB_TRY(upload(&S.push, push));
-    HGB_TRY(upload(&S.map3, map3));
-    HGB_TRY(upload(&S.dv_map, dv_map));
-    HGB_TRY(upload(&S.dv_row, dv_row));
-    HGB_TRY(upload(&S.ovf_codes, ovf_codes));
-    HGB_TRY(upload(&S.ovf_map, ovf_map));
+    S.n = P.n;
+    S.nblk = (int)P.blk.size();
+    S.nsteps = (int)P.desc.size();
+    S.R = P.R;
+    S.nt = P.nt;
+    S.cl = P.cl;
+    S.npk = (long)P.pk0.size();
+    S.novf = (long)P.ovf_codes.size();
+    HGB_TRY(upload(&S.blk, P.blk));
+    HGB_TRY(upload(&S.desc, P.desc));
+    HGB_TRY(upload(&S.pk0, P.pk0));
+    HGB_TRY(upload(&S.rj, P.rj));
+    HGB_TRY(upload(&S.push, P.push));
+    HGB_TRY(upload(&S.map3, P.map3));
+    HGB_TRY(upload(&S.dv_map, P.dv_map));
+    HGB_TRY(upload(&S.dv_row, P.dv_row));
+    HGB_TRY(upload(&S.ovf_codes, P.ovf_codes));
+    HGB_TRY(upload(&S.ovf_map, P.ovf_map));
     HGB_CUDA(cudaMalloc(&S.ticket, sizeof(int) * 2));
     HGB_CUDA(cudaMemset(S.ticket, 0, sizeof(int) * 2));
     return HGB_OK;
 }
+
+int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
+                   int rev, int R, int xsize, BlockSolve &S) {
+    std::vector<int> pntr(n + 1), indx(std::max(nnz, 1)), diag(std::max(n, 1));
+    HGB_CUDA(cudaMemcpyAsync(pntr.data(), pntr_d, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (nnz > 0)
+        HGB_CUDA(cudaMemcpyAsync(indx.data(), indx_d, sizeof(int) * nnz, cudaMemcpyDeviceToHost, c->stream));
+    if (n > 0) HGB_CUDA(cudaMemcpyAsync(diag.data(), diag_d, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    HGB_CUDA(cudaStreamSynchronize(c->stream));
+    BsPlan P;
+    HGB_TRY(bsolve_plan(c, n, nnz, pntr.data(), indx.data(), diag.data(), lower, rev, R, xsize, P));
+    return bsolve_upload(P, S);
+}
+
+// The forward (lower, unit) and backward (upper) schedules of one factor from host arrays, planned
+// in two host threads; uploaded separately, so the planning can overlap other work.
+struct BsPlanPair {
+    BsPlan L, U;
+};
+
+int bsolve_plan_pair(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const int *diag, int R, int xsize,
+                     BsPlanPair **out) {
+    *out = nullptr;
+    BsPlanPair *P = new BsPlanPair();
+    int stU = HGB_OK;
+    std::string msgU;
+    std::thread tu([&] {
+        DeviceGuard g(c->device);
+        stU = bsolve_plan(c, n, nnz, pntr, indx, diag, 0, 0, R, xsize, P->U);
+        if (stU) msgU = hgb_last_error();   // the message is thread-local
+    });
+    const int stL = bsolve_plan(c, n, nnz, pntr, indx, diag, 1, 0, R, xsize, P->L);
+    tu.join();
+    if (stL || stU) {
+        delete P;
+        return stL ? stL : fail(stU, "%s", msgU.c_str());
+    }
+    *out = P;
+    return HGB_OK;
+}
+
+int bsolve_upload_pair(BsPlanPair *P, BlockSolve &SL, BlockSolve &SU) {
+    HGB_TRY(bsolve_upload(P->L, SL));
+    return bsolve_upload(P->U, SU);
+}
+
+void bsolve_plan_pair_free(BsPlanPair *P) { delete P; }
 
 // Gather the values (store precision vsize) and the diagonal terms into the packets.  With piv
 // (FP64 pivots of a lower-precision store) the packets carry the pivots' reciprocals.
@@ -844,31 +935,32 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
     return launch_check("bsolve_load_values");
 }
 
-template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
-static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
-    const size_t smem = bs_smem_bytes<V, X>(S.R);
-    // the attribute allows the largest block of the class (16384 FP64 / 32768 FP32 rows), so
-    // solves with smaller blocks launch too
-    const size_t smem_max = bs_smem_bytes<V, X>(sizeof(X) == 8 ? 16384 : 32768);
+template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
+static int bs_launch_nt(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
+    constexpr int CTA = bs_cta<NT>();
+    const size_t smem = bs_smem_bytes<V, X, NT>(S.R);
+    // the attribute allows the largest block of the layout (narrow: 16384 FP64 / 32768 FP32 rows,
+    // wide: 32768 rows), so solves with smaller blocks launch too
+    const size_t smem_max = bs_smem_bytes<V, X, NT>((sizeof(X) == 8 && NT == kBsThreads) ? 16384 : 32768);
     static int attr_dev = -1;   // device on which the kernel's shared-memory attribute was set
     if (attr_dev != c->device) {
         int mx = 0;
         HGB_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
         if (smem_max > (size_t)mx)
             return fail(HGB_ERR_UNSUPPORTED, "bsolve: %zu bytes of shared memory (max %d)", smem_max, mx);
-        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem_max));
+        HGB_CUDA(cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP, NT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
         // clusters above 8 CTAs are planned only where the occupancy query accepted them with this
         // attribute set; a refusal here leaves the portable sizes working
-        if (cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP>, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                                 1) != cudaSuccess)
+        if (cudaFuncSetAttribute(bsolve_kernel<V, X, MODE, UNIT, RECIP, NT>,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
             cudaGetLastError();
         attr_dev = c->device;
     }
     if (smem > smem_max) return fail(HGB_ERR_UNSUPPORTED, "bsolve: %d rows per block", S.R);
     if (S.cl <= 1) {
         const int grid = std::max(1, std::min(S.nblk, c->num_sms));
-        bsolve_kernel<V, X, MODE, UNIT, RECIP><<<grid, kBsCta, smem, c->stream>>>(A, alpha, in, out, pend);
+        bsolve_kernel<V, X, MODE, UNIT, RECIP, NT><<<grid, CTA, smem, c->stream>>>(A, alpha, in, out, pend);
         return launch_check("bsolve_kernel");
     }
     // thread-block clusters of S.cl CTAs (the push targets were planned for that size); as many
@@ -884,7 +976,7 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
     at[0].val.clusterDim.x = S.cl;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(kBsCta);
+    cfg.blockDim = dim3(CTA);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = c->stream;
     cfg.attrs = at;
@@ -894,14 +986,25 @@ static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alp
         if (k.dev == c->device && k.cl == S.cl && k.smem == smem) clusters_max = k.n;
     if (clusters_max == 0) {
         cfg.gridDim = dim3(S.cl * 16);
-        HGB_CUDA(cudaOccupancyMaxActiveClusters(&clusters_max, bsolve_kernel<V, X, MODE, UNIT, RECIP>, &cfg));
+        HGB_CUDA(cudaOccupancyMaxActiveClusters(&clusters_max, bsolve_kernel<V, X, MODE, UNIT, RECIP, NT>, &cfg));
         if (clusters_max < 1) return fail(HGB_ERR_UNSUPPORTED, "bsolve: no cluster of %d CTAs fits", S.cl);
         fit_cache.push_back(FitKey{c->device, S.cl, smem, clusters_max});
     }
     const int runs = (S.nblk + S.cl - 1) / S.cl;
     cfg.gridDim = dim3(S.cl * std::max(1, std::min(runs, clusters_max)));
-    HGB_CUDA(cudaLaunchKernelEx(&cfg, bsolve_kernel<V, X, MODE, UNIT, RECIP>, A, alpha, in, out, pend));
+    HGB_CUDA(cudaLaunchKernelEx(&cfg, bsolve_kernel<V, X, MODE, UNIT, RECIP, NT>, A, alpha, in, out, pend));
     return launch_check("bsolve_kernel");
+}
+
+// the schedule's layout: 128 solver threads, or 256 for FP32 / BF16 solutions of the wide layout
+template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
+static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
+    if (S.nt == kBsThreads) return bs_launch_nt<V, X, MODE, UNIT, RECIP, kBsThreads>(c, S, A, alpha, in, out, pend);
+    if constexpr (sizeof(X) == 4) {
+        if (S.nt == kBsThreadsWide)
+            return bs_launch_nt<V, X, MODE, UNIT, RECIP, kBsThreadsWide>(c, S, A, alpha, in, out, pend);
+    }
+    return fail(HGB_ERR_ARG, "bsolve: a schedule of %d threads for a %d-byte solution", S.nt, (int)sizeof(X));
 }
 
 template <typename V, typename X>

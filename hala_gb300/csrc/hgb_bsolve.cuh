@@ -16,6 +16,7 @@ struct BlockSolve {
     int *rj = nullptr;          // [npk] first dependency of the row on an earlier block (fetched), or -1
     int *push = nullptr;        // [npk] where the row's value goes in the next block's ring, or -1
     int cl = 1;                 // CTAs per thread-block cluster the push targets assume
+    int nt = 128;               // solver threads per CTA (rows per step) the schedule was cut for
     int *ovf_codes = nullptr;   // [novf] dependencies beyond the third, column-major per step
     void *ovf_vals = nullptr;
     int *map3 = nullptr, *dv_map = nullptr, *dv_row = nullptr, *ovf_map = nullptr;   // value gather maps
@@ -29,6 +30,13 @@ int bsolve_rows(hgb_ctx *c, int xsize, int n);
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
                    int rev, int R, int xsize, BlockSolve &S);
+// the lower (unit) and upper schedules of an ILU factor planned from HOST copies of the pattern and
+// the diagonal index (two host threads), then uploaded
+struct BsPlanPair;
+int bsolve_plan_pair(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const int *diag, int R, int xsize,
+                     BsPlanPair **out);
+int bsolve_upload_pair(BsPlanPair *P, BlockSolve &SL, BlockSolve &SU);
+void bsolve_plan_pair_free(BsPlanPair *P);
 int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, const double *piv);
 template <typename V, typename X>
 int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,

@@ -34,6 +34,16 @@ int cuda_fail(cudaError_t e, const char *what) {
                 cudaGetErrorString(e));
 }
 
+int h2d_chunked(hgb_ctx *c, cudaStream_t s, void *dst, const void *src, size_t bytes) {
+    (void)c;
+    constexpr size_t kChunk = (size_t)16 << 20;
+    for (size_t o = 0; o < bytes; o += kChunk) {
+        const size_t b = std::min(kChunk, bytes - o);
+        HGB_CUDA(cudaMemcpyAsync((char *)dst + o, (const char *)src + o, b, cudaMemcpyHostToDevice, s));
+    }
+    return HGB_OK;
+}
+
 int dev_error_to_status(int w) {
     if (w & DEV_ERR_TIMEOUT) return HGB_ERR_TIMEOUT;
     if (w & DEV_ERR_CSR) return HGB_ERR_CSR;
@@ -226,6 +236,7 @@ int hgb_ctx_create(int device, hgb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->scal, sizeof(SolverScalars));
     if (e == cudaSuccess) e = cudaMallocHost(&c->host_result, sizeof(double) * 64);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->worker, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e == cudaSuccess) {
@@ -261,6 +272,7 @@ int hgb_ctx_destroy(hgb_ctx *c) {
     cudaFreeHost(c->host_result);
     cudaFree(c->arena);
     if (c->worker) cudaStreamDestroy(c->worker);
+    if (c->copy) cudaStreamDestroy(c->copy);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
     if (c->pool) cudaMemPoolDestroy(c->pool);   // released once the last stream-ordered free has run

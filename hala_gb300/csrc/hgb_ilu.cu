@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace hgb {
@@ -484,6 +485,9 @@ struct hgb_ilu {
     // block-local level schedules (hgb_bsolve.cu); the global-level kernel is the fallback
     bool use_bs = false, use_bsT = false;
     BlockSolve BL, BU, BLT, BUT;
+    // host-buffer creation: the object owns its device copies of the pattern and the values
+    int *own_pntr = nullptr, *own_indx = nullptr;
+    void *own_vals = nullptr;
 };
 
 namespace hgb {
@@ -511,6 +515,9 @@ static void ilu_free(hgb_ilu *M) {
     M->BU.release();
     M->BLT.release();
     M->BUT.release();
+    cudaFree(M->own_pntr);
+    cudaFree(M->own_indx);
+    cudaFree(M->own_vals);
     delete M;
 }
 
@@ -636,18 +643,21 @@ struct hgb_tri {
 
 extern "C" {
 
-int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const void *vals,
-                    hgb_dtype vals_dtype, hgb_dtype store, char policy, hgb_ilu **out) {
-    (void)policy;
-    if (!out) return fail(HGB_ERR_ARG, "ilu0_create: null output");
-    *out = nullptr;
+static int ilu_check_args(hgb_ctx *c, int n, int nnz, const void *pntr, const void *indx, const void *vals,
+                          hgb_dtype vals_dtype, hgb_dtype store) {
     if (!c || n <= 0 || nnz < n || !pntr || !indx || !vals) return fail(HGB_ERR_ARG, "ilu0_create: bad arguments (n=%d nnz=%d)", n, nnz);
     if (vals_dtype != HGB_F64 && vals_dtype != HGB_F32) return fail(HGB_ERR_ARG, "ilu0_create: vals dtype must be F64 or F32");
     if (store != HGB_F64 && store != HGB_F32 && store != HGB_BF16) return fail(HGB_ERR_ARG, "ilu0_create: store dtype");
     if (vals_dtype == HGB_F32 && store != HGB_F32) return fail(HGB_ERR_UNSUPPORTED, "ilu0_create: an F32 factor is stored as F32");
-    DeviceGuard g(c->device);
+    return HGB_OK;
+}
+
+// The device part of ILU(0) creation.  plan: when given, the block-solve schedules were planned on
+// the host already (from host arrays); otherwise they are planned here from D2H copies.
+static int ilu_create_device(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const void *vals,
+                             hgb_dtype vals_dtype, hgb_dtype store, hgb_ilu *M, int *zero_pivot_out,
+                             BsPlanPair *plan) {
     HGB_TRY(csr_check(c, n, n, nnz, pntr, indx));
-    hgb_ilu *M = new hgb_ilu();
     M->ctx = c;
     M->n = n;
     M->nnz = nnz;
@@ -690,9 +700,23 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
         }
         if (cudaMalloc(&M->tmp, xsize(store) * n) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
         {   // block-local schedules; patterns they cannot hold fall back to the global-level solve
-            const int R = bsolve_rows(c, (int)xsize(store), n);
-            int bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 1, 0, R, (int)xsize(store), M->BL);
-            if (!bs) bs = bsolve_analyse(c, n, nnz, pntr, indx, M->diag, 0, 0, R, (int)xsize(store), M->BU);
+            int bs = HGB_OK;
+            BsPlanPair *own = nullptr;
+            if (!plan) {   // planned here, from host copies of the pattern
+                const int R = bsolve_rows(c, (int)xsize(store), n);
+                std::vector<int> hp(n + 1), hi(nnz), hd(n);
+                if (cudaMemcpyAsync(hp.data(), pntr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                    cudaMemcpyAsync(hi.data(), indx, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                    cudaMemcpyAsync(hd.data(), M->diag, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                    cudaStreamSynchronize(c->stream) != cudaSuccess) {
+                    st = cuda_fail(cudaGetLastError(), "ilu0_create");
+                    break;
+                }
+                bs = bsolve_plan_pair(c, n, nnz, hp.data(), hi.data(), hd.data(), R, (int)xsize(store), &own);
+                plan = own;
+            }
+            if (!bs) bs = bsolve_upload_pair(plan, M->BL, M->BU);
+            bsolve_plan_pair_free(own);
             if (!bs) bs = bsolve_load_values(c, M->BL, M->svals, (int)vsize(store), nullptr);
             if (!bs) bs = bsolve_load_values(c, M->BU, M->svals, (int)vsize(store), M->piv);
             if (bs == HGB_OK) M->use_bs = true;
@@ -700,6 +724,93 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
         }
         if (cudaStreamSynchronize(c->stream) != cudaSuccess) { st = cuda_fail(cudaGetLastError(), "ilu0_create"); break; }
     } while (0);
+    if (zero_pivot_out) *zero_pivot_out = zero_pivot;
+    return st;
+}
+
+int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const void *vals,
+                    hgb_dtype vals_dtype, hgb_dtype store, char policy, hgb_ilu **out) {
+    (void)policy;
+    if (!out) return fail(HGB_ERR_ARG, "ilu0_create: null output");
+    *out = nullptr;
+    HGB_TRY(ilu_check_args(c, n, nnz, pntr, indx, vals, vals_dtype, store));
+    DeviceGuard g(c->device);
+    hgb_ilu *M = new hgb_ilu();
+    int zero_pivot = 0;
+    const int st = ilu_create_device(c, n, nnz, pntr, indx, vals, vals_dtype, store, M, &zero_pivot, nullptr);
+    if (st) {
+        ilu_free(M);
+        return st;
+    }
+    *out = M;
+    if (zero_pivot) return fail(HGB_ERR_ZERO_PIVOT, "ILU(0) met an exactly zero pivot");
+    return HGB_OK;
+}
+
+// Host-side structure check and diagonal index of a host CSR (the host planning reads the arrays
+// directly, so they are validated first): pntr monotone from 0 to nnz, columns in range and strictly
+// increasing in each row, every diagonal present.
+static int host_csr_diag(int n, int nnz, const int *pntr, const int *indx, std::vector<int> &diag) {
+    if (pntr[0] != 0 || pntr[n] != nnz) return fail(HGB_ERR_CSR, "ilu0_create_host: pntr[0] = %d, pntr[n] = %d (nnz %d)", pntr[0], pntr[n], nnz);
+    diag.assign(n, -1);
+    for (int i = 0; i < n; i++) {
+        const int a = pntr[i], e = pntr[i + 1];
+        if (e < a || e > nnz) return fail(HGB_ERR_CSR, "ilu0_create_host: row %d has pntr %d..%d", i, a, e);
+        int prev = -1;
+        for (int q = a; q < e; q++) {
+            const int col = indx[q];
+            if (col <= prev || col >= n) return fail(HGB_ERR_CSR, "ilu0_create_host: row %d column %d", i, col);
+            if (col == i) diag[i] = q;
+            prev = col;
+        }
+        if (diag[i] < 0) return fail(HGB_ERR_CSR, "ilu0_create_host: row %d has no diagonal entry", i);
+    }
+    return HGB_OK;
+}
+
+int hgb_ilu0_create_host(hgb_ctx *c, int n, int nnz, const int *pntr_h, const int *indx_h, const void *vals_h,
+                         hgb_dtype vals_dtype, hgb_dtype store, char policy, hgb_ilu **out) {
+    (void)policy;
+    if (!out) return fail(HGB_ERR_ARG, "ilu0_create_host: null output");
+    *out = nullptr;
+    HGB_TRY(ilu_check_args(c, n, nnz, pntr_h, indx_h, vals_h, vals_dtype, store));
+    DeviceGuard g(c->device);
+    std::vector<int> diag;
+    HGB_TRY(host_csr_diag(n, nnz, pntr_h, indx_h, diag));
+    hgb_ilu *M = new hgb_ilu();
+    const size_t vs = vsize(vals_dtype);
+    if (cudaMalloc(&M->own_pntr, sizeof(int) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&M->own_indx, sizeof(int) * (size_t)nnz) != cudaSuccess ||
+        cudaMalloc(&M->own_vals, vs * (size_t)nnz) != cudaSuccess) {
+        const int st = cuda_fail(cudaGetLastError(), "ilu0_create_host");
+        ilu_free(M);
+        return st;
+    }
+    // the pattern and the values go to the device on the context's copy stream, from a helper
+    // thread (pageable sources make cudaMemcpyAsync wait on the host), while this thread plans the
+    // triangular schedules from the host arrays
+    int copy_status = HGB_OK;
+    std::string copy_msg;
+    std::thread copier([&] {
+        DeviceGuard gc(c->device);
+        copy_status = h2d_chunked(c, c->copy, M->own_pntr, pntr_h, sizeof(int) * (n + 1));
+        if (!copy_status) copy_status = h2d_chunked(c, c->copy, M->own_indx, indx_h, sizeof(int) * (size_t)nnz);
+        if (!copy_status) copy_status = h2d_chunked(c, c->copy, M->own_vals, vals_h, vs * (size_t)nnz);
+        if (!copy_status && cudaStreamSynchronize(c->copy) != cudaSuccess)
+            copy_status = cuda_fail(cudaGetLastError(), "ilu0_create_host copy");
+        if (copy_status) copy_msg = hgb_last_error();
+    });
+    BsPlanPair *plan = nullptr;
+    const int pst = bsolve_plan_pair(c, n, nnz, pntr_h, indx_h, diag.data(), bsolve_rows(c, (int)xsize(store), n),
+                                     (int)xsize(store), &plan);
+    copier.join();
+    int st = copy_status ? fail(copy_status, "%s", copy_msg.c_str()) : HGB_OK;
+    int zero_pivot = 0;
+    // a pattern the block solve cannot hold leaves plan null: the device path plans (and falls back) itself
+    if (!st && pst && pst != HGB_ERR_UNSUPPORTED) st = pst;
+    if (!st) st = ilu_create_device(c, n, nnz, M->own_pntr, M->own_indx, M->own_vals, vals_dtype, store, M, &zero_pivot,
+                                    plan);
+    bsolve_plan_pair_free(plan);
     if (st) {
         ilu_free(M);
         return st;

@@ -73,6 +73,7 @@ struct hgb_ctx {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaMemPool_t pool = nullptr;          // solver workspaces: stream-ordered, memory kept between solves
     int spmv_mode = HGB_SPMV_FUSED;        // arithmetic of the 'N' products (hgb_ctx_set_spmv_mode)
+    cudaStream_t copy = nullptr;           // host-to-device transfers of the host-buffer entries
 };
 
 namespace hgb {
@@ -103,6 +104,10 @@ struct DeviceGuard {
 
 // read and clear the device error word (synchronises the stream)
 int collect_dev_error(hgb_ctx *ctx);
+
+// host -> device in chunks (one cudaMemcpyAsync per chunk) on stream s; a pageable source is staged
+// by the driver chunk by chunk, so the first chunks move while later ones are still being read
+int h2d_chunked(hgb_ctx *ctx, cudaStream_t s, void *dst, const void *src, size_t bytes);
 
 // Graph capture is not possible on the legacy NULL stream.  For the duration of a fused solve the
 // context's work moves to its private non-blocking stream, ordered after the caller's prior work

@@ -581,7 +581,7 @@ extern "C" int hgb_ru_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_il
 // operation for operation (explicitly rounded, no contraction); the inner products are parallel.
 namespace hgb {
 
-constexpr int kGmresMaxRestart = 64;
+constexpr int kGmresMaxRestart = 512;   // the Hessenberg factor (1 MB) lives in device memory
 
 struct GmresState {
     // header (read by the host after every cycle)
@@ -690,7 +690,8 @@ __global__ void gm_scale_kernel(long n, const GmresState *__restrict__ st, X *__
     }
 }
 
-// cf[0..k] = W[:, 0..k]^T r   (krylov_project's gemv 'T', :67-70)
+// cf[0..k] = W[:, 0..k]^T r   (krylov_project's gemv 'T', :67-70), for the k1 columns from W and cf
+// on (one group of up to 64 columns per launch)
 template <typename X, int KMAX>
 __global__ void gm_dots_kernel(long n, int k1, const GmresState *__restrict__ st, const X *__restrict__ W,
                                const X *__restrict__ r, double *cf, double *partials, unsigned *counter) {
@@ -724,13 +725,18 @@ __global__ void gm_update_kernel(long n, int k, GmresState *st, const X *__restr
     }
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
         const double nrm = __dsqrt_rn(v[0]);
-        double h[kGmresMaxRestart + 1];
-        for (int j = 0; j <= k; j++) h[j] = cf[j];
-        for (int i = 0; i < k; i++) gm_rot(h[i], h[i + 1], st->C[i], st->S[i]);
-        double beta = nrm, ic, is;
-        gm_rotg(h[k], beta, ic, is);
+        // the previous rotations applied to the new column in order, carrying h[i + 1] in a register
         double *Hk = st->H + (long)k * (k + 1) / 2;
-        for (int j = 0; j <= k; j++) Hk[j] = h[j];
+        double hi = cf[0];
+        for (int i = 0; i < k; i++) {
+            double hn = cf[i + 1];
+            gm_rot(hi, hn, st->C[i], st->S[i]);
+            Hk[i] = hi;
+            hi = hn;
+        }
+        double beta = nrm, ic, is;
+        gm_rotg(hi, beta, ic, is);
+        Hk[k] = hi;
         st->S[k] = is;
         st->C[k] = ic;
         const double res = fabs(__dmul_rn(is, st->Z[k]));
@@ -787,11 +793,17 @@ __global__ void gm_xupdate_kernel(long n, const GmresState *__restrict__ st, con
 template <typename X>
 static int gm_dots_launch(hgb_ctx *c, long n, int k1, const GmresState *st, const X *W, const X *r, double *cf) {
     const int grid = reduce_grid(c, n, 256 * 8);
-    if (k1 <= 8) gm_dots_kernel<X, 8><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
-    else if (k1 <= 16) gm_dots_kernel<X, 16><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
-    else if (k1 <= 32) gm_dots_kernel<X, 32><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
-    else gm_dots_kernel<X, 64><<<grid, 256, 0, c->stream>>>(n, k1, st, W, r, cf, c->partials, c->counter);
-    return launch_check("gm_dots_kernel");
+    for (int j0 = 0; j0 < k1; j0 += 64) {   // groups of up to 64 columns, one grid reduction each
+        const int kk = std::min(64, k1 - j0);
+        const X *Wj = W + (long)j0 * n;
+        double *cj = cf + j0;
+        if (kk <= 8) gm_dots_kernel<X, 8><<<grid, 256, 0, c->stream>>>(n, kk, st, Wj, r, cj, c->partials, c->counter);
+        else if (kk <= 16) gm_dots_kernel<X, 16><<<grid, 256, 0, c->stream>>>(n, kk, st, Wj, r, cj, c->partials, c->counter);
+        else if (kk <= 32) gm_dots_kernel<X, 32><<<grid, 256, 0, c->stream>>>(n, kk, st, Wj, r, cj, c->partials, c->counter);
+        else gm_dots_kernel<X, 64><<<grid, 256, 0, c->stream>>>(n, kk, st, Wj, r, cj, c->partials, c->counter);
+        HGB_TRY(launch_check("gm_dots_kernel"));
+    }
+    return HGB_OK;
 }
 
 // Runs restarted GMRES on (A, M) for b -> x (x holds the initial guess).  tol: absolute threshold
@@ -993,11 +1005,17 @@ extern "C" int hgb_mixed_cg_solve(hgb_ctx *c, int n, int nnz, const int *pntr_h,
     char *base = (char *)c->arena;
     int *dp = (int *)(base + op), *di = (int *)(base + oi);
     double *dv = (double *)(base + ov), *db = (double *)(base + ob), *dx = (double *)(base + ox);
-    HGB_CUDA(cudaMemcpyAsync(dp, pntr_h, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(di, indx_h, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(dv, vals_h, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(db, b_h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(dx, x_h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    // the loads (gpu_engine::load, wax/hala_lib_extensions.hpp:137-146) in chunks on the copy stream,
+    // ordered after the caller's earlier work on the context's stream and before the solve
+    HGB_CUDA(cudaEventRecord(c->ev_in, c->stream));
+    HGB_CUDA(cudaStreamWaitEvent(c->copy, c->ev_in, 0));
+    HGB_TRY(h2d_chunked(c, c->copy, dp, pntr_h, sizeof(int) * (n + 1)));
+    HGB_TRY(h2d_chunked(c, c->copy, di, indx_h, sizeof(int) * (size_t)nnz));
+    HGB_TRY(h2d_chunked(c, c->copy, dv, vals_h, sizeof(double) * (size_t)nnz));
+    HGB_TRY(h2d_chunked(c, c->copy, db, b_h, sizeof(double) * n));
+    HGB_TRY(h2d_chunked(c, c->copy, dx, x_h, sizeof(double) * n));
+    HGB_CUDA(cudaEventRecord(c->ev_out, c->copy));
+    HGB_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0));
     hgb_csr *A = nullptr;
     HGB_TRY(hgb_csr_create(c, n, n, nnz, dp, di, dv, HGB_F64, &A));
     int st = hgb_cg_solve(c, A, M, db, dx, tol, max_iter, info);
@@ -1049,14 +1067,27 @@ static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const 
     int *dp = (int *)(base + op), *di = (int *)(base + oi);
     double *dv = (double *)(base + ov), *db = (double *)(base + ob), *dx = (double *)(base + ox);
     void *dw = base + ow;
-    HGB_CUDA(cudaMemcpyAsync(dp, pntr_h, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(di, indx_h, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(dv, vals_h, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(db, b_h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    HGB_CUDA(cudaMemcpyAsync(dx, x_h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    f64_to_inner_kernel<<<ew_grid(c, nnz), 256, 0, c->stream>>>(nnz, dv, bf16 ? nullptr : (float *)dw,
-                                                                bf16 ? (uint16_t *)dw : nullptr);
-    HGB_TRY(launch_check("f64_to_inner_kernel"));
+    // The loads in chunks on the copy stream, overlapped with the conversion of the values to the
+    // inner precision on the context's stream: each chunk of values is converted as soon as it has
+    // landed, while the next chunks are in flight.
+    HGB_CUDA(cudaEventRecord(c->ev_in, c->stream));
+    HGB_CUDA(cudaStreamWaitEvent(c->copy, c->ev_in, 0));
+    HGB_TRY(h2d_chunked(c, c->copy, dp, pntr_h, sizeof(int) * (n + 1)));
+    HGB_TRY(h2d_chunked(c, c->copy, di, indx_h, sizeof(int) * (size_t)nnz));
+    constexpr long kChunk = 1L << 21;   // values per conversion chunk (16 MB of FP64)
+    for (long o = 0; o < nnz; o += kChunk) {
+        const long m = std::min(kChunk, (long)nnz - o);
+        HGB_TRY(h2d_chunked(c, c->copy, dv + o, vals_h + o, sizeof(double) * (size_t)m));
+        HGB_CUDA(cudaEventRecord(c->ev_out, c->copy));
+        HGB_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0));   // waits on this record, not later ones
+        f64_to_inner_kernel<<<ew_grid(c, m), 256, 0, c->stream>>>(
+            m, dv + o, bf16 ? nullptr : (float *)dw + o, bf16 ? (uint16_t *)dw + o : nullptr);
+        HGB_TRY(launch_check("f64_to_inner_kernel"));
+    }
+    HGB_TRY(h2d_chunked(c, c->copy, db, b_h, sizeof(double) * n));
+    HGB_TRY(h2d_chunked(c, c->copy, dx, x_h, sizeof(double) * n));
+    HGB_CUDA(cudaEventRecord(c->ev_out, c->copy));
+    HGB_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0));
     hgb_csr *A64 = nullptr, *Ai = nullptr;
     HGB_TRY(hgb_csr_create(c, n, n, nnz, dp, di, dv, HGB_F64, &A64));
     int st = hgb_csr_create(c, n, n, nnz, dp, di, dw, bf16 ? HGB_BF16 : HGB_F32, &Ai);

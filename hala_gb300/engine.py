@@ -143,6 +143,37 @@ def get_diagonal_index(engine, pntr, indx):
     return diag
 
 
+def split_pattern(engine, pntr, indx, diag):
+    """split_pattern (sparse/hala_sparse_core.hpp:72-94) on the device: the upper and lower CSR
+    patterns, the diagonal in both.  Returns (upper_pntr, upper_indx, lower_pntr, lower_indx)."""
+    _need(pntr, torch.int32, "pntr"); _need(indx, torch.int32, "indx"); _need(diag, torch.int32, "diag")
+    n = pntr.numel() - 1
+    up = torch.empty(n + 1, dtype=torch.int32, device=pntr.device)
+    lp = torch.empty(n + 1, dtype=torch.int32, device=pntr.device)
+    nu, nl = C.c_int(), C.c_int()
+    check(_h.lib().hgb_split_pattern_pntr(engine.h, n, _p(pntr), _p(diag), _p(up), _p(lp), C.byref(nu), C.byref(nl)),
+          "split_pattern")
+    ui = torch.empty(max(nu.value, 1), dtype=torch.int32, device=pntr.device)[:nu.value]
+    li = torch.empty(max(nl.value, 1), dtype=torch.int32, device=pntr.device)[:nl.value]
+    check(_h.lib().hgb_split_pattern_indx(engine.h, n, _p(pntr), _p(indx), _p(diag), _p(up), _p(lp), _p(ui), _p(li)),
+          "split_pattern")
+    return up, ui, lp, li
+
+
+def split_values(engine, uplo, diag, pntr, vals, upper_pntr, lower_pntr):
+    """split_values (sparse/hala_sparse_core.hpp:97-120) on the device.  Returns (upper_vals,
+    lower_vals); the diagonal of the triangle uplo does not select is 0 (diag 'N') or 1 ('U')."""
+    _need(pntr, torch.int32, "pntr"); _need(vals, name="vals")
+    n = pntr.numel() - 1
+    nu, nl = int(upper_pntr[-1]), int(lower_pntr[-1])
+    uv = torch.empty(max(nu, 1), dtype=vals.dtype, device=vals.device)[:nu]
+    lv = torch.empty(max(nl, 1), dtype=vals.dtype, device=vals.device)[:nl]
+    check(getattr(_h.lib(), f"hgb_split_values_{_sfx(vals)}")(engine.h, ch_(uplo), ch_(diag), n, _p(pntr), _p(vals),
+                                                               _p(upper_pntr), _p(lower_pntr), _p(uv), _p(lv)),
+          "split_values")
+    return uv, lv
+
+
 # ------------------------------------------------------------------------- sparse ------
 def sparse_gemv(engine, trans, M, N, alpha, pntr, indx, vals, x, beta, y):
     """sparse_gemv(gpu_engine, trans, M, N, alpha, pntr, indx, vals, x, beta, y),
@@ -265,6 +296,38 @@ class gpu_ilu:
 
 def make_ilu(engine, pntr, indx, vals, policy="N", store=None):
     return gpu_ilu(engine, pntr, indx, vals, policy, store)
+
+
+class mixed_ilu(gpu_ilu):
+    """make_ilu(mixed_engine, pntr, indx, vals, policy), wax/hala_lib_extensions.hpp:311-366: HOST
+    (numpy) pattern and values; the handle owns their device copies, which travel while the host
+    plans the triangular schedules (hgb_ilu0_create_host)."""
+
+    def __init__(self, engine, pntr_h, indx_h, vals_h, policy="N", store=None):
+        import numpy as np
+        pntr_h = np.ascontiguousarray(pntr_h, dtype=np.int32)
+        indx_h = np.ascontiguousarray(indx_h, dtype=np.int32)
+        vdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32}[vals_h.dtype]
+        vals_h = np.ascontiguousarray(vals_h)
+        store = vdt if store is None else store
+        self.engine = engine
+        self.n = len(pntr_h) - 1
+        self.nnz = len(indx_h)
+        self.store = store
+        self.fdtype = vdt
+        self._keep = ()
+        h = C.c_void_p()
+        st = _h.lib().hgb_ilu0_create_host(engine.h, self.n, self.nnz, pntr_h.ctypes.data_as(C.c_void_p),
+                                           indx_h.ctypes.data_as(C.c_void_p), vals_h.ctypes.data_as(C.c_void_p),
+                                           _DT[vdt], _DT[store], ch_(policy), C.byref(h))
+        self.h = h if h.value else None
+        self.zero_pivot = (st == _h.HGB_ERR_ZERO_PIVOT)
+        if st not in (_h.HGB_OK, _h.HGB_ERR_ZERO_PIVOT):
+            check(st, "make_ilu(mixed_engine)")
+
+
+def make_ilu_host(engine, pntr_h, indx_h, vals_h, policy="N", store=None):
+    return mixed_ilu(engine, pntr_h, indx_h, vals_h, policy, store)
 
 
 def ilu_apply(ilu, x, r, num_rhs=1):

@@ -57,6 +57,11 @@ _SIGS = {
     "hgb_copy_f64": ([vp, i32, vp, vp], i32),
     "hgb_copy_f32": ([vp, i32, vp, vp], i32),
     "hgb_set_zero": ([vp, C.c_size_t, vp], i32),
+    "hgb_split_pattern_pntr": ([vp, i32, vp, vp, vp, vp, C.POINTER(i32), C.POINTER(i32)], i32),
+    "hgb_split_pattern_indx": ([vp, i32, vp, vp, vp, vp, vp, vp, vp], i32),
+    "hgb_split_values_f64": ([vp, ch, ch, i32, vp, vp, vp, vp, vp, vp], i32),
+    "hgb_split_values_f32": ([vp, ch, ch, i32, vp, vp, vp, vp, vp, vp], i32),
+    "hgb_ilu0_create_host": ([vp, i32, i32, vp, vp, vp, i32, i32, ch, C.POINTER(vp)], i32),
     "hgb_gemv_f64": ([vp, ch, i32, i32, f64, vp, vp, f64, vp], i32),
     "hgb_gemv_f32": ([vp, ch, i32, i32, f32, vp, vp, f32, vp], i32),
     "hgb_dgmm_f64": ([vp, ch, i32, i32, vp, vp, vp], i32),

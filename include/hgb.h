@@ -153,6 +153,22 @@ int hgb_csr_destroy(hgb_csr *A);
 /* get_diagonal_index, sparse/hala_sparse_core.hpp:45-60; HGB_ERR_CSR if a diagonal is missing */
 int hgb_diag_index(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx, int *diag);
 
+/* split_pattern (sparse/hala_sparse_core.hpp:72-94) in the two passes of split_pattern_array
+ * (sparse/hala_sparse_utils.hpp:176-193).  Row i of the lower pattern is [pntr_i, diag_i], of the
+ * upper [diag_i, pntr_{i+1}): the diagonal is in both.  First pass: upper_pntr[n+1], lower_pntr[n+1]
+ * (device) and the two entry counts (host, synchronises), so the caller can size the index arrays;
+ * HGB_ERR_CSR if a diag_i lies outside its row.  Second pass: the column indices. */
+int hgb_split_pattern_pntr(hgb_ctx *ctx, int n, const int *pntr, const int *diag, int *upper_pntr,
+                           int *lower_pntr, int *upper_nnz_host, int *lower_nnz_host);
+int hgb_split_pattern_indx(hgb_ctx *ctx, int n, const int *pntr, const int *indx, const int *diag,
+                           const int *upper_pntr, const int *lower_pntr, int *upper_indx, int *lower_indx);
+/* split_values (core:97-120, split_values_array utils:201-221): each triangle's values; the diagonal
+ * of the triangle uplo does NOT select is set to 0 (diag 'N') or 1 (diag 'U'). */
+int hgb_split_values_f64(hgb_ctx *ctx, char uplo, char diag, int n, const int *pntr, const double *vals,
+                         const int *upper_pntr, const int *lower_pntr, double *upper_vals, double *lower_vals);
+int hgb_split_values_f32(hgb_ctx *ctx, char uplo, char diag, int n, const int *pntr, const float *vals,
+                         const int *upper_pntr, const int *lower_pntr, float *upper_vals, float *lower_vals);
+
 /* ------------------------------------------------ ILU(0) (gpu_ilu, gpu_ilu.hpp:45-185) ----- */
 /* make_ilu(gpu_engine, pntr, indx, vals, policy), gpu_ilu.hpp:54-109,192.
  * Factorises a copy of vals (the pattern is aliased, as in the reference) with the row-wise IKJ
@@ -166,6 +182,14 @@ int hgb_diag_index(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *ind
 int hgb_ilu0_create(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx,
                     const void *vals, hgb_dtype vals_dtype, hgb_dtype store, char policy,
                     hgb_ilu **ilu);
+/* make_ilu(mixed_engine, pntr, indx, vals, policy), wax/hala_lib_extensions.hpp:311-366 (mixed_ilu):
+ * HOST pattern and values.  The handle owns device copies of them.  The copies go to the device in
+ * chunks on the context's copy stream, from a helper thread, while the calling thread checks the
+ * pattern and plans the triangular schedules from the host arrays; the factorisation follows as in
+ * hgb_ilu0_create.  HGB_ERR_CSR for a malformed host pattern (checked before any copy). */
+int hgb_ilu0_create_host(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const int *indx_host,
+                         const void *vals_host, hgb_dtype vals_dtype, hgb_dtype store, char policy,
+                         hgb_ilu **ilu);
 /* gpu_ilu::apply(x, r), gpu_ilu.hpp:150-164: r = U^-1 L^-1 x (trans 'N'), the arithmetic of
  * apply_ilu_array (utils:263-276); trans 'T': r = (LU)^-T x (adjoint).  x and r may alias. */
 int hgb_ilu0_apply(hgb_ilu *ilu, char trans, const void *x, void *r);
@@ -251,7 +275,7 @@ int hgb_ru_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M
  * the reference's order.  The rotations and the back substitution run on the device and one
  * restart cycle is one CUDA graph (one host synchronisation per cycle, where the reference
  * reads the projection back in every inner iteration, :67-72).  max_iter bounds the restarts,
- * tol is absolute on the preconditioned residual estimate, restart 1..64.  F64, F32 or BF16
+ * tol is absolute on the preconditioned residual estimate, restart 1..512.  F64, F32 or BF16
  * values (A's precision; FP32 vectors for BF16) with a preconditioner of matching precision. */
 int hgb_gmres_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int restart, const void *b, void *x,
                     double tol, int max_iter, hgb_solve_info *info);

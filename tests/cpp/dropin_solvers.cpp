@@ -17,12 +17,14 @@
 #include "hala_solvers.hpp"
 
 #include <cmath>
+#include <csignal>
 #include <cstdio>
 #include <vector>
 
 namespace {
 
 int failures = 0;
+void stage(const char *what) { std::printf("case: %s\n", what); }
 void check(bool ok, const char *what) {
     std::printf("%s %s\n", ok ? "ok  " : "FAIL", what);
     if (!ok) failures++;
@@ -60,6 +62,7 @@ void aniso3d(int m, std::vector<int> &p, std::vector<int> &ix, std::vector<doubl
 }  // namespace
 
 int main() {
+    std::setvbuf(stdout, nullptr, _IONBF, 0);   // every line is out before anything can go wrong
     hala::gpu_engine engine(0);
     hala::mixed_engine mixed(engine);
     hala::cpu_engine cpu;
@@ -69,6 +72,7 @@ int main() {
         std::vector<double> v = {2, -1, -1, 2, -1, -1, 2, -1, -1, 2, -1, -1, 2};
         std::vector<double> b = {1, 0, 0, 0, 1}, xref = {1, 1, 1, 1, 1};
         std::vector<double> x;
+        stage("tridiagonal, mixed_engine");
         int it = hala::solve_cg_ilu(mixed, hala::stop_criteria<double>(2), p, ix, v, b, x);
         check(it == 2 && rel_err(x, xref) < 1e-14, "solve_cg_ilu(mixed_engine): the exact tridiagonal case");
         auto gp = engine.load(p);
@@ -76,6 +80,7 @@ int main() {
         auto gv = engine.load(v);
         auto gb = engine.load(b);
         hala::gpu_vector<double> gx(engine.device());
+        stage("tridiagonal, gpu_engine");
         it = hala::solve_cg_ilu(engine, hala::stop_criteria<double>(2), gp, gi, gv, gb, gx);
         check(it == 2 && rel_err(gx.unload(), xref) < 1e-14, "solve_cg_ilu(gpu_engine): the exact tridiagonal case");
     }
@@ -86,6 +91,7 @@ int main() {
         for (int r = 0; r < 5; r++)
             for (int k = p[r]; k < p[r + 1]; k++) b[r] += v[k] * xref[ix[k]];
         std::vector<double> x;
+        stage("gmres 5x5, mixed_engine");
         hala::solve_gmres_ilu(mixed, hala::stop_criteria<double>(1e-12, 20), 3, p, ix, v, b, x);
         check(rel_err(x, xref) < 1e-10, "solve_gmres_ilu(mixed_engine): nonsymmetric 5 x 5");
     }
@@ -102,13 +108,16 @@ int main() {
         for (double t : b) bn += t * t;
         const double tol = 1e-10 * std::sqrt(bn);
         std::vector<double> xc;
+        stage("12^3 cpu_engine");
         const int itc = hala::solve_cg_ilu(cpu, hala::stop_criteria<double>(tol), p, ix, v, b, xc);
         std::vector<double> xg;
         engine.set_spmv_mode("exact");
+        stage("12^3 mixed_engine cg_ilu");
         const int itg = hala::solve_cg_ilu(mixed, hala::stop_criteria<double>(tol), p, ix, v, b, xg);
         check(std::abs(itg - itc) <= 1 + itc / 20 && rel_err(xg, xc) < 1e-8,
               "solve_cg_ilu(mixed_engine) vs cpu_engine, 12^3: iterations within 5%, solution within 1e-8");
         std::vector<double> xu;
+        stage("12^3 mixed_engine cg");
         const int itu = hala::solve_cg(mixed, hala::stop_criteria<double>(tol), p, ix, v,
                                        [](auto const &in, auto &out) { hala::vcopy(in, out); }, b, xu);
         std::vector<double> xuc;
@@ -117,6 +126,7 @@ int main() {
         check(std::abs(itu - itc2) <= 1 + itc2 / 20 && rel_err(xu, xuc) < 1e-8,
               "solve_cg(mixed_engine) without preconditioner vs cpu_engine");
         std::vector<double> xgm;
+        stage("12^3 mixed_engine gmres");
         const int itgm = hala::solve_gmres_ilu(mixed, hala::stop_criteria<double>(tol, 50), 30, p, ix, v, b, xgm);
         check(itgm > 0 && rel_err(xgm, xt) < 1e-7, "solve_gmres_ilu(mixed_engine), GMRES(30), 12^3");
         // several right-hand sides with one matrix: the reference's batch CG
@@ -124,6 +134,7 @@ int main() {
         std::vector<double> B(hala::hala_size(n, nrhs)), X;
         for (int c = 0; c < nrhs; c++)
             for (int i = 0; i < n; i++) B[(size_t)c * n + i] = b[i] * (1.0 + c);
+        stage("12^3 mixed_engine batch cg");
         const int itb = hala::solve_batch_cg_ilu(mixed, hala::stop_criteria<double>(tol * nrhs), p, ix, v, B, X);
         double e = 0;
         for (int c = 0; c < nrhs; c++) {

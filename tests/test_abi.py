@@ -49,7 +49,7 @@ def test_solver_argument_checks_need_no_device():
     cases = [
         (lambda: L.hgb_cg_solve(None, None, None, None, None, 1e-10, 10, C.byref(info)), b"cg_solve"),
         (lambda: L.hgb_gmres_solve(None, None, None, 30, None, None, 1e-10, 10, C.byref(info)), b"gmres"),
-        (lambda: L.hgb_gmres_solve(None, None, None, 65, None, None, 1e-10, 10, C.byref(info)), b"restart"),
+        (lambda: L.hgb_gmres_solve(None, None, None, 513, None, None, 1e-10, 10, C.byref(info)), b"restart"),
         (lambda: L.hgb_ru_pcg_solve(None, None, None, None, None, None, 1e-10, 0.01, 10, C.byref(info)),
          b"ru_pcg"),
         (lambda: L.hgb_ru_pcg_solve_op(None, None, None, None, b"T", None, None, 1e-10, 0.01, 10, C.byref(info)),

@@ -12,7 +12,7 @@ import torch
 
 from hala_gb300 import engine as E
 from hala_gb300 import problems as P
-from hala_gb300.hgb import HgbError, HGB_ERR_TIMEOUT
+from hala_gb300.hgb import HgbError, HGB_ERR_CSR, HGB_ERR_TIMEOUT
 from hala_gb300 import hgb as H
 from oracle import oracle as O
 from tests import refcases as R
@@ -219,3 +219,40 @@ def test_apply_bit_exact_at_bench_size(eng, rng):
     exact = O.ilu_apply_mixed(p, i, do, fo.astype(np.float32), fo[do], x32)
     for _ in range(2):
         assert np.array_equal(ilu32.apply(T(x32)).cpu().numpy().view(np.uint32), exact.view(np.uint32))
+
+
+@pytest.mark.parametrize("store", [torch.float64, torch.float32])
+def test_host_buffer_ilu_matches_device_ilu(eng, rng, store):
+    # make_ilu(mixed_engine, ...): host pattern and values, copies overlapped with the host planning;
+    # the factor, the level sets and the apply are those of the device-input creation, bit for bit
+    p, i, v = P.aniso3d(41, 37, 23)
+    n = len(p) - 1
+    Md = E.make_ilu(eng, T(p), T(i), T(v), store=store)
+    Mh = E.make_ilu_host(eng, p, i, v, store=store)
+    fd, dd = Md.factor()
+    fh, dh = Mh.factor()
+    assert torch.equal(fd, fh) and torch.equal(dd, dh)
+    x = torch.from_numpy(rng.standard_normal(n)).to(dev).to(store)
+    rd, rh = torch.empty_like(x), torch.empty_like(x)
+    Md.apply(x, rd)
+    Mh.apply(x, rh)
+    assert torch.equal(rd, rh)
+    fo, do, _ = O.ilu_factor(p, i, v)
+    assert np.array_equal(fh.cpu().numpy(), fo)
+
+
+def test_host_buffer_ilu_rejects_bad_pattern(eng):
+    p, i, v = P.aniso3d(6)
+    i = i.copy()
+    i[p[3]:p[4]] = i[p[3]:p[4]][::-1]   # unsorted row
+    with pytest.raises(HgbError) as e:
+        E.make_ilu_host(eng, p, i, v)
+    assert e.value.status == HGB_ERR_CSR
+    i[p[3]:p[4]] = np.sort(i[p[3]:p[4]])
+    keep = np.ones(len(i), bool)
+    keep[int(O.diag_index(p, i)[5])] = False   # drop the diagonal of row 5
+    p2 = p.copy()
+    p2[6:] -= 1
+    with pytest.raises(HgbError) as e:
+        E.make_ilu_host(eng, p2, i[keep], v[keep])
+    assert e.value.status == HGB_ERR_CSR

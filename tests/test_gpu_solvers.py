@@ -198,7 +198,23 @@ def test_gmres_restart_bounds(eng):
     x = torch.zeros(len(p) - 1, dtype=torch.float64, device=dev)
     b = torch.ones(len(p) - 1, dtype=torch.float64, device=dev)
     with pytest.raises(HgbError):
-        E.solve_gmres(eng, E.stop_criteria(1e-9), 65, gp, gi, gv, b, x)
+        E.solve_gmres(eng, E.stop_criteria(1e-9), 513, gp, gi, gv, b, x)
+
+
+@pytest.mark.parametrize("restart", [65, 150])
+def test_gmres_long_restart(eng, rng, restart):
+    # restarts above 64: the projection runs in groups of 64 basis columns (the reference has no cap)
+    p, i, v = P.aniso3d(20)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    tol = 1e-10 * np.linalg.norm(b)
+    xo, ito = O.gmres(p, i, v, b, restart, tol=tol, max_iter=3)
+    gp, gi, gv = T(p), T(i), T(v)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    it = E.solve_gmres(eng, E.stop_criteria(tol, 3), restart, gp, gi, gv, T(b), x)
+    assert ito > 65                   # the Krylov space grew past 64 columns
+    assert within5(it, ito), (it, ito)
+    assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-8 * np.linalg.norm(xo)
 
 
 def test_gmres_fp32(eng, rng):
