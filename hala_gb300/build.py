@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libhgb.so")
-SOURCES = ["hgb_core.cu", "hgb_spmv.cu", "hgb_ilu.cu", "hgb_solvers.cu", "hgb_batch.cu", "hgb_bsolve.cu", "hgb_static.cu", "hgb_mrhs.cu", "hgb_pattern.cu"]
+SOURCES = ["hgb_core.cu", "hgb_spmv.cu", "hgb_ilu.cu", "hgb_solvers.cu", "hgb_batch.cu", "hgb_bsolve.cu", "hgb_static.cu", "hgb_mrhs.cu", "hgb_pattern.cu", "hgb_complex.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

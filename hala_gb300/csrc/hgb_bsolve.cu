@@ -40,12 +40,12 @@
 
 namespace hgb {
 
-// Solver threads per CTA (NT, one row per thread per step): 128 for FP64 stores, whose 128 KB
-// slice holds one 16384-row block; 256 for FP32 / BF16 stores of patterns whose blocks hold two or
-// more planes of the wavefront (32768 rows): two solver warps per scheduler interleave the
-// latency-bound steps, and half as many blocks halve the hops between blocks.
+// Solver threads per CTA (NT, one row per thread per step).  The kernel is written for any
+// multiple of 32; 128 is the one built.  256 threads over 32768-row FP32 blocks (two planes of a
+// 128^3 wavefront per block, half as many hops) measured slower on GB300: 0.45 against 0.40 ms
+// per ILU(0) application at 128^3 and 0.40 against 0.27 ms at 96^3, the longer steps of the wider
+// CTA costing more than the hops saved.
 constexpr int kBsThreads = 128;
-constexpr int kBsThreadsWide = 256;
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 template <int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * kBsFetchWarps; }
 constexpr int kBsF = 32;          // steps in the remote-value ring
@@ -54,14 +54,14 @@ constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on 
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
-// value pieces per packet (NV) and packet-ring depth in steps (bs_depth, a power of two; the wide
-// layout's slice leaves room for 4)
+// value pieces per packet (NV) and packet-ring depth in steps (bs_depth, a power of two; the FP64
+// slice leaves room for 4)
 template <typename V> struct BsCfg;
 template <> struct BsCfg<double> { static constexpr int NV = 3; };
 template <> struct BsCfg<float> { static constexpr int NV = 2; };
 template <> struct BsCfg<uint16_t> { static constexpr int NV = 1; };
 template <typename V, int NT> __host__ __device__ constexpr int bs_depth() {
-    return (sizeof(V) == 8 || NT != kBsThreads) ? 4 : 8;
+    return (sizeof(V) == 8 || NT > kBsThreads) ? 4 : 8;
 }
 
 // the packet word (piece 0 .w): bits 0-14 the row's slot in the block, bits 15-30 its number of
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(bs_cta<NT>(), 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = bs_depth<V, NT>(), NP = 1 + NV;
     constexpr int CTA = bs_cta<NT>(), RPL = NT / 32;   // fetcher rows per lane
-    static_assert(NT == 128 || NT == 256, "solver threads");
+    static_assert(NT % 32 == 0 && NT <= 256, "solver threads");
     static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
     static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps, "remote ring shape");
     if (A.skip && *A.skip) return;
@@ -593,17 +593,16 @@ void BlockSolve::release() {
     *this = BlockSolve();
 }
 
-// Co-resident thread-block clusters of cl block-solve CTAs of nt solver threads (queried once per
-// device, cluster size and layout, with the layout's largest shared memory).  On GB300 one CTA per
-// SM fits, and 15 clusters of 8, 36 of 4 or 76 of 2 are co-resident.
-static int bs_clusters_fit(hgb_ctx *c, int nt, int cl) {
-    static int cache[64][2][kBsMaxCluster + 1];
-    static bool init[64][2][kBsMaxCluster + 1];
+// Co-resident thread-block clusters of cl block-solve CTAs (queried once per device and cluster
+// size, with the largest shared memory of a block: the FP64 store's).  On GB300 one CTA per SM
+// fits, and 15 clusters of 8, 36 of 4 or 76 of 2 are co-resident.
+static int bs_clusters_fit(hgb_ctx *c, int cl) {
+    static int cache[64][kBsMaxCluster + 1];
+    static bool init[64][kBsMaxCluster + 1];
     static std::mutex mu;
     std::lock_guard<std::mutex> lock(mu);
-    const int ri = nt == kBsThreads ? 0 : 1;
     if (c->device < 0 || c->device >= 64 || cl < 1 || cl > kBsMaxCluster) return 0;
-    if (init[c->device][ri][cl]) return cache[c->device][ri][cl];
+    if (init[c->device][cl]) return cache[c->device][cl];
     auto fits = [&](auto kernel, size_t smem) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
             (cl > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)) {
@@ -612,7 +611,7 @@ static int bs_clusters_fit(hgb_ctx *c, int nt, int cl) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cl * 16);
-        cfg.blockDim = dim3(ri == 0 ? bs_cta<kBsThreads>() : bs_cta<kBsThreadsWide>());
+        cfg.blockDim = dim3(bs_cta<kBsThreads>());
         cfg.dynamicSmemBytes = smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -629,14 +628,10 @@ static int bs_clusters_fit(hgb_ctx *c, int nt, int cl) {
         return n;
     };
     DeviceGuard g(c->device);
-    // the largest shared-memory layout of the class (narrow: FP64 store; wide: FP32 store)
-    const int n = (ri == 0)
-                      ? fits(bsolve_kernel<double, double, 0, true, false, kBsThreads>,
-                             bs_smem_bytes<double, double, kBsThreads>(16384))
-                      : fits(bsolve_kernel<float, float, 0, true, false, kBsThreadsWide>,
-                             bs_smem_bytes<float, float, kBsThreadsWide>(32768));
-    cache[c->device][ri][cl] = n;
-    init[c->device][ri][cl] = true;
+    const int n = fits(bsolve_kernel<double, double, 0, true, false, kBsThreads>,
+                       bs_smem_bytes<double, double, kBsThreads>(16384));
+    cache[c->device][cl] = n;
+    init[c->device][cl] = true;
     return n;
 }
 
@@ -647,12 +642,12 @@ static int bs_clusters_fit(hgb_ctx *c, int nt, int cl) {
 // that, the largest of 8, 4, 2 that fits.  On GB300 (one CTA per SM) 15 clusters of 8 are
 // co-resident, so for 128 blocks a size between 9 and 16 that still fits 128 CTAs at once removes
 // the wait for a free cluster.
-static int bs_cluster_plan(hgb_ctx *c, int nt, int nblk) {
+static int bs_cluster_plan(hgb_ctx *c, int nblk) {
     if (nblk < 2) return 1;
     for (int cl = std::min(kBsMaxCluster, nblk); cl > 1; cl--)
-        if ((long)bs_clusters_fit(c, nt, cl) * cl >= nblk) return cl;
+        if ((long)bs_clusters_fit(c, cl) * cl >= nblk) return cl;
     for (int cl = 8; cl > 1; cl /= 2)
-        if (bs_clusters_fit(c, nt, cl) >= 1) return cl;
+        if (bs_clusters_fit(c, cl) >= 1) return cl;
     return 1;
 }
 
@@ -676,7 +671,7 @@ static int upload(T **dst, const std::vector<T> &src) {
 // The schedule on the host (structure only; the values are gathered on the device through map3 /
 // dv_map / dv_row / ovf_map), before its upload.
 struct BsPlan {
-    int n = 0, R = 0, nt = kBsThreads, cl = 1;
+    int n = 0, R = 0, cl = 1;
     std::vector<int4> blk, desc, pk0;
     std::vector<int> map3, dv_map, dv_row, ovf_codes, ovf_map, rj, push;
 };
@@ -708,15 +703,9 @@ static int bsolve_plan(hgb_ctx *c, int n, int nnz, const int *pntr, const int *i
         deps(row, a, e);
         if (e > a) bw = std::max(bw, lower ? row - indx[a] : indx[e - 1] - row);
     }
-    // FP32 / BF16 solutions of patterns with a wide wavefront (bandwidth of at least 4096 rows, two
-    // or more bands in 32768 rows) take the wide layout: 256 solver threads, blocks of 32768 rows
-    int NT = kBsThreads;
-    if (xsize == 4 && bw >= 4096 && bw <= 16384) {
-        NT = kBsThreadsWide;
-        R = 32768 / bw * bw;
-    } else if (bw >= 1 && bw <= R) {
-        R = R / bw * bw;
-    }
+    (void)xsize;
+    constexpr int NT = kBsThreads;
+    if (bw >= 1 && bw <= R) R = R / bw * bw;
     const int Rmax = R;
     lev.assign(R, 0);
     for (int p0 = 0; p0 < n;) {
@@ -802,7 +791,7 @@ static int bsolve_plan(hgb_ctx *c, int n, int nnz, const int *pntr, const int *i
     // straight to block b+1's ring (consumer step << 8 | consumer thread).  A producer row offers
     // to at most one consumer row.  Offered rows leave the fetchers' lists; an offer that is dropped
     // (the consumer more than a ring's length behind) is read from L2 by the consumer itself.
-    const int cl = bs_cluster_plan(c, NT, (int)blk.size());
+    const int cl = bs_cluster_plan(c, (int)blk.size());
     std::vector<int> &push = P.push;
     push.assign(pk0.size(), -1);
     if (cl > 1) {
@@ -831,7 +820,6 @@ static int bsolve_plan(hgb_ctx *c, int n, int nnz, const int *pntr, const int *i
     }
     P.n = n;
     P.R = Rmax;
-    P.nt = NT;
     P.cl = cl;
     return HGB_OK;
 }
@@ -842,7 +830,6 @@ static int bsolve_upload(const BsPlan &P, BlockSolve &S) {
     S.nblk = (int)P.blk.size();
     S.nsteps = (int)P.desc.size();
     S.R = P.R;
-    S.nt = P.nt;
     S.cl = P.cl;
     S.npk = (long)P.pk0.size();
     S.novf = (long)P.ovf_codes.size();
@@ -939,9 +926,9 @@ template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
 static int bs_launch_nt(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
     constexpr int CTA = bs_cta<NT>();
     const size_t smem = bs_smem_bytes<V, X, NT>(S.R);
-    // the attribute allows the largest block of the layout (narrow: 16384 FP64 / 32768 FP32 rows,
-    // wide: 32768 rows), so solves with smaller blocks launch too
-    const size_t smem_max = bs_smem_bytes<V, X, NT>((sizeof(X) == 8 && NT == kBsThreads) ? 16384 : 32768);
+    // the attribute allows the largest block (16384 FP64 / 32768 FP32 rows), so solves with smaller
+    // blocks launch too
+    const size_t smem_max = bs_smem_bytes<V, X, NT>(sizeof(X) == 8 ? 16384 : 32768);
     static int attr_dev = -1;   // device on which the kernel's shared-memory attribute was set
     if (attr_dev != c->device) {
         int mx = 0;
@@ -996,15 +983,9 @@ static int bs_launch_nt(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alph
     return launch_check("bsolve_kernel");
 }
 
-// the schedule's layout: 128 solver threads, or 256 for FP32 / BF16 solutions of the wide layout
 template <typename V, typename X, int MODE, bool UNIT, bool RECIP>
 static int bs_launch_one(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
-    if (S.nt == kBsThreads) return bs_launch_nt<V, X, MODE, UNIT, RECIP, kBsThreads>(c, S, A, alpha, in, out, pend);
-    if constexpr (sizeof(X) == 4) {
-        if (S.nt == kBsThreadsWide)
-            return bs_launch_nt<V, X, MODE, UNIT, RECIP, kBsThreadsWide>(c, S, A, alpha, in, out, pend);
-    }
-    return fail(HGB_ERR_ARG, "bsolve: a schedule of %d threads for a %d-byte solution", S.nt, (int)sizeof(X));
+    return bs_launch_nt<V, X, MODE, UNIT, RECIP, kBsThreads>(c, S, A, alpha, in, out, pend);
 }
 
 template <typename V, typename X>

@@ -16,7 +16,6 @@ struct BlockSolve {
     int *rj = nullptr;          // [npk] first dependency of the row on an earlier block (fetched), or -1
     int *push = nullptr;        // [npk] where the row's value goes in the next block's ring, or -1
     int cl = 1;                 // CTAs per thread-block cluster the push targets assume
-    int nt = 128;               // solver threads per CTA (rows per step) the schedule was cut for
     int *ovf_codes = nullptr;   // [novf] dependencies beyond the third, column-major per step
     void *ovf_vals = nullptr;
     int *map3 = nullptr, *dv_map = nullptr, *dv_row = nullptr, *ovf_map = nullptr;   // value gather maps

@@ -1,6 +1,7 @@
 // Library core: error reporting, the engine context, BLAS-1, tall-skinny gemv, diagonal index.
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
+#include "hgb_complex.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -330,6 +331,57 @@ int hgb_copy_f32(hgb_ctx *c, int n, const float *x, float *y) {
     DeviceGuard g(c->device);
     if (n) HGB_CUDA(cudaMemcpyAsync(y, x, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
     return HGB_OK;
+}
+
+int hgb_dotc_c128(hgb_ctx *c, int n, const void *x, const void *y, double *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "dotc: null context");
+    DeviceGuard g(c->device);
+    return zdot<double>(c, 0, n, x, y, r, d);
+}
+int hgb_dotc_c64(hgb_ctx *c, int n, const void *x, const void *y, float *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "dotc: null context");
+    DeviceGuard g(c->device);
+    return zdot<float>(c, 0, n, x, y, r, d);
+}
+int hgb_dotu_c128(hgb_ctx *c, int n, const void *x, const void *y, double *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "dotu: null context");
+    DeviceGuard g(c->device);
+    return zdot<double>(c, 1, n, x, y, r, d);
+}
+int hgb_dotu_c64(hgb_ctx *c, int n, const void *x, const void *y, float *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "dotu: null context");
+    DeviceGuard g(c->device);
+    return zdot<float>(c, 1, n, x, y, r, d);
+}
+int hgb_nrm2_c128(hgb_ctx *c, int n, const void *x, double *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "nrm2: null context");
+    DeviceGuard g(c->device);
+    return zdot<double>(c, 2, n, x, x, r, d);
+}
+int hgb_axpy_c128(hgb_ctx *c, int n, const double *a, const void *x, void *y) {
+    if (!c) return fail(HGB_ERR_ARG, "axpy: null context");
+    DeviceGuard g(c->device);
+    return zaxpy<double>(c, n, a, x, y);
+}
+int hgb_scal_c128(hgb_ctx *c, int n, const double *a, void *x) {
+    if (!c) return fail(HGB_ERR_ARG, "scal: null context");
+    DeviceGuard g(c->device);
+    return zscal<double>(c, n, a, x);
+}
+int hgb_nrm2_c64(hgb_ctx *c, int n, const void *x, float *r, int d) {
+    if (!c) return fail(HGB_ERR_ARG, "nrm2: null context");
+    DeviceGuard g(c->device);
+    return zdot<float>(c, 2, n, x, x, r, d);
+}
+int hgb_axpy_c64(hgb_ctx *c, int n, const float *a, const void *x, void *y) {
+    if (!c) return fail(HGB_ERR_ARG, "axpy: null context");
+    DeviceGuard g(c->device);
+    return zaxpy<float>(c, n, a, x, y);
+}
+int hgb_scal_c64(hgb_ctx *c, int n, const float *a, void *x) {
+    if (!c) return fail(HGB_ERR_ARG, "scal: null context");
+    DeviceGuard g(c->device);
+    return zscal<float>(c, n, a, x);
 }
 
 int hgb_set_zero(hgb_ctx *c, size_t bytes, void *x) {

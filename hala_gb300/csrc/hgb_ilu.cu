@@ -16,6 +16,7 @@
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
 #include "hgb_bsolve.cuh"
+#include "hgb_complex.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -485,6 +486,7 @@ struct hgb_ilu {
     // block-local level schedules (hgb_bsolve.cu); the global-level kernel is the fallback
     bool use_bs = false, use_bsT = false;
     BlockSolve BL, BU, BLT, BUT;
+    hgb_zilu *z = nullptr;      // the complex factor (C128 / C64); none of the fields above is used then
     // host-buffer creation: the object owns its device copies of the pattern and the values
     int *own_pntr = nullptr, *own_indx = nullptr;
     void *own_vals = nullptr;
@@ -492,8 +494,10 @@ struct hgb_ilu {
 
 namespace hgb {
 
-static size_t vsize(hgb_dtype t) { return t == HGB_F64 ? 8 : (t == HGB_F32 ? 4 : 2); }
-static size_t xsize(hgb_dtype store) { return store == HGB_F64 ? 8 : 4; }
+static size_t vsize(hgb_dtype t) {
+    return t == HGB_C128 ? 16 : (t == HGB_F64 || t == HGB_C64) ? 8 : (t == HGB_F32 ? 4 : 2);
+}
+static size_t xsize(hgb_dtype store) { return store == HGB_BF16 ? 4 : vsize(store); }
 
 static void ilu_free(hgb_ilu *M) {
     if (!M) return;
@@ -518,6 +522,7 @@ static void ilu_free(hgb_ilu *M) {
     cudaFree(M->own_pntr);
     cudaFree(M->own_indx);
     cudaFree(M->own_vals);
+    zilu_destroy(M->z);
     delete M;
 }
 
@@ -634,6 +639,7 @@ struct hgb_tri {
     hgb_dtype dtype = HGB_F64;
     int *diag = nullptr;
     Schedule S;
+    hgb_ztri *z = nullptr;     // the complex triangle (C128 / C64)
     bool has_T = false;
     Transpose T;
     int *diagT = nullptr;
@@ -646,7 +652,11 @@ extern "C" {
 static int ilu_check_args(hgb_ctx *c, int n, int nnz, const void *pntr, const void *indx, const void *vals,
                           hgb_dtype vals_dtype, hgb_dtype store) {
     if (!c || n <= 0 || nnz < n || !pntr || !indx || !vals) return fail(HGB_ERR_ARG, "ilu0_create: bad arguments (n=%d nnz=%d)", n, nnz);
-    if (vals_dtype != HGB_F64 && vals_dtype != HGB_F32) return fail(HGB_ERR_ARG, "ilu0_create: vals dtype must be F64 or F32");
+    if (vals_dtype == HGB_C128 || vals_dtype == HGB_C64) {
+        if (store != vals_dtype) return fail(HGB_ERR_UNSUPPORTED, "ilu0_create: a complex factor is stored in its own precision");
+        return HGB_OK;
+    }
+    if (vals_dtype != HGB_F64 && vals_dtype != HGB_F32) return fail(HGB_ERR_ARG, "ilu0_create: vals dtype must be F64, F32, C128 or C64");
     if (store != HGB_F64 && store != HGB_F32 && store != HGB_BF16) return fail(HGB_ERR_ARG, "ilu0_create: store dtype");
     if (vals_dtype == HGB_F32 && store != HGB_F32) return fail(HGB_ERR_UNSUPPORTED, "ilu0_create: an F32 factor is stored as F32");
     return HGB_OK;
@@ -728,6 +738,18 @@ static int ilu_create_device(hgb_ctx *c, int n, int nnz, const int *pntr, const 
     return st;
 }
 
+// complex factors: the level-synchronous factorisation and sweeps of hgb_complex.cu
+static int ilu_create_complex(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const void *vals,
+                              hgb_dtype dt, hgb_ilu *M, int *zero_pivot) {
+    M->ctx = c;
+    M->n = n;
+    M->nnz = nnz;
+    M->pntr = pntr;
+    M->indx = indx;
+    M->fdtype = M->store = dt;
+    return zilu_create(c, n, nnz, pntr, indx, vals, dt == HGB_C128 ? 8 : 4, &M->z, zero_pivot);
+}
+
 int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx, const void *vals,
                     hgb_dtype vals_dtype, hgb_dtype store, char policy, hgb_ilu **out) {
     (void)policy;
@@ -737,7 +759,9 @@ int hgb_ilu0_create(hgb_ctx *c, int n, int nnz, const int *pntr, const int *indx
     DeviceGuard g(c->device);
     hgb_ilu *M = new hgb_ilu();
     int zero_pivot = 0;
-    const int st = ilu_create_device(c, n, nnz, pntr, indx, vals, vals_dtype, store, M, &zero_pivot, nullptr);
+    const int st = (vals_dtype == HGB_C128 || vals_dtype == HGB_C64)
+                       ? ilu_create_complex(c, n, nnz, pntr, indx, vals, vals_dtype, M, &zero_pivot)
+                       : ilu_create_device(c, n, nnz, pntr, indx, vals, vals_dtype, store, M, &zero_pivot, nullptr);
     if (st) {
         ilu_free(M);
         return st;
@@ -800,16 +824,19 @@ int hgb_ilu0_create_host(hgb_ctx *c, int n, int nnz, const int *pntr_h, const in
             copy_status = cuda_fail(cudaGetLastError(), "ilu0_create_host copy");
         if (copy_status) copy_msg = hgb_last_error();
     });
+    const bool cplx = (vals_dtype == HGB_C128 || vals_dtype == HGB_C64);
     BsPlanPair *plan = nullptr;
-    const int pst = bsolve_plan_pair(c, n, nnz, pntr_h, indx_h, diag.data(), bsolve_rows(c, (int)xsize(store), n),
-                                     (int)xsize(store), &plan);
+    const int pst = cplx ? HGB_ERR_UNSUPPORTED
+                         : bsolve_plan_pair(c, n, nnz, pntr_h, indx_h, diag.data(),
+                                            bsolve_rows(c, (int)xsize(store), n), (int)xsize(store), &plan);
     copier.join();
     int st = copy_status ? fail(copy_status, "%s", copy_msg.c_str()) : HGB_OK;
     int zero_pivot = 0;
     // a pattern the block solve cannot hold leaves plan null: the device path plans (and falls back) itself
     if (!st && pst && pst != HGB_ERR_UNSUPPORTED) st = pst;
-    if (!st) st = ilu_create_device(c, n, nnz, M->own_pntr, M->own_indx, M->own_vals, vals_dtype, store, M, &zero_pivot,
-                                    plan);
+    if (!st && cplx) st = ilu_create_complex(c, n, nnz, M->own_pntr, M->own_indx, M->own_vals, vals_dtype, M, &zero_pivot);
+    else if (!st) st = ilu_create_device(c, n, nnz, M->own_pntr, M->own_indx, M->own_vals, vals_dtype, store, M,
+                                         &zero_pivot, plan);
     bsolve_plan_pair_free(plan);
     if (st) {
         ilu_free(M);
@@ -834,6 +861,10 @@ int ilu_apply_internal(hgb_ilu *M, char trans, const void *x, void *r, const int
     bool nt = (trans == 'N' || trans == 'n');
     bool tt = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
     if (!nt && !tt) return fail(HGB_ERR_ARG, "ilu0_apply: trans '%c'", trans);
+    if (M->z) {
+        HGB_TRY(zilu_apply(M->z, trans, x, r));
+        return collect_dev_error(M->ctx);
+    }
     switch (M->store) {
         case HGB_F64: return nt ? ilu_apply_n<double, double>(M, x, r, skip) : ilu_apply_t<double, double>(M, x, r, skip);
         case HGB_F32: return nt ? ilu_apply_n<float, float>(M, x, r, skip) : ilu_apply_t<float, float>(M, x, r, skip);
@@ -848,14 +879,19 @@ int hgb_ilu0_export(hgb_ilu *M, void *factor_vals, int *diag) {
     if (!M) return fail(HGB_ERR_ARG, "ilu0_export: null handle");
     hgb_ctx *c = M->ctx;
     DeviceGuard g(c->device);
-    if (factor_vals) HGB_CUDA(cudaMemcpyAsync(factor_vals, M->fvals, vsize(M->fdtype) * M->nnz, cudaMemcpyDeviceToDevice, c->stream));
-    if (diag) HGB_CUDA(cudaMemcpyAsync(diag, M->diag, sizeof(int) * M->n, cudaMemcpyDeviceToDevice, c->stream));
+    if (M->z) {
+        HGB_TRY(zilu_export(M->z, factor_vals, diag));
+    } else {
+        if (factor_vals) HGB_CUDA(cudaMemcpyAsync(factor_vals, M->fvals, vsize(M->fdtype) * M->nnz, cudaMemcpyDeviceToDevice, c->stream));
+        if (diag) HGB_CUDA(cudaMemcpyAsync(diag, M->diag, sizeof(int) * M->n, cudaMemcpyDeviceToDevice, c->stream));
+    }
     HGB_CUDA(cudaStreamSynchronize(c->stream));
     return HGB_OK;
 }
 
 int hgb_ilu0_levels(hgb_ilu *M, char uplo, int *level, int *nlevels) {
     if (!M) return fail(HGB_ERR_ARG, "ilu0_levels: null handle");
+    if (M->z) return fail(HGB_ERR_UNSUPPORTED, "ilu0_levels: real factors");
     hgb_ctx *c = M->ctx;
     DeviceGuard g(c->device);
     const Schedule &S = (uplo == 'L' || uplo == 'l') ? M->L : M->U;
@@ -881,9 +917,22 @@ int hgb_tri_create(hgb_ctx *c, char uplo, char diagc, int n, int nnz, const int 
     bool lower = (uplo == 'L' || uplo == 'l');
     if (!lower && uplo != 'U' && uplo != 'u') return fail(HGB_ERR_ARG, "tri_create: uplo '%c'", uplo);
     if (diagc != 'U' && diagc != 'u' && diagc != 'N' && diagc != 'n') return fail(HGB_ERR_ARG, "tri_create: diag '%c'", diagc);
-    if (dtype != HGB_F64 && dtype != HGB_F32) return fail(HGB_ERR_UNSUPPORTED, "tri_create: F64 or F32 values");
+    if (dtype != HGB_F64 && dtype != HGB_F32 && dtype != HGB_C128 && dtype != HGB_C64)
+        return fail(HGB_ERR_UNSUPPORTED, "tri_create: F64, F32, C128 or C64 values");
     DeviceGuard g(c->device);
     HGB_TRY(csr_check(c, n, n, nnz, pntr, indx));
+    if (dtype == HGB_C128 || dtype == HGB_C64) {
+        hgb_ztri *z = nullptr;
+        HGB_TRY(ztri_create(c, lower ? 'L' : 'U', diagc, n, nnz, pntr, indx, vals, dtype == HGB_C128 ? 8 : 4, &z));
+        hgb_tri *T = new hgb_tri();
+        T->ctx = c;
+        T->n = n;
+        T->nnz = nnz;
+        T->dtype = dtype;
+        T->z = z;
+        *out = T;
+        return HGB_OK;
+    }
     hgb_tri *T = new hgb_tri();
     T->ctx = c;
     T->n = n;
@@ -964,6 +1013,12 @@ int hgb_tri_solve(hgb_tri *T, char trans, double alpha, const void *b, void *x) 
     if (trans != 'N' && trans != 'n' && trans != 'T' && trans != 't' && trans != 'C' && trans != 'c')
         return fail(HGB_ERR_ARG, "tri_solve: trans '%c'", trans);
     DeviceGuard g(T->ctx->device);
+    if (T->z) {
+        const double a2[2] = {alpha, 0.0};
+        const float a1[2] = {(float)alpha, 0.0f};
+        HGB_TRY(ztri_solve(T->z, trans, T->dtype == HGB_C128 ? (const void *)a2 : (const void *)a1, b, x));
+        return collect_dev_error(T->ctx);
+    }
     int st = (T->dtype == HGB_F64) ? tri_solve_t<double>(T, trans, alpha, b, x) : tri_solve_t<float>(T, trans, alpha, b, x);
     if (st) return st;
     return collect_dev_error(T->ctx);
@@ -972,6 +1027,7 @@ int hgb_tri_solve(hgb_tri *T, char trans, double alpha, const void *b, void *x) 
 int hgb_tri_destroy(hgb_tri *T) {
     if (!T) return HGB_OK;
     DeviceGuard g(T->ctx->device);
+    ztri_destroy(T->z);
     cudaFree(T->diag);
     cudaFree(T->bcopy);
     T->S.release();
@@ -990,4 +1046,6 @@ int hgb_tri_destroy(hgb_tri *T) {
 namespace hgb {
 hgb_dtype ilu_store(const hgb_ilu *M) { return M->store; }
 int ilu_n(const hgb_ilu *M) { return M->n; }
+size_t ilu_xbytes(const hgb_ilu *M) { return M->store == HGB_BF16 ? 4 : vsize(M->store); }
+hgb_zilu *ilu_zfactor(const hgb_ilu *M) { return M->z; }
 }  // namespace hgb

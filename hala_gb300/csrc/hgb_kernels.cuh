@@ -3,6 +3,8 @@
 
 #include "hgb_internal.cuh"
 
+struct hgb_zilu;
+
 namespace hgb {
 
 // ------------------------------------------------------------ TMA / mbarrier helpers ----
@@ -146,6 +148,15 @@ int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int
 int ilu_apply_internal(hgb_ilu *M, char trans, const void *x, void *r, const int *skip = nullptr);
 hgb_dtype ilu_store(const hgb_ilu *M);
 int ilu_n(const hgb_ilu *M);
+size_t ilu_xbytes(const hgb_ilu *M);       // bytes of one element of the vectors the apply reads and writes
+hgb_zilu *ilu_zfactor(const hgb_ilu *M);   // the complex factor of a C128 / C64 handle, else null
+inline bool real_inner(hgb_dtype t) { return t == HGB_F32 || t == HGB_BF16; }
+// a preconditioner stored in precision s serves a matrix of dtype t: F64, C128 and C64 alike,
+// F32 / BF16 matrices with either F32 or BF16 stores (vectors float)
+inline bool ilu_matches(hgb_dtype s, hgb_dtype t) {
+    if (t == HGB_F64 || t == HGB_C128 || t == HGB_C64) return s == t;
+    return real_inner(s);
+}
 
 // transposed operator for the adjoint solves: build (once) the cached transpose, then
 // y = alpha A^T x + beta y with an optional fused <dot_x, y>

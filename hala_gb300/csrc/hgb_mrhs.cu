@@ -213,6 +213,9 @@ int hgb_csr_gemm(hgb_csr *A, int nrhs, double alpha, const void *x, int ldx, dou
             return mr_gemm<double>(A, nrhs, alpha, (const double *)x, ldx, beta, (double *)y, ldy);
         case HGB_F32:
             return mr_gemm<float>(A, nrhs, (float)alpha, (const float *)x, ldx, (float)beta, (float *)y, ldy);
+        case HGB_C128:
+        case HGB_C64:
+            return fail(HGB_ERR_UNSUPPORTED, "csr_gemm: real matrices (complex products go column by column through csr_gemv)");
         default:
             return mr_gemm<uint16_t>(A, nrhs, (float)alpha, (const float *)x, ldx, (float)beta, (float *)y, ldy);
     }
@@ -221,7 +224,7 @@ int hgb_csr_gemm(hgb_csr *A, int nrhs, double alpha, const void *x, int ldx, dou
 int hgb_ilu0_apply_nrhs(hgb_ilu *M, char trans, int nrhs, const void *x, void *r) {
     if (!M || nrhs < 0 || (nrhs > 0 && (!x || !r))) return fail(HGB_ERR_ARG, "ilu0_apply_nrhs: bad arguments");
     const long n = ilu_n(M);
-    const size_t xs = ilu_store(M) == HGB_F64 ? 8 : 4;
+    const size_t xs = ilu_xbytes(M);
     for (int k = 0; k < nrhs; k++)
         HGB_TRY(ilu_apply_internal(M, trans, (const char *)x + k * n * xs, (char *)r + k * n * xs));
     return HGB_OK;
@@ -234,10 +237,10 @@ int hgb_cg_solve_nrhs(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int nrhs, const void *
     if (max_iter < 1) return fail(HGB_ERR_ARG, "cg_solve_nrhs: max_iter < 1");
     DeviceGuard g(c->device);
     const hgb_dtype dt = csr_dtype(A);
+    if (dt == HGB_C128 || dt == HGB_C64) return fail(HGB_ERR_UNSUPPORTED, "cg_solve_nrhs: real matrices");
     if (M) {
         if (ilu_n(M) != csr_rows(A)) return fail(HGB_ERR_ARG, "cg_solve_nrhs: preconditioner size");
-        const bool ok = (dt == HGB_F64) ? (ilu_store(M) == HGB_F64) : (ilu_store(M) != HGB_F64);
-        if (!ok) return fail(HGB_ERR_ARG, "cg_solve_nrhs: preconditioner precision does not match the matrix");
+        if (!ilu_matches(ilu_store(M), dt)) return fail(HGB_ERR_ARG, "cg_solve_nrhs: preconditioner precision does not match the matrix");
     }
     int it = 0;
     double rn = 0.0;

@@ -9,6 +9,7 @@
 // iteration as the reference does (cublasDdot / cublasDnrm2 in host pointer mode).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
+#include "hgb_complex.cuh"
 
 #include <algorithm>
 #include <cstddef>
@@ -259,8 +260,11 @@ int hgb_cg_solve_op(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, char trans, const void *
     hgb_dtype dt = csr_dtype(A);
     if (M) {
         if (ilu_n(M) != csr_rows(A)) return fail(HGB_ERR_ARG, "cg_solve: preconditioner size");
-        bool ok = (dt == HGB_F64) ? (ilu_store(M) == HGB_F64) : (ilu_store(M) != HGB_F64);
-        if (!ok) return fail(HGB_ERR_ARG, "cg_solve: preconditioner precision does not match the matrix");
+        if (!ilu_matches(ilu_store(M), dt)) return fail(HGB_ERR_ARG, "cg_solve: preconditioner precision does not match the matrix");
+    }
+    if (dt == HGB_C128 || dt == HGB_C64) {
+        if (tr) return fail(HGB_ERR_UNSUPPORTED, "cg_solve: transposed complex solves");
+        return zcg_solve(c, A, M ? ilu_zfactor(M) : nullptr, b, x, tol, max_iter, info);
     }
     int it = 0;
     double rr = 0.0;
@@ -293,8 +297,8 @@ int hgb_ir_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *Mi, char
     if (!tr && trans != 'N' && trans != 'n') return fail(HGB_ERR_ARG, "ir_pcg: trans '%c'", trans);
     if (tr && csr_dtype(Ai) == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "ir_pcg: transposed solve with a bf16 matrix");
     if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the outer matrix must be F64");
-    if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the inner matrix must be F32 or BF16");
-    if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ir_pcg: the inner preconditioner must store F32 or BF16");
+    if (!real_inner(csr_dtype(Ai))) return fail(HGB_ERR_ARG, "ir_pcg: the inner matrix must be F32 or BF16");
+    if (Mi && !real_inner(ilu_store(Mi))) return fail(HGB_ERR_ARG, "ir_pcg: the inner preconditioner must store F32 or BF16");
     const long n = csr_rows(A64);
     if (csr_rows(Ai) != n || csr_cols(A64) != n) return fail(HGB_ERR_ARG, "ir_pcg: sizes");
     if (max_inner < 1 || max_outer < 0 || !(inner_rtol > 0.0)) return fail(HGB_ERR_ARG, "ir_pcg: limits");
@@ -544,8 +548,8 @@ extern "C" int hgb_ru_pcg_solve_op(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_il
     if (!tr && trans != 'N' && trans != 'n') return fail(HGB_ERR_ARG, "ru_pcg: trans '%c'", trans);
     if (tr && csr_dtype(Ai) == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "ru_pcg: transposed solve with a bf16 matrix");
     if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the outer matrix must be F64");
-    if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the inner matrix must be F32 or BF16");
-    if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ru_pcg: the preconditioner must store F32 or BF16");
+    if (!real_inner(csr_dtype(Ai))) return fail(HGB_ERR_ARG, "ru_pcg: the inner matrix must be F32 or BF16");
+    if (Mi && !real_inner(ilu_store(Mi))) return fail(HGB_ERR_ARG, "ru_pcg: the preconditioner must store F32 or BF16");
     const long n = csr_rows(A64);
     if (csr_rows(Ai) != n || csr_cols(A64) != n || csr_cols(Ai) != n || (Mi && ilu_n(Mi) != n))
         return fail(HGB_ERR_ARG, "ru_pcg: sizes");
@@ -897,10 +901,11 @@ extern "C" int hgb_gmres_solve(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, int restart, 
     const hgb_dtype dt = csr_dtype(A);
     if (M) {
         if (ilu_n(M) != csr_rows(A)) return fail(HGB_ERR_ARG, "gmres: preconditioner size");
-        bool ok = (dt == HGB_F64) ? (ilu_store(M) == HGB_F64) : (ilu_store(M) != HGB_F64);
-        if (!ok) return fail(HGB_ERR_ARG, "gmres: preconditioner precision does not match the matrix");
+        if (!ilu_matches(ilu_store(M), dt)) return fail(HGB_ERR_ARG, "gmres: preconditioner precision does not match the matrix");
     }
     DeviceGuard g(c->device);
+    if (dt == HGB_C128 || dt == HGB_C64)
+        return zgmres_solve(c, A, M ? ilu_zfactor(M) : nullptr, restart, bv, xv, tol, max_iter, info);
     int total = 0, outer = 0;
     double res = 0.0;
     long long launches = 0;
@@ -930,8 +935,8 @@ extern "C" int hgb_ir_gmres_solve(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu
     if (!c || !A64 || !Ai || !b || !x || restart < 1 || restart > kGmresMaxRestart)
         return fail(HGB_ERR_ARG, "ir_gmres: bad arguments (restart 1..%d)", kGmresMaxRestart);
     if (csr_dtype(A64) != HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the outer matrix must be F64");
-    if (csr_dtype(Ai) == HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the inner matrix must be F32 or BF16");
-    if (Mi && ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "ir_gmres: the inner preconditioner must store F32 or BF16");
+    if (!real_inner(csr_dtype(Ai))) return fail(HGB_ERR_ARG, "ir_gmres: the inner matrix must be F32 or BF16");
+    if (Mi && !real_inner(ilu_store(Mi))) return fail(HGB_ERR_ARG, "ir_gmres: the inner preconditioner must store F32 or BF16");
     const long n = csr_rows(A64);
     if (csr_rows(Ai) != n || csr_cols(A64) != n || csr_cols(Ai) != n || (Mi && ilu_n(Mi) != n))
         return fail(HGB_ERR_ARG, "ir_gmres: sizes");
@@ -1049,7 +1054,7 @@ static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const 
                             Solve solve) {
     if (!c || n <= 0 || nnz < 0 || !pntr_h || !indx_h || !vals_h || !b_h || !x_h || !Mi)
         return fail(HGB_ERR_ARG, "%s: bad arguments", what);
-    if (ilu_store(Mi) == HGB_F64) return fail(HGB_ERR_ARG, "%s: the preconditioner must store F32 or BF16", what);
+    if (!real_inner(ilu_store(Mi))) return fail(HGB_ERR_ARG, "%s: the preconditioner must store F32 or BF16", what);
     DeviceGuard g(c->device);
     const bool bf16 = ilu_store(Mi) == HGB_BF16;
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };

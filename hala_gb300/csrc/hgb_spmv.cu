@@ -16,6 +16,7 @@
 //    rounding of the individual products (a few ulps of the row sum).
 #include "hgb_internal.cuh"
 #include "hgb_kernels.cuh"
+#include "hgb_complex.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -565,7 +566,8 @@ int hgb_csr_create(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr,
     if (!out) return fail(HGB_ERR_ARG, "csr_create: null output");
     *out = nullptr;
     HGB_TRY(check_spmv_args(c, 'N', n_rows, n_cols, nnz, pntr, indx, vals, pntr, pntr));
-    if (dtype != HGB_F64 && dtype != HGB_F32 && dtype != HGB_BF16) return fail(HGB_ERR_ARG, "csr_create: dtype");
+    if (dtype != HGB_F64 && dtype != HGB_F32 && dtype != HGB_BF16 && dtype != HGB_C128 && dtype != HGB_C64)
+        return fail(HGB_ERR_ARG, "csr_create: dtype");
     DeviceGuard g(c->device);
     HGB_TRY(csr_check(c, n_rows, n_cols, nnz, pntr, indx));
     hgb_csr *A = new hgb_csr();
@@ -587,6 +589,10 @@ int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double bet
     HGB_TRY(check_spmv_args(c, trans, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->vals, x, y));
     DeviceGuard g(c->device);
     bool nt = (trans == 'N' || trans == 'n');
+    if (A->dtype == HGB_C128 || A->dtype == HGB_C64) {
+        const double a[2] = {alpha, 0.0}, b[2] = {beta, 0.0};
+        return hgb_csr_gemv_z(A, trans, a, x, b, y);
+    }
     if (nt) {
         switch (A->dtype) {
             case HGB_F64: return spmv_n_launch<double>(c, A->n_rows, A->pntr, A->indx, (const double *)A->vals, alpha, (const double *)x, beta, (double *)y, nullptr, nullptr);
@@ -604,8 +610,43 @@ int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double bet
     return spmv_t_launch<float>(c, A->n_rows, A->n_cols, A->pntr, A->indx, (const float *)A->vals, (float)alpha, (const float *)x, (float)beta, (float *)y, &A->T);
 }
 
+int hgb_csr_gemv_z(hgb_csr *A, char trans, const double *alpha, const void *x, const double *beta, void *y) {
+    if (!A || !alpha || !beta) return fail(HGB_ERR_ARG, "csr_gemv_z: bad arguments");
+    if (A->dtype != HGB_C128 && A->dtype != HGB_C64) return fail(HGB_ERR_ARG, "csr_gemv_z: a complex matrix");
+    hgb_ctx *c = A->ctx;
+    HGB_TRY(check_spmv_args(c, trans, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->vals, x, y));
+    DeviceGuard g(c->device);
+    const bool nt = (trans == 'N' || trans == 'n');
+    if (!nt && !A->has_T) {
+        HGB_TRY(build_transpose(c, A->n_rows, A->n_cols, A->nnz, A->pntr, A->indx, A->T));
+        A->has_T = true;
+    }
+    const Transpose *T = nt ? nullptr : &A->T;
+    if (A->dtype == HGB_C128)
+        return zspmv<double>(c, trans, A->n_rows, A->n_cols, A->pntr, A->indx, A->vals, alpha, x, beta, y, T);
+    const float a[2] = {(float)alpha[0], (float)alpha[1]}, b[2] = {(float)beta[0], (float)beta[1]};
+    return zspmv<float>(c, trans, A->n_rows, A->n_cols, A->pntr, A->indx, A->vals, a, x, b, y, T);
+}
+
+int hgb_spmv_c128(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                  const void *vals, const double *alpha, const void *x, const double *beta, void *y) {
+    HGB_TRY(check_spmv_args(c, trans, n_rows, n_cols, nnz, pntr, indx, vals, x, y));
+    if (!alpha || !beta) return fail(HGB_ERR_ARG, "spmv_c128: null scalar");
+    DeviceGuard g(c->device);
+    return zspmv<double>(c, trans, n_rows, n_cols, pntr, indx, vals, alpha, x, beta, y, nullptr);
+}
+
+int hgb_spmv_c64(hgb_ctx *c, char trans, int n_rows, int n_cols, int nnz, const int *pntr, const int *indx,
+                 const void *vals, const float *alpha, const void *x, const float *beta, void *y) {
+    HGB_TRY(check_spmv_args(c, trans, n_rows, n_cols, nnz, pntr, indx, vals, x, y));
+    if (!alpha || !beta) return fail(HGB_ERR_ARG, "spmv_c64: null scalar");
+    DeviceGuard g(c->device);
+    return zspmv<float>(c, trans, n_rows, n_cols, pntr, indx, vals, alpha, x, beta, y, nullptr);
+}
+
 int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out) {
     if (!A || !dot_out) return fail(HGB_ERR_ARG, "csr_gemv_dot: bad arguments");
+    if (A->dtype == HGB_C128 || A->dtype == HGB_C64) return fail(HGB_ERR_UNSUPPORTED, "csr_gemv_dot: real matrices");
     if (A->n_rows != A->n_cols) return fail(HGB_ERR_ARG, "csr_gemv_dot: square matrix required");
     hgb_ctx *c = A->ctx;
     DeviceGuard g(c->device);
@@ -618,7 +659,7 @@ int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out) {
 
 int hgb_csr_pattern_grad(hgb_csr *A, double alpha, const void *lam, const void *u, void *grad) {
     if (!A || !lam || !u || !grad) return fail(HGB_ERR_ARG, "csr_pattern_grad: bad arguments");
-    if (A->dtype == HGB_BF16) return fail(HGB_ERR_UNSUPPORTED, "csr_pattern_grad: F64 or F32 matrices");
+    if (A->dtype != HGB_F64 && A->dtype != HGB_F32) return fail(HGB_ERR_UNSUPPORTED, "csr_pattern_grad: F64 or F32 matrices");
     hgb_ctx *c = A->ctx;
     DeviceGuard g(c->device);
     if (A->n_rows == 0) return HGB_OK;

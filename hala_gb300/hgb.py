@@ -12,7 +12,7 @@ from . import build as _build
 
 HGB_OK, HGB_ERR_ARG, HGB_ERR_CSR, HGB_ERR_ZERO_PIVOT, HGB_ERR_TIMEOUT = 0, 1, 2, 3, 4
 HGB_ERR_NOT_CONVERGED, HGB_ERR_CUDA, HGB_ERR_ALLOC, HGB_ERR_UNSUPPORTED = 5, 6, 7, 8
-HGB_F64, HGB_F32, HGB_BF16 = 0, 1, 2
+HGB_F64, HGB_F32, HGB_BF16, HGB_C128, HGB_C64 = 0, 1, 2, 3, 4
 HGB_SPMV_FUSED, HGB_SPMV_EXACT = 0, 1
 
 
@@ -69,6 +69,19 @@ _SIGS = {
     "hgb_spmv_f64": ([vp, ch, i32, i32, i32, vp, vp, vp, f64, vp, f64, vp], i32),
     "hgb_spmv_f32": ([vp, ch, i32, i32, i32, vp, vp, vp, f32, vp, f32, vp], i32),
     "hgb_spmv_bf16f32": ([vp, ch, i32, i32, i32, vp, vp, vp, f32, vp, f32, vp], i32),
+    "hgb_spmv_c128": ([vp, ch, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp], i32),
+    "hgb_spmv_c64": ([vp, ch, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp], i32),
+    "hgb_dotc_c128": ([vp, i32, vp, vp, vp, i32], i32),
+    "hgb_dotc_c64": ([vp, i32, vp, vp, vp, i32], i32),
+    "hgb_dotu_c128": ([vp, i32, vp, vp, vp, i32], i32),
+    "hgb_dotu_c64": ([vp, i32, vp, vp, vp, i32], i32),
+    "hgb_nrm2_c128": ([vp, i32, vp, vp, i32], i32),
+    "hgb_nrm2_c64": ([vp, i32, vp, vp, i32], i32),
+    "hgb_axpy_c128": ([vp, i32, vp, vp, vp], i32),
+    "hgb_axpy_c64": ([vp, i32, vp, vp, vp], i32),
+    "hgb_scal_c128": ([vp, i32, vp, vp], i32),
+    "hgb_scal_c64": ([vp, i32, vp, vp], i32),
+    "hgb_csr_gemv_z": ([vp, ch, vp, vp, vp, vp], i32),
     "hgb_csr_create": ([vp, i32, i32, i32, vp, vp, vp, i32, C.POINTER(vp)], i32),
     "hgb_csr_gemv": ([vp, ch, f64, vp, f64, vp], i32),
     "hgb_csr_gemv_dot": ([vp, vp, vp, vp], i32),

@@ -40,7 +40,9 @@ typedef enum hgb_status {
     HGB_ERR_UNSUPPORTED = 8    /* combination not implemented (e.g. transpose on a bf16 matrix) */
 } hgb_status;
 
-typedef enum hgb_dtype { HGB_F64 = 0, HGB_F32 = 1, HGB_BF16 = 2 } hgb_dtype;
+/* Element types.  HGB_C128 / HGB_C64: complex, interleaved (real, imaginary) pairs of doubles /
+ * floats, the layout of std::complex and cuDoubleComplex / cuComplex. */
+typedef enum hgb_dtype { HGB_F64 = 0, HGB_F32 = 1, HGB_BF16 = 2, HGB_C128 = 3, HGB_C64 = 4 } hgb_dtype;
 
 /* Arithmetic of the non-transposed SpMV (and of every solver product built on it).
  * HGB_SPMV_FUSED: one fused multiply-add per entry in column order (the default; within a few
@@ -134,14 +136,45 @@ int hgb_spmv_bf16f32(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, 
                      const int *indx, const uint16_t *vals, float alpha, const float *x,
                      float beta, float *y);
 
+/* ----------------------------------------------------------- complex (C128 / C64) ---------- */
+/* The reference's templates take std::complex<double> / std::complex<float> throughout
+ * (sparse/hala_sparse_utils.hpp:104-336; gpu/hala_gpu_blas1.hpp dispatches them to cuBLAS Z / C
+ * routines).  Vectors and values are interleaved pairs; complex scalars are R[2] = {re, im}.
+ * Products and sums are separately rounded (re = ac - bd, im = ad + bc); division by Smith's
+ * method.  y = alpha op(A) x + beta y; trans 'N', 'T' or 'C' (conjugate transpose); 'T' / 'C'
+ * without a matrix handle scatter with atomics. */
+int hgb_spmv_c128(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                  const int *indx, const void *vals, const double *alpha, const void *x,
+                  const double *beta, void *y);
+int hgb_spmv_c64(hgb_ctx *ctx, char trans, int n_rows, int n_cols, int nnz, const int *pntr,
+                 const int *indx, const void *vals, const float *alpha, const void *x,
+                 const float *beta, void *y);
+/* dot (conjugated: sum conj(x_i) y_i, cublasZdotc), dotu (sum x_i y_i), nrm2 (real result).
+ * result: R[2] (R[1] for nrm2), on the device when result_on_device, else on the host
+ * (synchronises).  Sums accumulate in double. */
+int hgb_dotc_c128(hgb_ctx *ctx, int n, const void *x, const void *y, double *result, int result_on_device);
+int hgb_dotc_c64(hgb_ctx *ctx, int n, const void *x, const void *y, float *result, int result_on_device);
+int hgb_dotu_c128(hgb_ctx *ctx, int n, const void *x, const void *y, double *result, int result_on_device);
+int hgb_dotu_c64(hgb_ctx *ctx, int n, const void *x, const void *y, float *result, int result_on_device);
+int hgb_nrm2_c128(hgb_ctx *ctx, int n, const void *x, double *result, int result_on_device);
+int hgb_nrm2_c64(hgb_ctx *ctx, int n, const void *x, float *result, int result_on_device);
+/* y += alpha x, x *= alpha with complex alpha {re, im} (host); a copy is hgb_copy_f64 / _f32 over 2n reals */
+int hgb_axpy_c128(hgb_ctx *ctx, int n, const double *alpha, const void *x, void *y);
+int hgb_axpy_c64(hgb_ctx *ctx, int n, const float *alpha, const void *x, void *y);
+int hgb_scal_c128(hgb_ctx *ctx, int n, const double *alpha, void *x);
+int hgb_scal_c64(hgb_ctx *ctx, int n, const float *alpha, void *x);
+
 /* ---------------------- sparse matrix object (gpu_sparse_matrix, general.hpp:192-375) ------ */
 /* Non-owning view of pntr/indx/vals (general.hpp:202) plus cached analysis: the row tiling of
  * the SpMV kernel and, on first transposed use, a transpose that makes op='T' deterministic and
- * identical to sparse_gemv_array<'T'> (utils:113-118).  vals dtype: F64, F32 or BF16. */
+ * identical to sparse_gemv_array<'T'> (utils:113-118).  vals dtype: F64, F32, BF16, C128 or C64. */
 int hgb_csr_create(hgb_ctx *ctx, int n_rows, int n_cols, int nnz, const int *pntr,
                    const int *indx, const void *vals, hgb_dtype dtype, hgb_csr **A);
-/* gpu_sparse_matrix::gemv, general.hpp:265-277.  x/y are double for F64, float otherwise. */
+/* gpu_sparse_matrix::gemv, general.hpp:265-277.  x/y are double for F64, float for F32 / BF16, complex
+ * pairs for C128 / C64 (alpha, beta then act as real scalars).  trans 'C' conjugates complex values. */
 int hgb_csr_gemv(hgb_csr *A, char trans, double alpha, const void *x, double beta, void *y);
+/* the same with complex scalars {re, im} (doubles, also for C64 matrices); the matrix must be C128 or C64 */
+int hgb_csr_gemv_z(hgb_csr *A, char trans, const double *alpha, const void *x, const double *beta, void *y);
 /* y = A x and *dot_out (device) = <x, y> in one pass (the fused SpMV + BLAS-1 epilogue) */
 int hgb_csr_gemv_dot(hgb_csr *A, const void *x, void *y, double *dot_out_device);
 /* grad[p] = alpha * lam[i] * u[indx[p]] for every stored entry p of row i: dL/dA restricted to
@@ -178,7 +211,9 @@ int hgb_split_values_f32(hgb_ctx *ctx, char uplo, char diag, int n, const int *p
  * F64 (vectors double), F32 or BF16 (vectors float; the pivots stay FP64: each pivot's reciprocal
  * is computed in FP64 and rounded once to FP32, and the FP32 backward sweep multiplies by it).
  * policy 'L'/'N' is accepted for signature parity; level scheduling is
- * always used.  Returns HGB_ERR_ZERO_PIVOT (with a valid handle) when a pivot is exactly 0. */
+ * always used.  Returns HGB_ERR_ZERO_PIVOT (with a valid handle) when a pivot is exactly 0.
+ * Complex factors: vals_dtype = store = HGB_C128 or HGB_C64 (the IKJ order with complex operations,
+ * rows of one level factorised in parallel; the apply sweeps level by level; trans 'T' and 'C'). */
 int hgb_ilu0_create(hgb_ctx *ctx, int n, int nnz, const int *pntr, const int *indx,
                     const void *vals, hgb_dtype vals_dtype, hgb_dtype store, char policy,
                     hgb_ilu **ilu);
@@ -206,7 +241,8 @@ int hgb_ilu0_destroy(hgb_ilu *ilu);
 int hgb_tri_create(hgb_ctx *ctx, char uplo, char diag, int n, int nnz, const int *pntr,
                    const int *indx, const void *vals, hgb_dtype dtype, hgb_tri **tri);
 /* gpu_triangular_matrix::trsv, triangular.hpp:341-354: op(T) x = alpha b, with the arithmetic
- * of sparse_trsv_array (sparse/hala_sparse_utils.hpp:284-336). */
+ * of sparse_trsv_array (sparse/hala_sparse_utils.hpp:284-336).  dtype may be C128 / C64 (then
+ * alpha is real and trans 'C' conjugates). */
 int hgb_tri_solve(hgb_tri *tri, char trans, double alpha, const void *b, void *x);
 int hgb_tri_destroy(hgb_tri *tri);
 
@@ -215,7 +251,8 @@ int hgb_tri_destroy(hgb_tri *tri);
  * fused: device-resident scalars, the SpMV+dot and axpy+nrm2 fused, iterations replayed from a
  * CUDA graph.  M may be NULL (identity preconditioner).  Stop: iterations == max_iter or
  * ||r||_2 < tol (absolute, as the reference; pass tol*||b|| for a relative target).
- * Precision follows A (F64: x,b double; F32/BF16: float). */
+ * Precision follows A (F64: x,b double; F32/BF16: float).  C128 / C64 matrices: the same loop
+ * with the conjugated inner product and host scalars, as the reference's GPU path runs it. */
 int hgb_cg_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, const void *b, void *x, double tol,
                  int max_iter, hgb_solve_info *info);
 /* Same on op(A) = A^T ('T') or A ('N'): the transposed product goes through the matrix's cached
@@ -276,7 +313,8 @@ int hgb_ru_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M
  * restart cycle is one CUDA graph (one host synchronisation per cycle, where the reference
  * reads the projection back in every inner iteration, :67-72).  max_iter bounds the restarts,
  * tol is absolute on the preconditioned residual estimate, restart 1..512.  F64, F32 or BF16
- * values (A's precision; FP32 vectors for BF16) with a preconditioner of matching precision. */
+ * values (A's precision; FP32 vectors for BF16) with a preconditioner of matching precision.
+ * C128 / C64: the same loop driven from the host, projecting with the conjugated inner product. */
 int hgb_gmres_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int restart, const void *b, void *x,
                     double tol, int max_iter, hgb_solve_info *info);
 /* Mixed precision GMRES: FP64 iterative refinement (residual, update and stopping test

@@ -118,8 +118,10 @@ int main() {
               "solve_cg_ilu(mixed_engine) vs cpu_engine, 12^3: iterations within 5%, solution within 1e-8");
         std::vector<double> xu;
         stage("12^3 mixed_engine cg");
+        // the preconditioner of the mixed_engine overload receives gpu vectors
+        // (hex/solvers/hala_solvers_core.hpp:97-100), so its copy names the GPU engine
         const int itu = hala::solve_cg(mixed, hala::stop_criteria<double>(tol), p, ix, v,
-                                       [](auto const &in, auto &out) { hala::vcopy(in, out); }, b, xu);
+                                       [&](auto const &in, auto &out) { hala::vcopy(engine, in, out); }, b, xu);
         std::vector<double> xuc;
         const int itc2 = hala::solve_cg(cpu, hala::stop_criteria<double>(tol), p, ix, v,
                                         [](auto const &in, auto &out) { hala::vcopy(in, out); }, b, xuc);
