@@ -28,7 +28,9 @@ def nvcc_path():
 
 
 def _compile(src, obj, extra):
-    cmd = [nvcc_path(), "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
+    # host code without contracted multiply-adds: the host-side scalar work gives the same bits on
+    # x86 and Arm hosts
+    cmd = [nvcc_path(), "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I" + os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src), "-o", obj, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -16,7 +16,15 @@ from . import hgb as _h
 from .hgb import SolveInfo, check, ch_
 
 INT_MAX = 2**31 - 1
-_DT = {torch.float64: _h.HGB_F64, torch.float32: _h.HGB_F32, torch.bfloat16: _h.HGB_BF16}
+_DT = {torch.float64: _h.HGB_F64, torch.float32: _h.HGB_F32, torch.bfloat16: _h.HGB_BF16,
+       torch.complex128: _h.HGB_C128, torch.complex64: _h.HGB_C64}
+_CPLX = {torch.complex128: ("c128", C.c_double), torch.complex64: ("c64", C.c_float)}
+
+
+def _pair(v, ct):
+    """a complex scalar as the {re, im} array the complex entry points take"""
+    v = complex(v)
+    return (ct * 2)(v.real, v.imag)
 
 
 def _p(t):
@@ -92,16 +100,35 @@ def _sfx(t):
 
 
 def dot(engine, x, y):
-    """gpu/hala_gpu_blas1.hpp:179 (host-returned scalar)."""
+    """gpu/hala_gpu_blas1.hpp:179 (host-returned scalar; complex: conjugated, cublasZdotc)."""
     _need(x, name="x"); _need(y, x.dtype, "y")
+    if x.dtype in _CPLX:
+        sx, ct = _CPLX[x.dtype]
+        r = (ct * 2)()
+        check(getattr(_h.lib(), "hgb_dotc_" + sx)(engine.h, x.numel(), _p(x), _p(y), r, 0), "dot")
+        return complex(r[0], r[1])
     r = (C.c_double if x.dtype == torch.float64 else C.c_float)()
     check(getattr(_h.lib(), "hgb_dot_" + _sfx(x))(engine.h, x.numel(), _p(x), _p(y), C.byref(r), 0), "dot")
     return r.value
 
 
+def dotu(engine, x, y):
+    """the unconjugated complex product sum x_i y_i (gpu/hala_gpu_blas1.hpp:179, dotu)."""
+    _need(x, name="x"); _need(y, x.dtype, "y")
+    sx, ct = _CPLX[x.dtype]
+    r = (ct * 2)()
+    check(getattr(_h.lib(), "hgb_dotu_" + sx)(engine.h, x.numel(), _p(x), _p(y), r, 0), "dotu")
+    return complex(r[0], r[1])
+
+
 def norm2(engine, x):
     """gpu/hala_gpu_blas1.hpp:102."""
     _need(x, name="x")
+    if x.dtype in _CPLX:
+        sx, ct = _CPLX[x.dtype]
+        r = ct()
+        check(getattr(_h.lib(), "hgb_nrm2_" + sx)(engine.h, x.numel(), _p(x), C.byref(r), 0), "norm2")
+        return r.value
     r = (C.c_double if x.dtype == torch.float64 else C.c_float)()
     check(getattr(_h.lib(), "hgb_nrm2_" + _sfx(x))(engine.h, x.numel(), _p(x), C.byref(r), 0), "norm2")
     return r.value
@@ -110,18 +137,28 @@ def norm2(engine, x):
 def axpy(engine, alpha, x, y):
     """y += alpha x, gpu/hala_gpu_blas1.hpp:205."""
     _need(x, name="x"); _need(y, x.dtype, "y")
+    if x.dtype in _CPLX:
+        sx, ct = _CPLX[x.dtype]
+        check(getattr(_h.lib(), "hgb_axpy_" + sx)(engine.h, x.numel(), _pair(alpha, ct), _p(x), _p(y)), "axpy")
+        return
     check(getattr(_h.lib(), "hgb_axpy_" + _sfx(x))(engine.h, x.numel(), alpha, _p(x), _p(y)), "axpy")
 
 
 def scal(engine, alpha, x):
     """x *= alpha, gpu/hala_gpu_blas1.hpp:229."""
     _need(x, name="x")
+    if x.dtype in _CPLX:
+        sx, ct = _CPLX[x.dtype]
+        check(getattr(_h.lib(), "hgb_scal_" + sx)(engine.h, x.numel(), _pair(alpha, ct), _p(x)), "scal")
+        return
     check(getattr(_h.lib(), "hgb_scal_" + _sfx(x))(engine.h, x.numel(), alpha, _p(x)), "scal")
 
 
 def vcopy(engine, x, y):
     """y = x, gpu/hala_gpu_blas1.hpp:49."""
     _need(x, name="x"); _need(y, x.dtype, "y")
+    if x.dtype in _CPLX:   # interleaved pairs: a copy of 2n reals
+        x, y = torch.view_as_real(x).reshape(-1), torch.view_as_real(y).reshape(-1)
     check(getattr(_h.lib(), "hgb_copy_" + _sfx(x))(engine.h, x.numel(), _p(x), _p(y)), "vcopy")
 
 
@@ -188,6 +225,10 @@ def sparse_gemv(engine, trans, M, N, alpha, pntr, indx, vals, x, beta, y):
         st = L.hgb_spmv_f32(engine.h, t, M, N, nnz, _p(pntr), _p(indx), _p(vals), alpha, _p(x), beta, _p(y))
     elif vals.dtype == torch.bfloat16:
         st = L.hgb_spmv_bf16f32(engine.h, t, M, N, nnz, _p(pntr), _p(indx), _p(vals), alpha, _p(x), beta, _p(y))
+    elif vals.dtype in _CPLX:
+        sx, ct = _CPLX[vals.dtype]
+        st = getattr(L, "hgb_spmv_" + sx)(engine.h, t, M, N, nnz, _p(pntr), _p(indx), _p(vals), _pair(alpha, ct),
+                                          _p(x), _pair(beta, ct), _p(y))
     else:
         raise TypeError(f"unsupported value dtype {vals.dtype}")
     check(st, "sparse_gemv")
@@ -210,6 +251,10 @@ class gpu_sparse_matrix:
         self.h = h
 
     def gemv(self, trans, alpha, x, beta, y):
+        if self.dtype in _CPLX:
+            check(_h.lib().hgb_csr_gemv_z(self.h, ch_(trans), _pair(alpha, C.c_double), _p(x),
+                                          _pair(beta, C.c_double), _p(y)), "gemv")
+            return y
         check(_h.lib().hgb_csr_gemv(self.h, ch_(trans), float(alpha), _p(x), float(beta), _p(y)), "gemv")
         return y
 
@@ -260,7 +305,9 @@ class gpu_ilu:
 
     @property
     def vector_dtype(self):
-        return torch.float64 if self.store == torch.float64 else torch.float32
+        if self.store in _CPLX or self.store == torch.float64:
+            return self.store
+        return torch.float32
 
     def apply(self, x, r=None, trans="N"):
         r = torch.empty_like(x) if r is None else r
@@ -307,7 +354,8 @@ class mixed_ilu(gpu_ilu):
         import numpy as np
         pntr_h = np.ascontiguousarray(pntr_h, dtype=np.int32)
         indx_h = np.ascontiguousarray(indx_h, dtype=np.int32)
-        vdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32}[vals_h.dtype]
+        vdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+               np.dtype(np.complex128): torch.complex128, np.dtype(np.complex64): torch.complex64}[vals_h.dtype]
         vals_h = np.ascontiguousarray(vals_h)
         store = vdt if store is None else store
         self.engine = engine

@@ -13,6 +13,10 @@ requires (sparse/hala_sparse_core.hpp:45-60).
                      the two cells; a Dirichlet boundary face uses 2*k_cell (half-cell distance).
 * ``er_laplacian_batch``  independent Erdos-Renyi graph Laplacians + shift*I, block-diagonal CSR.
 * ``grf2d``          Gaussian random field with squared-exponential covariance (FFT sampling).
+* ``magnetic2d``     complex Hermitian positive definite: the 2D 5-point Laplacian with a phase on
+                     every edge (a_ij = -exp(i theta_ij), theta_ji = -theta_ij, the discrete magnetic
+                     Laplacian) plus shift*I.
+* ``helmholtz_shift`` complex non-Hermitian: a real operator plus (sigma_re + i sigma_im) I.
 """
 from __future__ import annotations
 
@@ -235,3 +239,33 @@ def random_csr(n, density, rng, with_diag=True, dominant=True, ncols=None):
     pntr = np.zeros(n + 1, np.int64)
     np.cumsum(np.bincount(r, minlength=n), out=pntr[1:])
     return pntr.astype(np.int32), c.astype(np.int32), v.astype(np.float64)
+
+
+def magnetic2d(nx, ny=None, flux=0.3, shift=0.05):
+    """Hermitian positive definite complex matrix: 5-point Laplacian whose edge (i, j) carries the
+    phase exp(i theta_ij), theta_ij = flux * (x_i + y_j) * sign, theta_ji = -theta_ij; diagonal
+    4 + shift (the Gershgorin disks stay in the right half plane)."""
+    p, i, v = poisson2d(nx, ny)
+    nxx = nx
+    vals = v.astype(np.complex128)
+    for r in range(len(p) - 1):
+        for q in range(p[r], p[r + 1]):
+            c = int(i[q])
+            if c == r:
+                vals[q] = 4.0 + shift
+            else:
+                lo, hi = min(r, c), max(r, c)
+                th = flux * ((lo % nxx) + 0.5 * (hi // nxx) + 0.25 * (hi - lo))
+                vals[q] = -np.exp(1j * th) if r < c else -np.exp(-1j * th)
+    return p, i, vals
+
+
+def helmholtz_shift(p, i, v, sigma=(0.5, 0.5)):
+    """v + (sigma_re + i sigma_im) on the diagonal, complex128."""
+    vals = np.asarray(v, np.complex128).copy()
+    s = complex(*sigma)
+    for r in range(len(p) - 1):
+        for q in range(p[r], p[r + 1]):
+            if i[q] == r:
+                vals[q] += s
+    return p, i, vals

@@ -314,7 +314,8 @@ int hgb_ru_pcg_solve_op(hgb_ctx *ctx, hgb_csr *A64, hgb_csr *A_inner, hgb_ilu *M
  * reads the projection back in every inner iteration, :67-72).  max_iter bounds the restarts,
  * tol is absolute on the preconditioned residual estimate, restart 1..512.  F64, F32 or BF16
  * values (A's precision; FP32 vectors for BF16) with a preconditioner of matching precision.
- * C128 / C64: the same loop driven from the host, projecting with the conjugated inner product. */
+ * C128 / C64: the same loop driven from the host; the projection does not conjugate (W^T r, as the
+ * reference's krylov_project, gemv 'T' at hex/solvers/hala_solvers_gmres.hpp:47-50,67-72). */
 int hgb_gmres_solve(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, int restart, const void *b, void *x,
                     double tol, int max_iter, hgb_solve_info *info);
 /* Mixed precision GMRES: FP64 iterative refinement (residual, update and stopping test

@@ -116,6 +116,40 @@ int or_ir_gmres(int n, const int *pntr, const int *indx, const double *vals, con
                 const int *diag, const float *ilu32, const double *piv, int restart, const double *b,
                 double *x, double tol, double inner_rtol, int max_inner, int max_outer, int *outer_out);
 
+#ifndef __cplusplus
+/* ------------------------------------------------------------------- complex ------------ */
+/* hala_oracle_cplx.c: suffix _z = double complex, _c = float complex (interleaved pairs, the
+ * layout of std::complex).  Scalars alpha / beta of the products are {re, im} pairs.  The same
+ * reference code as the real functions above, on std::complex values:
+ *   or_spmv         sparse_gemv_array, sparse/hala_sparse_utils.hpp:104-119 ('C' conjugates)
+ *   or_ilu_factor   factorize_ilu_array, utils:229-255 (returns first zero pivot row + 1, or 0)
+ *   or_ilu_apply    apply_ilu_array, utils:263-276;  or_ilu_apply_t: (LU)^-T / (LU)^-H
+ *   or_trsv         sparse_trsv_array, utils:284-336 (real alpha)
+ *   or_dotc, or_nrm2  hala::dot (conjugated), dznrm2 / scnrm2
+ *   or_cg           solve_cg_core + solve_cg, hex/solvers/hala_solvers_cg.hpp:92-156,207-226
+ *   or_gmres        solve_gmres, hex/solvers/hala_solvers_gmres.hpp:127-230 (unconjugated
+ *                   projection, gemv 'T' at :47-50, as the reference) */
+#define OR_CPLX_DECL(CT, RT, S)                                                                        \
+    void or_spmv_##S(char trans, int m, int ncols, const RT *alpha, const int *pntr, const int *indx,   \
+                     const CT *vals, const CT *x, const RT *beta, CT *y);                               \
+    int or_ilu_factor_##S(int n, const int *pntr, const int *indx, const int *diag, CT *ilu);          \
+    void or_ilu_apply_##S(int n, const int *pntr, const int *indx, const int *diag, const CT *ilu,     \
+                          CT *x);                                                                      \
+    void or_ilu_apply_t_##S(char trans, int n, const int *pntr, const int *indx, const int *diag,      \
+                            const CT *ilu, CT *x);                                                     \
+    void or_trsv_##S(char uplo, char diag, char trans, int n, RT alpha, const int *pntr,              \
+                     const int *indx, const CT *vals, const CT *b, CT *x);                              \
+    void or_dotc_##S(int n, const CT *x, const CT *y, RT *out);                                        \
+    RT or_nrm2_##S(int n, const CT *x);                                                                \
+    int or_cg_##S(int n, const int *pntr, const int *indx, const CT *vals, const int *diag,            \
+                  const CT *ilu, const CT *b, CT *x, RT tol, int max_iter, RT *res_out);               \
+    int or_gmres_##S(int n, const int *pntr, const int *indx, const CT *vals, const int *diag,         \
+                     const CT *ilu, int restart, const CT *b, CT *x, RT tol, int max_iter);
+OR_CPLX_DECL(double _Complex, double, z)
+OR_CPLX_DECL(float _Complex, float, c)
+#undef OR_CPLX_DECL
+#endif
+
 #ifdef __cplusplus
 }
 #endif

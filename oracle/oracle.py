@@ -308,3 +308,172 @@ def ref():
         r.ref_solve_batch_cg_ilu_d.restype = i
         _ref = r
     return _ref
+
+
+# ------------------------------------------------------------------------------ complex -----
+# C128 (numpy complex128) and C64 (complex64) through hala_oracle_cplx.c (suffix z / c) and, when
+# built, the reference's templates on std::complex (ref_*_z / ref_*_c in oracle/ref/ref_shim.cpp).
+
+def _zs(dtype):
+    dt = np.dtype(dtype)
+    if dt == np.complex128:
+        return "z", C.c_double, np.float64
+    if dt == np.complex64:
+        return "c", C.c_float, np.float32
+    raise TypeError(f"complex oracle: {dt}")
+
+
+def _vp(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _pair(v, rt):
+    v = complex(v)
+    return np.array([v.real, v.imag], rt)
+
+
+def _zbind(lib_, prefix, s, rt):
+    """argtypes of the complex entry points named prefix + name + '_' + s."""
+    i, c, vp = C.c_int, C.c_char, C.c_void_p
+    sigs = {
+        "spmv": ([c, i, i, vp, vp, vp, vp, vp, vp, vp], None),
+        "ilu_factor": ([i, vp, vp, vp, vp], i),
+        "ilu_apply": ([i, vp, vp, vp, vp, vp], None),
+        "ilu_apply_t": ([c, i, vp, vp, vp, vp, vp], None),
+        "trsv": ([c, c, c, i, rt, vp, vp, vp, vp, vp], None),
+        "dotc": ([i, vp, vp, vp], None),
+        "nrm2": ([i, vp], rt),
+        "cg": ([i, vp, vp, vp, vp, vp, vp, vp, rt, i, C.POINTER(rt)], i),
+        "gmres": ([i, vp, vp, vp, vp, vp, i, vp, vp, rt, i], i),
+    }
+    for name, (args, res) in sigs.items():
+        f = getattr(lib_, f"{prefix}{name}_{s}")
+        f.argtypes, f.restype = args, res
+
+
+_zbound = set()
+
+
+def _zlib(dtype):
+    s, rt, rnp = _zs(dtype)
+    L = lib()
+    if s not in _zbound:
+        _zbind(L, "or_", s, rt)
+        _zbound.add(s)
+    return L, s, rt, rnp
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+def zspmv(trans, m, ncols, alpha, pntr, indx, vals, x, beta, y=None):
+    L, s, rt, rnp = _zlib(vals.dtype)
+    out_len = m if trans in ("N", "n") else ncols
+    y = np.zeros(out_len, vals.dtype) if y is None else np.array(y, vals.dtype)
+    p, ix, v, xx = _i32(pntr), _i32(indx), np.ascontiguousarray(vals), np.ascontiguousarray(x, vals.dtype)
+    a, b = _pair(alpha, rnp), _pair(beta, rnp)
+    getattr(L, f"or_spmv_{s}")(_b(trans), m, ncols, _vp(a), _vp(p), _vp(ix), _vp(v), _vp(xx), _vp(b), _vp(y))
+    return y
+
+
+def zilu_factor(pntr, indx, vals, diag=None):
+    """factorize_ilu_array on complex values.  Returns (factor, diag, first zero pivot row + 1 or 0)."""
+    L, s, rt, rnp = _zlib(vals.dtype)
+    diag = diag_index(_i32(pntr), _i32(indx)) if diag is None else _i32(diag)
+    p, ix = _i32(pntr), _i32(indx)
+    f = np.array(vals, copy=True)
+    st = getattr(L, f"or_ilu_factor_{s}")(len(p) - 1, _vp(p), _vp(ix), _vp(diag), _vp(f))
+    return f, diag, st
+
+
+def zilu_apply(pntr, indx, diag, ilu, x, trans="N"):
+    L, s, rt, rnp = _zlib(ilu.dtype)
+    p, ix, d = _i32(pntr), _i32(indx), _i32(diag)
+    f = np.ascontiguousarray(ilu)
+    y = np.array(x, ilu.dtype, copy=True)
+    if trans in ("N", "n"):
+        getattr(L, f"or_ilu_apply_{s}")(len(p) - 1, _vp(p), _vp(ix), _vp(d), _vp(f), _vp(y))
+    else:
+        getattr(L, f"or_ilu_apply_t_{s}")(_b(trans), len(p) - 1, _vp(p), _vp(ix), _vp(d), _vp(f), _vp(y))
+    return y
+
+
+def ztrsv(uplo, diagc, trans, alpha, pntr, indx, vals, b):
+    L, s, rt, rnp = _zlib(vals.dtype)
+    p, ix, v = _i32(pntr), _i32(indx), np.ascontiguousarray(vals)
+    bb = np.ascontiguousarray(b, vals.dtype)
+    x = np.zeros(len(p) - 1, vals.dtype)
+    getattr(L, f"or_trsv_{s}")(_b(uplo), _b(diagc), _b(trans), len(p) - 1, float(alpha), _vp(p), _vp(ix), _vp(v),
+                               _vp(bb), _vp(x))
+    return x
+
+
+def zdotc(x, y):
+    L, s, rt, rnp = _zlib(x.dtype)
+    xx, yy = np.ascontiguousarray(x), np.ascontiguousarray(y, x.dtype)
+    out = np.zeros(2, rnp)
+    getattr(L, f"or_dotc_{s}")(len(xx), _vp(xx), _vp(yy), _vp(out))
+    return complex(out[0], out[1])
+
+
+def znrm2(x):
+    L, s, rt, rnp = _zlib(x.dtype)
+    xx = np.ascontiguousarray(x)
+    return getattr(L, f"or_nrm2_{s}")(len(xx), _vp(xx))
+
+
+def _opt(a):
+    return None if a is None else _vp(a)
+
+
+def zcg(pntr, indx, vals, b, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):
+    """solve_cg / solve_cg_ilu on complex data.  Returns (x, iterations, final ||r||)."""
+    L, s, rt, rnp = _zlib(vals.dtype)
+    p, ix, v = _i32(pntr), _i32(indx), np.ascontiguousarray(vals)
+    n = len(p) - 1
+    x = np.zeros(n, vals.dtype) if x0 is None else np.array(x0, vals.dtype, copy=True)
+    bb = np.ascontiguousarray(b, vals.dtype)
+    d = None if diag is None else _i32(diag)
+    f = None if ilu is None else np.ascontiguousarray(ilu, vals.dtype)
+    res = rt(0)
+    it = getattr(L, f"or_cg_{s}")(n, _vp(p), _vp(ix), _vp(v), _opt(d), _opt(f), _vp(bb), _vp(x), tol, max_iter,
+                                  C.byref(res))
+    return x, it, res.value
+
+
+def zgmres(pntr, indx, vals, b, restart, x0=None, tol=0.0, max_iter=2**31 - 1, diag=None, ilu=None):
+    """solve_gmres / solve_gmres_ilu on complex data.  Returns (x, total applications)."""
+    L, s, rt, rnp = _zlib(vals.dtype)
+    p, ix, v = _i32(pntr), _i32(indx), np.ascontiguousarray(vals)
+    n = len(p) - 1
+    x = np.zeros(n, vals.dtype) if x0 is None else np.array(x0, vals.dtype, copy=True)
+    bb = np.ascontiguousarray(b, vals.dtype)
+    d = None if diag is None else _i32(diag)
+    f = None if ilu is None else np.ascontiguousarray(ilu, vals.dtype)
+    it = getattr(L, f"or_gmres_{s}")(n, _vp(p), _vp(ix), _vp(v), _opt(d), _opt(f), restart, _vp(bb), _vp(x), tol,
+                                     max_iter)
+    return x, it
+
+
+_zref_bound = set()
+
+
+def zref(dtype):
+    """(library, suffix) of the reference's complex templates, or None when not built."""
+    r = ref()
+    if r is None:
+        return None
+    s, rt, rnp = _zs(dtype)
+    if s not in _zref_bound:
+        i, c, vp = C.c_int, C.c_char, C.c_void_p
+        getattr(r, f"ref_sparse_gemv_{s}").argtypes = [c, i, i, vp, vp, vp, vp, vp, vp, vp]
+        getattr(r, f"ref_factorize_ilu_{s}").argtypes = [i, vp, vp, vp, vp]
+        getattr(r, f"ref_apply_ilu_{s}").argtypes = [i, vp, vp, vp, vp, vp]
+        getattr(r, f"ref_trsv_{s}").argtypes = [c, c, c, i, rt, vp, vp, vp, vp, vp]
+        getattr(r, f"ref_solve_cg_{s}").argtypes = [i, vp, vp, vp, vp, vp, vp, vp, rt, i]
+        getattr(r, f"ref_solve_cg_{s}").restype = i
+        getattr(r, f"ref_solve_gmres_{s}").argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, rt, i]
+        getattr(r, f"ref_solve_gmres_{s}").restype = i
+        _zref_bound.add(s)
+    return r, s

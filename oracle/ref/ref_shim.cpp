@@ -14,13 +14,20 @@
  *   solve_cg               hex/solvers/hala_solvers_cg.hpp:181 (identity or ILU preconditioner)
  *   solve_gmres            hex/solvers/hala_solvers_gmres.hpp:127 (cpu_engine)
  *   solve_batch_cg         hex/solvers/hala_solvers_cg_batch.hpp (multi right-hand side)
+ * Suffixes: _d double, _f float, _z std::complex<double>, _c std::complex<float> (complex scalars
+ * of the products as {re, im} pairs, interleaved complex arrays).
  */
 #include "hala.hpp"
 #include "hala_solvers.hpp"
 
+#include <complex>
 #include <vector>
 
 namespace {
+
+using zd = std::complex<double>;
+using zf = std::complex<float>;
+template <typename T> using prec_t = hala::get_precision_type<std::vector<T>>;
 
 template <typename T>
 std::vector<T> vec(const T *p, long n) { return std::vector<T>(p, p + n); }
@@ -42,6 +49,29 @@ void gemv_t(char trans, int M, int N, T alpha, const int *pntr, const int *indx,
 }
 
 template <typename T>
+void factorize_t(int n, const int *pntr, const int *indx, const T *vals, T *ilu) {
+    auto P = vec(pntr, n + 1);
+    auto I = vec(indx, pntr[n]);
+    auto V = vec(vals, pntr[n]);
+    std::vector<int> D;
+    hala::get_diagonal_index(P, I, D);
+    std::vector<T> F;
+    hala::factorize_ilu(P, I, V, *const_cast<std::vector<int> const *>(&D), F);
+    out(F, ilu);
+}
+
+template <typename T>
+void apply_ilu_t(int n, const int *pntr, const int *indx, const int *diag, const T *ilu, T *x) {
+    auto P = vec(pntr, n + 1);
+    auto I = vec(indx, pntr[n]);
+    auto D = vec(diag, n);
+    auto F = vec(ilu, pntr[n]);
+    auto X = vec(x, n);
+    hala::apply_ilu(P, I, D, F, X);
+    out(X, x);
+}
+
+template <typename T>
 void trsv_t(char uplo, char diag, char trans, int n, T alpha, const int *pntr, const int *indx,
             const T *vals, const T *b, T *x) {
     int nnz = pntr[n];
@@ -58,7 +88,7 @@ void trsv_t(char uplo, char diag, char trans, int n, T alpha, const int *pntr, c
 /* ilu == nullptr: identity preconditioner (plain CG); else the given ILU(0) factor values */
 template <typename T>
 int cg_t(int n, const int *pntr, const int *indx, const T *vals, const int *diag, const T *ilu,
-         const T *b, T *x, T tol, int max_iter) {
+         const T *b, T *x, prec_t<T> tol, int max_iter) {
     int nnz = pntr[n];
     auto P = vec(pntr, n + 1);
     auto I = vec(indx, nnz);
@@ -68,7 +98,7 @@ int cg_t(int n, const int *pntr, const int *indx, const T *vals, const int *diag
     std::vector<int> D;
     std::vector<T> F;
     if (ilu) { D = vec(diag, n); F = vec(ilu, nnz); }
-    int it = hala::solve_cg(hala::stop_criteria<T>(tol, max_iter), P, I, V,
+    int it = hala::solve_cg(hala::stop_criteria<prec_t<T>>(tol, max_iter), P, I, V,
                             [&](std::vector<T> const &in, std::vector<T> &o) -> void {
                                 hala::vcopy(in, o);
                                 if (ilu) hala::apply_ilu(P, I, D, F, o);
@@ -80,7 +110,7 @@ int cg_t(int n, const int *pntr, const int *indx, const T *vals, const int *diag
 
 template <typename T>
 int gmres_t(int n, const int *pntr, const int *indx, const T *vals, const int *diag, const T *ilu,
-            int restart, const T *b, T *x, T tol, int max_iter) {
+            int restart, const T *b, T *x, prec_t<T> tol, int max_iter) {
     int nnz = pntr[n];
     auto P = vec(pntr, n + 1);
     auto I = vec(indx, nnz);
@@ -90,7 +120,7 @@ int gmres_t(int n, const int *pntr, const int *indx, const T *vals, const int *d
     std::vector<int> D;
     std::vector<T> F;
     if (ilu) { D = vec(diag, n); F = vec(ilu, nnz); }
-    int it = hala::solve_gmres(hala::cpu_engine(), hala::stop_criteria<T>(tol, max_iter), restart,
+    int it = hala::solve_gmres(hala::cpu_engine(), hala::stop_criteria<prec_t<T>>(tol, max_iter), restart,
                                P, I, V,
                                [&](std::vector<T> const &in, std::vector<T> &o) -> void {
                                    hala::vcopy(in, o);
@@ -228,5 +258,34 @@ int ref_solve_batch_cg_ilu_d(int n, const int *pntr, const int *indx, const doub
     out(X, x);
     return it;
 }
+
+/* complex: the same templates on std::complex (alpha / beta {re, im}; trsv's alpha real) */
+#define REF_COMPLEX(S, Z, R)                                                                            \
+    void ref_sparse_gemv_##S(char trans, int M, int N, const R *alpha, const int *pntr, const int *indx, \
+                             const Z *vals, const Z *x, const R *beta, Z *y) {                           \
+        gemv_t<Z>(trans, M, N, Z(alpha[0], alpha[1]), pntr, indx, vals, x, Z(beta[0], beta[1]), y);     \
+    }                                                                                                    \
+    void ref_factorize_ilu_##S(int n, const int *pntr, const int *indx, const Z *vals, Z *ilu) {         \
+        factorize_t<Z>(n, pntr, indx, vals, ilu);                                                        \
+    }                                                                                                    \
+    void ref_apply_ilu_##S(int n, const int *pntr, const int *indx, const int *diag, const Z *ilu,       \
+                           Z *x) {                                                                       \
+        apply_ilu_t<Z>(n, pntr, indx, diag, ilu, x);                                                     \
+    }                                                                                                    \
+    void ref_trsv_##S(char uplo, char diag, char trans, int n, R alpha, const int *pntr,                \
+                      const int *indx, const Z *vals, const Z *b, Z *x) {                                \
+        trsv_t<Z>(uplo, diag, trans, n, Z(alpha), pntr, indx, vals, b, x);                               \
+    }                                                                                                    \
+    int ref_solve_cg_##S(int n, const int *pntr, const int *indx, const Z *vals, const int *diag,        \
+                         const Z *ilu, const Z *b, Z *x, R tol, int max_iter) {                          \
+        return cg_t<Z>(n, pntr, indx, vals, diag, ilu, b, x, tol, max_iter);                             \
+    }                                                                                                    \
+    int ref_solve_gmres_##S(int n, const int *pntr, const int *indx, const Z *vals, const int *diag,     \
+                            const Z *ilu, int restart, const Z *b, Z *x, R tol, int max_iter) {          \
+        return gmres_t<Z>(n, pntr, indx, vals, diag, ilu, restart, b, x, tol, max_iter);                 \
+    }
+REF_COMPLEX(z, zd, double)
+REF_COMPLEX(c, zf, float)
+#undef REF_COMPLEX
 
 }  // extern "C"
