@@ -263,6 +263,9 @@ def other_workloads(E, eng, dev, stream, flush, peak, steps=3, warm=2):
     iters = torch.zeros(S, dtype=torch.int32, device=dev)
     rel = torch.zeros(S, dtype=torch.float64, device=dev)
 
+    # launch shape: timed on this batch before the measurement (setup, not in the timed region)
+    shape = B.autotune(gb, x, 1e-8)
+
     def batch():
         x.zero_()
         return B.solve(gb, x, rtol=1e-8, iters=iters, relres=rel)
@@ -276,6 +279,7 @@ def other_workloads(E, eng, dev, stream, flush, peak, steps=3, warm=2):
     mat_bytes = float(np.sum(it * (8 * nnz_i + 4 * (ni + 1)))) + float(np.sum(16 * ni))
     gbs = mat_bytes / (msb * 1e-3) / 1e9
     out["batch_4096"] = {"ms_per_batch": msb, "systems_per_s": S * 1e3 / msb, "rows": nt, "nnz": len(i),
+                         "launch_shape": {"block_threads": shape[0], "warp_max_n": shape[1]},
                          "max_rel_residual": float(rel.max()), "iterations_total": int(it.sum()),
                          "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                                       "frac": gbs / peak, "algorithmic_bytes": mat_bytes,

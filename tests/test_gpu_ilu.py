@@ -94,7 +94,8 @@ def test_reference_ilu_golden(eng):
     assert R.testvec(ilu.apply(T(c["x"])).cpu().numpy(), c["apply"])
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))))
+@pytest.mark.parametrize("path", sorted(f for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                                        if not os.path.basename(f).startswith("cplx_")))
 def test_gpu_matches_reference_fixture(eng, path):
     g = np.load(path)
     p, i, v = g["pntr"], g["indx"], g["vals"]
