@@ -168,6 +168,197 @@ static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, 
     return launch_check("cg iteration");
 }
 
+// ------------------------------------------------------------------ persistent CG -------
+// Unpreconditioned CG on a system whose matrix and vectors stay in L2 (the 256^2 Poisson class):
+// there the graph-replayed iteration is bound by its launches and their reductions' tails
+// (about 27 us per iteration for six launches), not by bytes.  One cooperative launch runs up to
+// kCgpChunk iterations with three grid barriers each: after the SpMV (<p, Ap> complete), after
+// the x / r update (||r||^2 complete) and after the direction update (p complete before the next
+// product).  Every CTA keeps its rows for the whole launch, writes one partial per reduction and,
+// after the barrier, sums all CTAs' partials in the same order, so every CTA takes the same
+// decision with the same bits and no CTA waits on a single finisher.  The arithmetic is the
+// graph path's (the same DotAcc partials per thread, the same separately rounded updates, the
+// product in the context's SpMV mode), with z = r, so <r, z> is ||r||^2.  Barriers are bounded:
+// a barrier that runs out of polls sets DEV_ERR_TIMEOUT and every CTA returns.
+constexpr int kCgpThreads = 256;
+constexpr int kCgpChunk = 4096;                 // iterations per launch (the barrier counter stays small)
+constexpr long kCgpMaxRows = 1L << 20;          // larger systems take the graph path
+constexpr size_t kCgpMaxBytes = 48u << 20;      // matrix + vectors resident in L2 (129 MB)
+
+// acc += v * x: separately rounded (the exact SpMV mode) or one fused multiply-add
+template <bool EXACT, typename X>
+__device__ __forceinline__ X cgp_acc(X acc, X v, X x) {
+    return EXACT ? add_rn(acc, mul_rn(v, x)) : fma(v, x, acc);
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// All CTAs of the cooperative launch arrive; false when the wait ran out (DEV_ERR_TIMEOUT set).
+__device__ __forceinline__ bool cgp_barrier(unsigned *count, unsigned target, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        int spins = 0, good = 1;
+        while (ld_acquire_u32(count) < target) {
+            if (++spins > kSpinLimit || ((spins & 1023) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT))) {
+                atomicOr(err, DEV_ERR_TIMEOUT);
+                good = 0;
+                break;
+            }
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// the sum of the G partials, in one fixed order: the same bits in every CTA
+__device__ __forceinline__ double cgp_sum(const double *part, int G) {
+    __shared__ double res;
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < G; b += blockDim.x) v[0] += __ldcg(part + b);
+    block_sum<1>(v);
+    if (threadIdx.x == 0) res = v[0];
+    __syncthreads();
+    const double r = res;
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ void cgp_partial(double v, double *part) {
+    double a[1] = {v};
+    block_sum<1>(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a[0];
+}
+
+template <typename V, typename X, bool EXACT>
+__global__ void __launch_bounds__(kCgpThreads)
+cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
+                     X *x, X *r, X *p, X *Ap, SolverScalars *s, double *part, unsigned *count, int *err) {
+    const int G = gridDim.x;
+    if (s->done) return;
+    double zr = s->zr, rrv = s->rr;
+    int it = s->it;
+    const int max_iter = s->max_iter;
+    const double tol2 = s->tol2;
+    double *partA = part, *partB = part + G;
+    const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x, stride = (long)G * blockDim.x;
+    unsigned target = 0;
+    bool done = false;
+    int k = 0;
+    for (; k < kCgpChunk; k++) {
+        // Ap = A p and <p, Ap>; p's entries of other CTAs' rows come from L2 (__ldcg)
+        DotAcc<X> pap;
+        for (long i = t0; i < n; i += stride) {
+            X acc = X(0);
+            for (int j = pntr[i]; j < pntr[i + 1]; j++) acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
+            Ap[i] = acc;
+            pap.add(p[i], acc);
+        }
+        cgp_partial(pap.get(), partA);
+        target += G;
+        if (!cgp_barrier(count, target, err)) return;
+        const double pAp = cgp_sum(partA, G);
+        // a = <r,z> / <p,Ap>; x += a p; r -= a Ap; ||r||^2
+        const X a = (X)(zr / pAp), ma = -a;
+        DotAcc<X> rr;
+        for (long i = t0; i < n; i += stride) {
+            x[i] = add_rn(x[i], mul_rn(a, p[i]));
+            const X ri = add_rn(r[i], mul_rn(ma, Ap[i]));
+            r[i] = ri;
+            rr.add(ri, ri);
+        }
+        cgp_partial(rr.get(), partB);
+        target += G;
+        if (!cgp_barrier(count, target, err)) return;
+        rrv = cgp_sum(partB, G);
+        it++;
+        done = (it >= max_iter) || (rrv < tol2) || !(rrv == rrv);
+        if (done) break;
+        // z = r: <r, z> = ||r||^2 (the same partials); p = (zr_new / zr_old) p + z
+        const X bta = (X)(rrv / zr);
+        for (long i = t0; i < n; i += stride) p[i] = add_rn(mul_rn(bta, p[i]), r[i]);
+        zr = rrv;
+        target += G;
+        if (!cgp_barrier(count, target, err)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s->it = it;
+        s->rr = rrv;
+        s->nzr = s->zr;
+        s->zr = zr;
+        s->done = done ? 1 : 0;
+    }
+}
+
+// Whether the persistent CG takes this solve, and its grid (0: not co-resident at all).
+template <typename V, typename X, bool EXACT>
+static int cgp_grid(hgb_ctx *c, long n) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, cg_persistent_kernel<V, X, EXACT>, kCgpThreads, 0) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    // about four rows per thread: fewer CTAs make cheaper barriers, the data are in L2 anyway
+    const long want = std::max<long>(1, (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads));
+    return (int)std::min<long>(want, (long)nb * c->num_sms);
+}
+
+template <typename V, typename X>
+static bool cgp_eligible(hgb_csr *A, hgb_ilu *M, bool trans) {
+    const long n = csr_rows(A);
+    const size_t bytes = (size_t)csr_nnz(A) * (sizeof(V) + 4) + (size_t)(n + 1) * 4 + (size_t)n * sizeof(X) * 5;
+    return !M && !trans && n > 0 && n <= kCgpMaxRows && bytes <= kCgpMaxBytes;
+}
+
+// Runs the loop of an initialised CgWork (r, p, the scalars' zr / it / tol2) to the end.
+template <typename V, typename X>
+static int cgp_run(hgb_ctx *c, hgb_csr *A, CgWork<X> &w, X *x, long n, long long *launches, SolverScalars &hs) {
+    const bool exact = (c->spmv_mode == HGB_SPMV_EXACT);
+    const int G = exact ? cgp_grid<V, X, true>(c, n) : cgp_grid<V, X, false>(c, n);
+    if (G < 1) return fail(HGB_ERR_UNSUPPORTED, "persistent cg: no co-resident grid");
+    double *part = nullptr;
+    unsigned *count = nullptr;
+    int st = HGB_OK;
+    if (ws_alloc(c, &part, 2 * (size_t)G) || ws_alloc(c, &count, 1)) st = cuda_fail(cudaErrorMemoryAllocation, "persistent cg");
+    const int *pntr = csr_pntr(A), *indx = csr_indx(A);
+    const V *vals = (const V *)csr_vals(A);
+    SolverScalars *s = c->scal;
+    int *err = c->err;
+    X *r = w.r, *p = w.p, *Ap = w.Ap;
+    void *args[] = {&n, &pntr, &indx, &vals, &x, &r, &p, &Ap, &s, &part, &count, &err};
+    while (!st) {
+        if (cudaMemsetAsync(count, 0, sizeof(unsigned), c->stream) != cudaSuccess) {
+            st = cuda_fail(cudaGetLastError(), "persistent cg");
+            break;
+        }
+        const void *fn = exact ? (const void *)cg_persistent_kernel<V, X, true> : (const void *)cg_persistent_kernel<V, X, false>;
+        if (cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kCgpThreads), args, 0, c->stream) != cudaSuccess) {
+            st = cuda_fail(cudaGetLastError(), "persistent cg launch");
+            break;
+        }
+        *launches += 1;
+        if (cudaMemcpyAsync(c->host_result, s, sizeof(SolverScalars), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+            cudaStreamSynchronize(c->stream) != cudaSuccess) {
+            st = cuda_fail(cudaGetLastError(), "persistent cg sync");
+            break;
+        }
+        memcpy(&hs, c->host_result, sizeof(SolverScalars));
+        if ((st = collect_dev_error(c))) break;
+        if (hs.done) break;
+    }
+    ws_free(c, part);
+    ws_free(c, count);
+    return st;
+}
+
 // Runs CG on (A, M) for b -> x (x holds the initial guess).  zero_x0: skip r = b - A x.
 // kernels per captured CG iteration: SpMV+dot, update+norm, [L solve, U solve], <r,z>, p update
 static int cg_launches_per_iter(bool precond) { return precond ? 6 : 4; }
@@ -196,6 +387,10 @@ static int cg_run(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, const X *b, X *x, double t
         copy_kernel<X><<<ew_grid(c, n), 256, 0, c->stream>>>(n, z, w.p);
         cg_rz_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 1);
         if ((st = launch_check("cg init"))) break;
+        if (cgp_eligible<V, X>(A, M, trans)) {   // small, L2-resident, unpreconditioned: one persistent launch
+            st = cgp_run<V, X>(c, A, w, x, n, launches, hs);
+            break;
+        }
         // capture ITERS_PER_GRAPH iterations
         cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
         if (cudaStreamBeginCapture(c->stream, mode)) { st = cuda_fail(cudaGetLastError(), "begin capture"); break; }

@@ -87,6 +87,36 @@ def test_cg_iteration_limit(eng, rng):
     assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-10 * np.linalg.norm(xo)
 
 
+@pytest.mark.parametrize("vdt", [torch.float64, torch.float32, torch.bfloat16])
+def test_cg_persistent_small_systems(eng, eng_fused, rng, vdt):
+    """unpreconditioned CG on an L2-resident system runs as one persistent cooperative launch
+    (three grid barriers per iteration): against the oracle's loop in both SpMV modes"""
+    p, i, v = P.poisson2d(100)
+    n = len(p) - 1
+    b = rng.uniform(-1, 1, n)
+    if vdt == torch.float64:
+        vv, bb, tol = v, b, 1e-10 * np.linalg.norm(b)
+    else:
+        vv = v.astype(np.float32)
+        bb = b.astype(np.float32)
+        tol = 1e-5 * float(np.linalg.norm(bb))
+    xo, ito, _ = O.cg(p, i, vv, bb, tol=tol)
+    gv = T(vv) if vdt != torch.bfloat16 else T(vv).to(torch.bfloat16)   # 4 and -1 are exact in bf16
+    xdt = torch.float64 if vdt == torch.float64 else torch.float32
+    for e in (eng, eng_fused):
+        x = torch.zeros(n, dtype=xdt, device=dev)
+        info = E.solve_cg_info(e, E.make_sparse_matrix(e, n, T(p), T(i), gv), None, T(bb), x, tol)
+        assert info.kernel_launches < info.iterations   # one launch per 4,096 iterations after the set-up
+        xs = x.cpu().numpy().astype(np.float64)
+        if vdt == torch.float64:
+            assert within5(info.iterations, ito), (info.iterations, ito)
+            assert np.linalg.norm(b - P.csr_matvec(p, i, v, xs)) < 2 * tol
+            assert np.linalg.norm(xs - xo) <= 1e-8 * np.linalg.norm(xo)
+        else:   # FP32 recurrences: the count within 10 %, the iterate near the oracle's
+            assert abs(info.iterations - ito) <= max(2, ito // 10), (info.iterations, ito)
+            assert np.linalg.norm(xs - xo) <= 1e-2 * np.linalg.norm(xo)
+
+
 def test_gmres_matches_oracle(eng, rng):
     p, i, v = P.convdiff3d(16)
     n = len(p) - 1
