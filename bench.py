@@ -483,6 +483,12 @@ def main():
         x.zero_()
         return E.solve_ir_pcg(eng, A64, A32, M32, gb, x, tol, inner_rtol=IR_INNER_RTOL)
 
+    M16 = E.make_ilu(eng, gp, gi, gv, store=torch.bfloat16)
+
+    def solve_mixed_bf16_store():
+        x.zero_()
+        return E.solve_ru_pcg(eng, A64, A32, M16, gb, x, tol, delta=RU_DELTA)
+
     clocks = ClockSampler(torch.cuda.current_device())
     if world > 1:
         dist.barrier()
@@ -493,6 +499,7 @@ def main():
     msmx, infmx = timed(solve_mixed, args.steps, args.warmup)
     xmx = x.clone()
     msir, infir = timed(solve_ir, args.steps, args.warmup)
+    msbs, infbs = timed(solve_mixed_bf16_store, args.steps, args.warmup)
     torch.cuda.synchronize()
 
     # ---- kernel timing for the roofline (same stream, CUDA events, L2 flushed per launch)
@@ -613,7 +620,7 @@ def main():
     resmx = float(np.linalg.norm(b - P.csr_matvec(p, i, v, xm)) / np.linalg.norm(b))
     it64 = inf64[-1].iterations
     launches = (sum(int(q.kernel_launches) for q in inf64) + sum(int(q.kernel_launches) for q in infmx)
-                + sum(int(q.kernel_launches) for q in infir))
+                + sum(int(q.kernel_launches) for q in infir) + sum(int(q.kernel_launches) for q in infbs))
     launches += 5 * 20 * 5 + 4 * 10   # kernel timing: 5 x 100 SpMV, 2 x 10 ILU applies (2 launches each)
     # dominant kernel of the headline (mixed) solve: the FP32-store triangular sweeps (ILU apply)
     ach_ilu = ib32 / (t_ilu32 * 1e-3) / 1e9
@@ -668,6 +675,9 @@ def main():
                   "err_vs_fp64": float(np.linalg.norm(xm - xs) / np.linalg.norm(xs)),
                   "err_vs_xtrue": float(np.linalg.norm(xm - xt) / np.linalg.norm(xt)), "setup_ms": setup32 * 1e3},
         "mixed_over_fp64": t_64 / t_mx,
+        "mixed_bf16_store": {"solves_per_s": 1e3 / statistics.mean(msbs), "ms_per_solve": statistics.mean(msbs),
+                             "inner_iterations": infbs[-1].iterations, "reliable_updates": infbs[-1].outer,
+                             "form": "as mixed, the ILU(0) factor stored in BF16 (FP64 pivots), FP32 operator"},
         "mixed_restarted_ir": {"solves_per_s": aggregate_rate(world, t_ir),
                                "ms_per_solve": t_ir, "inner_iterations": infir[-1].iterations,
                                "sweeps": infir[-1].outer, "inner_rtol": IR_INNER_RTOL},

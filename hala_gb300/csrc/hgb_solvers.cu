@@ -1251,7 +1251,9 @@ static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const 
         return fail(HGB_ERR_ARG, "%s: bad arguments", what);
     if (!real_inner(ilu_store(Mi))) return fail(HGB_ERR_ARG, "%s: the preconditioner must store F32 or BF16", what);
     DeviceGuard g(c->device);
-    const bool bf16 = ilu_store(Mi) == HGB_BF16;
+    // the inner operator is FP32 whatever the factor's store: BF16 values shift the operator (on the
+    // 128^3 system the rounded diagonal moves it by nine times its smallest eigenvalue) and the
+    // refinement's fixed point with it, while a BF16 factor only changes the preconditioner
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     size_t op = 0, oi = op + al(sizeof(int) * (n + 1)), ov = oi + al(sizeof(int) * (size_t)nnz);
     size_t ow = ov + al(sizeof(double) * (size_t)nnz), ob = ow + al(sizeof(float) * (size_t)nnz);
@@ -1281,7 +1283,7 @@ static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const 
         HGB_CUDA(cudaEventRecord(c->ev_out, c->copy));
         HGB_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0));   // waits on this record, not later ones
         f64_to_inner_kernel<<<ew_grid(c, m), 256, 0, c->stream>>>(
-            m, dv + o, bf16 ? nullptr : (float *)dw + o, bf16 ? (uint16_t *)dw + o : nullptr);
+            m, dv + o, (float *)dw + o, nullptr);
         HGB_TRY(launch_check("f64_to_inner_kernel"));
     }
     HGB_TRY(h2d_chunked(c, c->copy, db, b_h, sizeof(double) * n));
@@ -1290,7 +1292,7 @@ static int mixed_host_solve(hgb_ctx *c, const char *what, int n, int nnz, const 
     HGB_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0));
     hgb_csr *A64 = nullptr, *Ai = nullptr;
     HGB_TRY(hgb_csr_create(c, n, n, nnz, dp, di, dv, HGB_F64, &A64));
-    int st = hgb_csr_create(c, n, n, nnz, dp, di, dw, bf16 ? HGB_BF16 : HGB_F32, &Ai);
+    int st = hgb_csr_create(c, n, n, nnz, dp, di, dw, HGB_F32, &Ai);
     if (!st) st = solve(A64, Ai, db, dx);
     hgb_csr_destroy(A64);
     hgb_csr_destroy(Ai);

@@ -334,8 +334,9 @@ int hgb_mixed_cg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const
                        double tol, int max_iter, hgb_solve_info *info);
 
 /* Host-buffer form of hgb_ir_pcg_solve: HOST pntr/indx/vals (FP64) and b/x are loaded per call,
- * the inner matrix is converted on the device to M_inner's store precision (F32 or BF16), the
- * refinement runs as hgb_ir_pcg_solve and x is written back to the host. */
+ * the inner matrix is converted on the device to FP32 (also beside a BF16-stored M_inner: a BF16
+ * operator shifts the fixed point of the refinement, see the design notes), the refinement runs as
+ * hgb_ir_pcg_solve and x is written back to the host. */
 int hgb_mixed_ir_pcg_solve(hgb_ctx *ctx, int n, int nnz, const int *pntr_host, const int *indx_host,
                            const double *vals_host, hgb_ilu *M_inner, const double *b_host,
                            double *x_host, double tol, double inner_rtol, int max_inner,

@@ -341,15 +341,17 @@ def test_ru_pcg_iteration_limit(eng, rng):
     assert np.linalg.norm(x.cpu().numpy() - xo) <= 1e-5 * np.linalg.norm(xo)
 
 
+@pytest.mark.parametrize("store", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("solver", ["ir", "ru"])
-def test_mixed_host_buffers(eng, rng, solver):
-    # host pntr/indx/vals/b/x in, x out: the end-to-end entry points of the mixed solves
+def test_mixed_host_buffers(eng, rng, solver, store):
+    # host pntr/indx/vals/b/x in, x out: the end-to-end entry points of the mixed solves; the inner
+    # operator is FP32 also beside a BF16-stored factor
     p, i, v = P.aniso3d(20)
     n = len(p) - 1
     xt = rng.standard_normal(n)
     b = P.csr_matvec(p, i, v, xt)
     tol = 1e-10 * np.linalg.norm(b)
-    M = E.make_ilu(eng, T(p), T(i), T(v), store=torch.float32)
+    M = E.make_ilu(eng, T(p), T(i), T(v), store=store)
     x = np.zeros(n)
     if solver == "ir":
         info = E.solve_ir_pcg_mixed(eng, tol, p, i, v, M, b, x, inner_rtol=1e-4)
