@@ -177,9 +177,9 @@ static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, 
 // product).  Every CTA keeps its rows for the whole launch, writes one partial per reduction and,
 // after the barrier, sums all CTAs' partials in the same order, so every CTA takes the same
 // decision with the same bits and no CTA waits on a single finisher.  The arithmetic is the
-// graph path's (the same DotAcc partials per thread, the same separately rounded updates, the
-// product in the context's SpMV mode), with z = r, so <r, z> is ||r||^2.  Barriers are bounded:
-// a barrier that runs out of polls sets DEV_ERR_TIMEOUT and every CTA returns.
+// graph path's (DotAcc partials per thread, the same separately rounded updates, the product in
+// the context's SpMV mode), with z = r, so <r, z> is ||r||^2.  Barriers are bounded: a barrier
+// that runs out of polls sets DEV_ERR_TIMEOUT and every CTA returns.
 constexpr int kCgpThreads = 256;
 constexpr int kCgpChunk = 4096;                 // iterations per launch (the barrier counter stays small)
 constexpr long kCgpMaxRows = 1L << 20;          // larger systems take the graph path
@@ -237,7 +237,13 @@ __device__ __forceinline__ void cgp_partial(double v, double *part) {
     if (threadIdx.x == 0) part[blockIdx.x] = a[0];
 }
 
-template <typename V, typename X, bool EXACT>
+// RPT > 0: thread t owns rows t, t + stride, ... (RPT of them) for the whole launch and keeps their
+// x, r, p and (rows of at most kCgpMaxE entries) their matrix entries in registers: an iteration
+// then reads only the neighbours' p from L2.  RPT = 0: the rows are walked with grid-stride loops
+// and every vector lives in memory (systems too large for one register-resident row set).
+constexpr int kCgpMaxE = 8;
+
+template <typename V, typename X, bool EXACT, int RPT>
 __global__ void __launch_bounds__(kCgpThreads)
 cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
                      X *x, X *r, X *p, X *Ap, SolverScalars *s, double *part, unsigned *count, int *err) {
@@ -251,15 +257,63 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
     const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x, stride = (long)G * blockDim.x;
     unsigned target = 0;
     bool done = false;
-    int k = 0;
-    for (; k < kCgpChunk; k++) {
-        // Ap = A p and <p, Ap>; p's entries of other CTAs' rows come from L2 (__ldcg)
+    constexpr int K = RPT > 0 ? RPT : 1;
+    long row[K];
+    int beg[K], len[K], ci[K][kCgpMaxE];
+    X cv[K][kCgpMaxE], xr[K], rr[K], pr[K];
+    if (RPT > 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            row[k] = t0 + k * stride;
+            len[k] = 0;
+            beg[k] = 0;
+            if (row[k] < n) {
+                beg[k] = pntr[row[k]];
+                len[k] = pntr[row[k] + 1] - beg[k];
+                xr[k] = x[row[k]];
+                rr[k] = r[row[k]];
+                pr[k] = p[row[k]];
+#pragma unroll
+                for (int e = 0; e < kCgpMaxE; e++)
+                    if (e < len[k]) {
+                        ci[k][e] = indx[beg[k] + e];
+                        cv[k][e] = Val<V>::get(vals[beg[k] + e]);
+                    }
+            }
+        }
+    }
+    for (int c = 0; c < kCgpChunk; c++) {
+        // Ap = A p and <p, Ap>; the neighbours' p come from L2 (__ldcg: other CTAs wrote them)
         DotAcc<X> pap;
-        for (long i = t0; i < n; i += stride) {
-            X acc = X(0);
-            for (int j = pntr[i]; j < pntr[i + 1]; j++) acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
-            Ap[i] = acc;
-            pap.add(p[i], acc);
+        X ap[K];
+        if (RPT > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (row[k] >= n) continue;
+                X acc = X(0);
+                if (len[k] <= kCgpMaxE) {
+                    X pv[kCgpMaxE];
+#pragma unroll
+                    for (int e = 0; e < kCgpMaxE; e++)
+                        if (e < len[k]) pv[e] = __ldcg(p + ci[k][e]);
+#pragma unroll
+                    for (int e = 0; e < kCgpMaxE; e++)
+                        if (e < len[k]) acc = cgp_acc<EXACT, X>(acc, cv[k][e], pv[e]);
+                } else {
+                    for (int j = beg[k]; j < beg[k] + len[k]; j++)
+                        acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
+                }
+                ap[k] = acc;
+                pap.add(pr[k], acc);
+            }
+        } else {
+            for (long i = t0; i < n; i += stride) {
+                X acc = X(0);
+                for (int j = pntr[i]; j < pntr[i + 1]; j++)
+                    acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
+                Ap[i] = acc;
+                pap.add(p[i], acc);
+            }
         }
         cgp_partial(pap.get(), partA);
         target += G;
@@ -267,14 +321,24 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
         const double pAp = cgp_sum(partA, G);
         // a = <r,z> / <p,Ap>; x += a p; r -= a Ap; ||r||^2
         const X a = (X)(zr / pAp), ma = -a;
-        DotAcc<X> rr;
-        for (long i = t0; i < n; i += stride) {
-            x[i] = add_rn(x[i], mul_rn(a, p[i]));
-            const X ri = add_rn(r[i], mul_rn(ma, Ap[i]));
-            r[i] = ri;
-            rr.add(ri, ri);
+        DotAcc<X> rrd;
+        if (RPT > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (row[k] >= n) continue;
+                xr[k] = add_rn(xr[k], mul_rn(a, pr[k]));
+                rr[k] = add_rn(rr[k], mul_rn(ma, ap[k]));
+                rrd.add(rr[k], rr[k]);
+            }
+        } else {
+            for (long i = t0; i < n; i += stride) {
+                x[i] = add_rn(x[i], mul_rn(a, p[i]));
+                const X ri = add_rn(r[i], mul_rn(ma, Ap[i]));
+                r[i] = ri;
+                rrd.add(ri, ri);
+            }
         }
-        cgp_partial(rr.get(), partB);
+        cgp_partial(rrd.get(), partB);
         target += G;
         if (!cgp_barrier(count, target, err)) return;
         rrv = cgp_sum(partB, G);
@@ -283,10 +347,27 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
         if (done) break;
         // z = r: <r, z> = ||r||^2 (the same partials); p = (zr_new / zr_old) p + z
         const X bta = (X)(rrv / zr);
-        for (long i = t0; i < n; i += stride) p[i] = add_rn(mul_rn(bta, p[i]), r[i]);
+        if (RPT > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (row[k] >= n) continue;
+                pr[k] = add_rn(mul_rn(bta, pr[k]), rr[k]);
+                p[row[k]] = pr[k];
+            }
+        } else {
+            for (long i = t0; i < n; i += stride) p[i] = add_rn(mul_rn(bta, p[i]), r[i]);
+        }
         zr = rrv;
         target += G;
         if (!cgp_barrier(count, target, err)) return;
+    }
+    if (RPT > 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (row[k] < n) {
+                x[row[k]] = xr[k];
+                r[row[k]] = rr[k];
+            }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         s->it = it;
@@ -297,18 +378,30 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
     }
 }
 
-// Whether the persistent CG takes this solve, and its grid (0: not co-resident at all).
+// Launch shape of the persistent CG: {grid, rows per thread (0: grid-stride)}; grid 0 when no
+// co-resident grid exists.  One row per thread while that keeps the grid at about two CTAs per SM
+// (cheap barriers), two rows per thread below four CTAs per SM, else grid-stride loops.
+struct CgpShape {
+    int grid = 0, rpt = 0;
+};
 template <typename V, typename X, bool EXACT>
-static int cgp_grid(hgb_ctx *c, long n) {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, cg_persistent_kernel<V, X, EXACT>, kCgpThreads, 0) !=
-        cudaSuccess) {
+static CgpShape cgp_shape(hgb_ctx *c, long n) {
+    CgpShape sh;
+    int nb[3] = {0, 0, 0};
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], cg_persistent_kernel<V, X, EXACT, 0>, kCgpThreads, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], cg_persistent_kernel<V, X, EXACT, 1>, kCgpThreads, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], cg_persistent_kernel<V, X, EXACT, 2>, kCgpThreads, 0)) {
         cudaGetLastError();
-        return 0;
+        return sh;
     }
+    const long g1 = (n + kCgpThreads - 1) / kCgpThreads, g2 = (n + 2L * kCgpThreads - 1) / (2L * kCgpThreads);
+    if (g1 <= std::min<long>((long)nb[1] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g1, 1};
+    if (g2 <= std::min<long>((long)nb[2] * c->num_sms, 4L * c->num_sms)) return CgpShape{(int)g2, 2};
     // about four rows per thread: fewer CTAs make cheaper barriers, the data are in L2 anyway
     const long want = std::max<long>(1, (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads));
-    return (int)std::min<long>(want, (long)nb * c->num_sms);
+    sh.grid = (int)std::min<long>(want, (long)nb[0] * c->num_sms);
+    sh.rpt = 0;
+    return sh;
 }
 
 template <typename V, typename X>
@@ -318,11 +411,19 @@ static bool cgp_eligible(hgb_csr *A, hgb_ilu *M, bool trans) {
     return !M && !trans && n > 0 && n <= kCgpMaxRows && bytes <= kCgpMaxBytes;
 }
 
+template <typename V, typename X, bool EXACT>
+static const void *cgp_kernel(int rpt) {
+    return rpt == 1 ? (const void *)cg_persistent_kernel<V, X, EXACT, 1>
+                    : rpt == 2 ? (const void *)cg_persistent_kernel<V, X, EXACT, 2>
+                               : (const void *)cg_persistent_kernel<V, X, EXACT, 0>;
+}
+
 // Runs the loop of an initialised CgWork (r, p, the scalars' zr / it / tol2) to the end.
 template <typename V, typename X>
 static int cgp_run(hgb_ctx *c, hgb_csr *A, CgWork<X> &w, X *x, long n, long long *launches, SolverScalars &hs) {
     const bool exact = (c->spmv_mode == HGB_SPMV_EXACT);
-    const int G = exact ? cgp_grid<V, X, true>(c, n) : cgp_grid<V, X, false>(c, n);
+    const CgpShape sh = exact ? cgp_shape<V, X, true>(c, n) : cgp_shape<V, X, false>(c, n);
+    const int G = sh.grid;
     if (G < 1) return fail(HGB_ERR_UNSUPPORTED, "persistent cg: no co-resident grid");
     double *part = nullptr;
     unsigned *count = nullptr;
@@ -339,7 +440,7 @@ static int cgp_run(hgb_ctx *c, hgb_csr *A, CgWork<X> &w, X *x, long n, long long
             st = cuda_fail(cudaGetLastError(), "persistent cg");
             break;
         }
-        const void *fn = exact ? (const void *)cg_persistent_kernel<V, X, true> : (const void *)cg_persistent_kernel<V, X, false>;
+        const void *fn = exact ? cgp_kernel<V, X, true>(sh.rpt) : cgp_kernel<V, X, false>(sh.rpt);
         if (cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kCgpThreads), args, 0, c->stream) != cudaSuccess) {
             st = cuda_fail(cudaGetLastError(), "persistent cg launch");
             break;

@@ -48,9 +48,14 @@ __device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
     return spmv_acc<false>(mul_rn(beta, *yp), alpha, acc);
 }
 
+// CTAs per SM the register budget is held to: the FP64 staging (50 KB per CTA) allows 4, and
+// without the bound the FP64 kernel took 78 registers and ran 3 CTAs per SM (a variant with 4
+// measured 45 against 56 us per 128^3 product); FP32 / BF16 keep 48 registers, 5 CTAs, no spills
+template <typename V> constexpr int spmv_min_ctas() { return sizeof(V) == 8 ? 4 : 5; }
+
 // y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A)
 template <typename V, bool FUSE_DOT, bool EXACT>
-__global__ void __launch_bounds__(kWarpBlock)
+__global__ void __launch_bounds__(kWarpBlock, spmv_min_ctas<V>())
 spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
                  typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, typename Val<V>::X beta,
                  typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter, double *dot_out,
