@@ -230,7 +230,7 @@ int hgb_ctx_create(int device, hgb_ctx **out) {
     hgb_ctx *c = new hgb_ctx();
     c->device = device;
     cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * kMaxReduceBlocks * 64);
+    if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * kPartialsDoubles);
     if (e == cudaSuccess) e = cudaMalloc(&c->counter, sizeof(unsigned) * 8);
     if (e == cudaSuccess) e = cudaMalloc(&c->result, sizeof(double) * 8);
     if (e == cudaSuccess) e = cudaMalloc(&c->err, sizeof(int));

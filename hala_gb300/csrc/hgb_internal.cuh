@@ -37,6 +37,10 @@ int dev_error_to_status(int word);
 // Maximum number of CTAs a reduction kernel launches; bounds the partial-sum scratch.
 constexpr int kMaxReduceBlocks = 2048;
 constexpr int kReduceSlots = 4;   // values reduced together in one pass
+// the context's partials: kMaxReduceBlocks x 64 slots for the grid reductions (up to 64 values per
+// pass), then kMaxReduceBlocks per-CTA <x, y> parts of a fused SpMV whose consumer sums them
+constexpr long kSpmvPartsOffset = (long)kMaxReduceBlocks * 64;
+constexpr long kPartialsDoubles = kSpmvPartsOffset + kMaxReduceBlocks;
 
 // Scalars kept on the device by the fused solvers (one set per context).
 struct SolverScalars {
@@ -60,7 +64,7 @@ struct hgb_ctx {
     cudaStream_t stream = nullptr;
     int num_sms = 0;
     // scratch: reduction partials, counter, results, device error word, solver scalars
-    double *partials = nullptr;            // kMaxReduceBlocks * kReduceSlots
+    double *partials = nullptr;            // kPartialsDoubles: grid reductions, then the SpMV's per-CTA parts
     unsigned *counter = nullptr;           // reduction arrival counter (self-resetting)
     double *result = nullptr;              // 8 result slots
     int *err = nullptr;                    // device error word

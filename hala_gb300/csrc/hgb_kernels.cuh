@@ -138,7 +138,7 @@ int build_transpose(hgb_ctx *c, int n_rows, int n_cols, int nnz, const int *pntr
 template <typename V>
 int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
-                  typename Val<V>::X *y, double *dot_out, const int *skip = nullptr);
+                  typename Val<V>::X *y, double *dot_out, const int *skip = nullptr, int *nparts = nullptr);
 template <typename V>
 int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,

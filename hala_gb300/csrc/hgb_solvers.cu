@@ -20,13 +20,28 @@ namespace hgb {
 
 constexpr int kItersPerGraph = 16;
 
+// <p, Ap>: the SpMV's per-CTA parts summed in one order in every CTA (pap_n > 0), or the value
+// its grid reduction stored (pap_n == 0: the transposed product)
+__device__ __forceinline__ double parts_sum(const double *part, int np, double stored) {
+    if (np == 0) return stored;
+    __shared__ double res;
+    double v[1] = {0.0};
+    for (int b = threadIdx.x; b < np; b += blockDim.x) v[0] += part[b];
+    block_sum<1>(v);
+    if (threadIdx.x == 0) res = v[0];
+    __syncthreads();
+    return res;
+}
+
 template <typename X>
 __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in, SolverScalars *s,
                                  const X *__restrict__ p, const X *__restrict__ Ap, X *__restrict__ x,
-                                 X *__restrict__ r, double *partials, unsigned *counter) {
+                                 X *__restrict__ r, double *partials, unsigned *counter, const double *pap_part,
+                                 int pap_n) {
     if (s_in->done) return;
+    const double pap = parts_sum(pap_part, pap_n, s_in->pap);
     // a = <r,z> / <p,Ap>; x += a p; r -= a Ap  (axpy(a,p,x), axpy(-a,Ap,r))
-    const X a = (X)(s_in->zr / s_in->pap);
+    const X a = (X)(s_in->zr / pap);
     const X ma = -a;
     DotAcc<X> rr;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
@@ -37,6 +52,7 @@ __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in,
     }
     double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
+        s->pap = pap;
         s->rr = v[0];
         s->it += 1;
         s->done = (s->it >= s->max_iter) || (v[0] < s->tol2) || !(v[0] == v[0]);
@@ -139,19 +155,24 @@ struct CgWork {
     }
 };
 
+// y = alpha op(A) x + beta y with an optional fused <x, y>: into *dot, or (nparts, 'N' only) as
+// per-CTA parts left for the consuming kernel (*nparts: their count; 0 when *dot was written)
 template <typename V, typename X>
 static int spmv_A(hgb_ctx *c, hgb_csr *A, X alpha, const X *x, X beta, X *y, double *dot, const int *skip,
-                  bool trans = false) {
-    if (trans) return spmv_t_fused_launch<V>(A, alpha, x, beta, y, x, dot, skip);
-    return spmv_n_launch<V>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const V *)csr_vals(A), alpha, x, beta, y, dot,
-                            skip);
+                  bool trans = false, int *nparts = nullptr) {
+    if (trans) {
+        if (nparts) *nparts = 0;
+        return spmv_t_fused_launch<V>(A, alpha, x, beta, y, x, dot, skip);
+    }
+    return spmv_n_launch<V>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const V *)csr_vals(A), alpha, x, beta, y,
+                            nparts ? nullptr : dot, skip, nparts);
 }
 template <>
 int spmv_A<uint16_t, float>(hgb_ctx *c, hgb_csr *A, float alpha, const float *x, float beta, float *y, double *dot,
-                           const int *skip, bool trans) {
+                           const int *skip, bool trans, int *nparts) {
     if (trans) return fail(HGB_ERR_UNSUPPORTED, "transposed product of a bf16 matrix");
     return spmv_n_launch<uint16_t>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const uint16_t *)csr_vals(A), alpha, x,
-                                   beta, y, dot, skip);
+                                   beta, y, nparts ? nullptr : dot, skip, nparts);
 }
 
 // One CG iteration: the launches captured into the graph.
@@ -159,8 +180,10 @@ template <typename V, typename X>
 static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, long n, bool trans) {
     SolverScalars *s = c->scal;
     const int *done = &s->done;
-    HGB_TRY(spmv_A<V, X>(c, A, X(1), w.p, X(0), w.Ap, &s->pap, done, trans));
-    cg_update_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, s, w.p, w.Ap, x, w.r, c->partials, c->counter);
+    int np = 0;
+    HGB_TRY(spmv_A<V, X>(c, A, X(1), w.p, X(0), w.Ap, &s->pap, done, trans, &np));
+    cg_update_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, s, w.p, w.Ap, x, w.r, c->partials,
+                                                                           c->counter, c->partials + kSpmvPartsOffset, np);
     X *z = M ? w.z : w.r;
     if (M) HGB_TRY(ilu_apply_internal(M, trans ? 'T' : 'N', w.r, w.z, done));
     cg_rz_kernel<X><<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.r, z, c->partials, c->counter, 0);
@@ -680,9 +703,11 @@ __global__ void ru_init_kernel(SolverScalars *s, double tol2, double delta2, dou
 
 // a = <r,z>/<p,Ap>; d += a p; r -= a Ap; ||r||^2; decide whether this iteration updates
 __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict__ p, const float *__restrict__ Ap,
-                               float *__restrict__ d, float *__restrict__ r, double *partials, unsigned *counter) {
+                               float *__restrict__ d, float *__restrict__ r, double *partials, unsigned *counter,
+                               const double *pap_part, int pap_n) {
     if (s->done) return;
-    const float a = (float)(s->zr / s->pap);
+    const double pap = parts_sum(pap_part, pap_n, s->pap);
+    const float a = (float)(s->zr / pap);
     const float ma = -a;
     DotAcc<float> rr;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
@@ -694,6 +719,7 @@ __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict
     double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
         const double rr = v[0];
+        s->pap = pap;
         s->rr = rr;
         s->it += 1;
         s->rmax2 = fmax(s->rmax2, rr);
@@ -752,8 +778,10 @@ static int ru_iteration(hgb_ctx *c, hgb_csr *A64, hgb_csr *Ai, hgb_ilu *M, CgWor
                         double *r64, const double *b, long n, bool trans) {
     SolverScalars *s = c->scal;
     const int *done = &s->done;
-    HGB_TRY(spmv_A<V, float>(c, Ai, 1.0f, w.p, 0.0f, w.Ap, &s->pap, done, trans));
-    ru_step_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.p, w.Ap, d, w.r, c->partials, c->counter);
+    int np = 0;
+    HGB_TRY(spmv_A<V, float>(c, Ai, 1.0f, w.p, 0.0f, w.Ap, &s->pap, done, trans, &np));
+    ru_step_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, w.p, w.Ap, d, w.r, c->partials, c->counter,
+                                                                      c->partials + kSpmvPartsOffset, np);
     ru_fold_kernel<<<ew_grid(c, n), 256, 0, c->stream>>>(n, s, b, d, x, r64);
     HGB_TRY(spmv_A<double, double>(c, A64, -1.0, x, 1.0, r64, nullptr, &s->ru_skip, trans));
     ru_replace_kernel<<<reduce_grid(c, n, 256 * 4), 256, 0, c->stream>>>(n, s, r64, w.r, c->partials, c->counter);

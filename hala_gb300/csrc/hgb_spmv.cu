@@ -53,6 +53,19 @@ __device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
 // measured 45 against 56 us per 128^3 product); FP32 / BF16 keep 48 registers, 5 CTAs, no spills
 template <typename V> constexpr int spmv_min_ctas() { return sizeof(V) == 8 ? 4 : 5; }
 
+// The fused <x, y>: with a counter, the grid reduction into *dot_out (the last CTA adds the
+// parts); without one, each CTA's part goes to partials[blockIdx.x] and the consuming kernel sums
+// them (in one order in every CTA), which keeps the serial last-CTA step out of the product.
+__device__ __forceinline__ void spmv_dot_epilogue(double d, double *partials, unsigned *counter, double *dot_out) {
+    double dsum[1] = {d};
+    if (counter) {
+        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
+    } else {
+        block_sum<1>(dsum);
+        if (threadIdx.x == 0) partials[blockIdx.x] = dsum[0];
+    }
+}
+
 // y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A)
 template <typename V, bool FUSE_DOT, bool EXACT>
 __global__ void __launch_bounds__(kWarpBlock, spmv_min_ctas<V>())
@@ -164,10 +177,7 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
         }
     }
     cp_async_wait<0>();
-    if (FUSE_DOT) {
-        double dsum[1] = {dacc.get()};
-        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
-    }
+    if (FUSE_DOT) spmv_dot_epilogue(dacc.get(), partials, counter, dot_out);
 }
 
 // Arrays that are not 16-byte aligned cannot be staged with cp.async: one row per thread,
@@ -201,10 +211,7 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
         y[r] = out;
         if (FUSE_DOT) dacc.add(__ldg(x + r), out);
     }
-    if (FUSE_DOT) {
-        double dsum[1] = {dacc.get()};
-        grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
-    }
+    if (FUSE_DOT) spmv_dot_epilogue(dacc.get(), partials, counter, dot_out);
 }
 
 
@@ -398,9 +405,10 @@ void Transpose::release() {
 template <typename V, bool FUSE_DOT, bool EXACT>
 static int spmv_n_launch_mode(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                               typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
-                              typename Val<V>::X *y, double *dot_out, const int *skip) {
-    double *partials = FUSE_DOT ? c->partials : nullptr;
-    unsigned *counter = FUSE_DOT ? c->counter : nullptr;
+                              typename Val<V>::X *y, double *dot_out, const int *skip, int *nparts) {
+    // nparts: the per-CTA parts of <x, y> stay in the context's parts slots (their count returned)
+    double *partials = FUSE_DOT ? (nparts ? c->partials + kSpmvPartsOffset : c->partials) : nullptr;
+    unsigned *counter = (FUSE_DOT && !nparts) ? c->counter : nullptr;
     if (aligned16(vals) && aligned16(indx)) {
         // persistent grid: the resident CTAs of every SM (occupancy queried once per kernel)
         static int occ = 0;
@@ -410,11 +418,13 @@ static int spmv_n_launch_mode(hgb_ctx *c, int n_rows, const int *pntr, const int
         }
         const long tiles = ((long)n_rows + 31) / 32;
         const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, std::min(c->num_sms * occ, kMaxReduceBlocks)));
+        if (nparts) *nparts = g;
         spmv_warp_kernel<V, FUSE_DOT, EXACT><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
                                                                             partials, counter, dot_out, skip);
         return launch_check("spmv_warp_kernel");
     }
     const int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
+    if (nparts) *nparts = g;
     spmv_direct_kernel<V, FUSE_DOT, EXACT><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, partials,
                                                                    counter, dot_out, skip);
     return launch_check("spmv_direct_kernel");
@@ -423,22 +433,23 @@ static int spmv_n_launch_mode(hgb_ctx *c, int n_rows, const int *pntr, const int
 template <typename V>
 int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
-                  typename Val<V>::X *y, double *dot_out, const int *skip) {
+                  typename Val<V>::X *y, double *dot_out, const int *skip, int *nparts) {
+    if (nparts) *nparts = 0;
     if (n_rows <= 0) return HGB_OK;
     const bool exact = c->spmv_mode == HGB_SPMV_EXACT;
-    if (dot_out)
-        return exact ? spmv_n_launch_mode<V, true, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip)
-                     : spmv_n_launch_mode<V, true, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip);
-    return exact ? spmv_n_launch_mode<V, false, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip)
-                 : spmv_n_launch_mode<V, false, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip);
+    if (dot_out || nparts)
+        return exact ? spmv_n_launch_mode<V, true, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nparts)
+                     : spmv_n_launch_mode<V, true, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nparts);
+    return exact ? spmv_n_launch_mode<V, false, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr)
+                 : spmv_n_launch_mode<V, false, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr);
 }
 
 template int spmv_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, double,
-                                   const double *, double, double *, double *, const int *);
+                                   const double *, double, double *, double *, const int *, int *);
 template int spmv_n_launch<float>(hgb_ctx *, int, const int *, const int *, const float *, float,
-                                  const float *, float, float *, double *, const int *);
+                                  const float *, float, float *, double *, const int *, int *);
 template int spmv_n_launch<uint16_t>(hgb_ctx *, int, const int *, const int *, const uint16_t *, float,
-                                     const float *, float, float *, double *, const int *);
+                                     const float *, float, float *, double *, const int *, int *);
 
 template <typename V>
 int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,
