@@ -20,6 +20,11 @@ namespace hgb {
 
 constexpr int kItersPerGraph = 16;
 
+// Elements a thread takes per round in the CG vector kernels, their loads issued together: the
+// kernels are short and latency-bound (about 14 elements per thread at 128^3), so one element per
+// round left a thread waiting on one memory round trip per element.
+template <typename X> constexpr int ew_unroll() { return sizeof(X) == 8 ? 4 : 8; }
+
 // <p, Ap>: the SpMV's per-CTA parts summed in one order in every CTA (pap_n > 0), or the value
 // its grid reduction stored (pap_n == 0: the transposed product)
 __device__ __forceinline__ double parts_sum(const double *part, int np, double stored) {
@@ -44,11 +49,30 @@ __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in,
     const X a = (X)(s_in->zr / pap);
     const X ma = -a;
     DotAcc<X> rr;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        x[i] = add_rn(x[i], mul_rn(a, p[i]));
-        X ri = add_rn(r[i], mul_rn(ma, Ap[i]));
-        r[i] = ri;
-        rr.add(ri, ri);
+    constexpr int U = ew_unroll<X>();
+    const long T = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
+        X pv[U], av[U], xv[U], rv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                pv[u] = p[i];
+                av[u] = Ap[i];
+                xv[u] = x[i];
+                rv[u] = r[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                x[i] = add_rn(xv[u], mul_rn(a, pv[u]));
+                const X ri = add_rn(rv[u], mul_rn(ma, av[u]));
+                r[i] = ri;
+                rr.add(ri, ri);
+            }
+        }
     }
     double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
@@ -64,10 +88,25 @@ __global__ void cg_rz_kernel(long n, SolverScalars *s, const X *__restrict__ r, 
                              double *partials, unsigned *counter, int init) {
     if (!init && s->done) return;
     DotAcc<X> rz, rr;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const X ri = r[i];
-        rz.add(ri, z[i]);
-        if (init) rr.add(ri, ri);
+    constexpr int U = ew_unroll<X>();
+    const long T = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
+        X rv[U], zv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                rv[u] = r[i];
+                zv[u] = z[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (base + u * T < n) {
+                rz.add(rv[u], zv[u]);
+                if (init) rr.add(rv[u], rv[u]);
+            }
+        }
     }
     double acc[2] = {rz.get(), rr.get()};
     grid_sum<2>(acc, partials, counter, [&](double (&v)[2]) {
@@ -89,8 +128,24 @@ template <typename X>
 __global__ void cg_p_kernel(long n, const SolverScalars *__restrict__ s, X *__restrict__ p, const X *__restrict__ z) {
     if (s->done) return;
     const X bta = (X)(s->zr / s->nzr);
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        p[i] = add_rn(mul_rn(bta, p[i]), z[i]);
+    constexpr int U = ew_unroll<X>();
+    const long T = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
+        X pv[U], zv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                pv[u] = p[i];
+                zv[u] = z[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) p[i] = add_rn(mul_rn(bta, pv[u]), zv[u]);
+        }
+    }
 }
 
 __global__ void cg_init_kernel(SolverScalars *s, double tol2, double rel, int max_iter) {
@@ -710,11 +765,30 @@ __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict
     const float a = (float)(s->zr / pap);
     const float ma = -a;
     DotAcc<float> rr;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        d[i] = __fadd_rn(d[i], __fmul_rn(a, p[i]));
-        const float ri = __fadd_rn(r[i], __fmul_rn(ma, Ap[i]));
-        r[i] = ri;
-        rr.add(ri, ri);
+    constexpr int U = ew_unroll<float>();
+    const long T = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
+        float pv[U], av[U], dv[U], rv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                pv[u] = p[i];
+                av[u] = Ap[i];
+                dv[u] = d[i];
+                rv[u] = r[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                d[i] = __fadd_rn(dv[u], __fmul_rn(a, pv[u]));
+                const float ri = __fadd_rn(rv[u], __fmul_rn(ma, av[u]));
+                r[i] = ri;
+                rr.add(ri, ri);
+            }
+        }
     }
     double acc[1] = {rr.get()};
     grid_sum<1>(acc, partials, counter, [&](double (&v)[1]) {
@@ -769,8 +843,24 @@ __global__ void ru_p_kernel(long n, const SolverScalars *__restrict__ s, float *
                             const float *__restrict__ z) {
     if (s->done) return;
     const float bta = s->restart ? 0.0f : (float)(s->zr / s->nzr);
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        p[i] = __fadd_rn(__fmul_rn(bta, p[i]), z[i]);
+    constexpr int U = ew_unroll<float>();
+    const long T = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
+        float pv[U], zv[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) {
+                pv[u] = p[i];
+                zv[u] = z[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const long i = base + u * T;
+            if (i < n) p[i] = __fadd_rn(__fmul_rn(bta, pv[u]), zv[u]);
+        }
+    }
 }
 
 template <typename V>
