@@ -280,8 +280,8 @@ __device__ __forceinline__ bool cgp_barrier(unsigned *count, unsigned target, in
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(count, 1u);
+        // release at GPU scope, cumulative over the CTA's writes that the bar.sync ordered before it
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
         int spins = 0, good = 1;
         while (ld_acquire_u32(count) < target) {
             if (++spins > kSpinLimit || ((spins & 1023) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT))) {
@@ -457,8 +457,9 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
 }
 
 // Launch shape of the persistent CG: {grid, rows per thread (0: grid-stride)}; grid 0 when no
-// co-resident grid exists.  One row per thread while that keeps the grid at about two CTAs per SM
-// (cheap barriers), two rows per thread below four CTAs per SM, else grid-stride loops.
+// co-resident grid exists.  One row per thread while that needs at most one CTA per SM, else two
+// rows per thread up to two CTAs per SM (every CTA costs each barrier one more arrival on the
+// counter), else grid-stride loops.
 struct CgpShape {
     int grid = 0, rpt = 0;
 };
@@ -473,8 +474,8 @@ static CgpShape cgp_shape(hgb_ctx *c, long n) {
         return sh;
     }
     const long g1 = (n + kCgpThreads - 1) / kCgpThreads, g2 = (n + 2L * kCgpThreads - 1) / (2L * kCgpThreads);
-    if (g1 <= std::min<long>((long)nb[1] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g1, 1};
-    if (g2 <= std::min<long>((long)nb[2] * c->num_sms, 4L * c->num_sms)) return CgpShape{(int)g2, 2};
+    if (g1 <= std::min<long>((long)nb[1] * c->num_sms, (long)c->num_sms)) return CgpShape{(int)g1, 1};
+    if (g2 <= std::min<long>((long)nb[2] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g2, 2};
     // about four rows per thread: fewer CTAs make cheaper barriers, the data are in L2 anyway
     const long want = std::max<long>(1, (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads));
     sh.grid = (int)std::min<long>(want, (long)nb[0] * c->num_sms);
