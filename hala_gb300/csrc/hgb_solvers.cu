@@ -23,7 +23,7 @@ constexpr int kItersPerGraph = 16;
 // Elements a thread takes per round in the CG vector kernels, their loads issued together: the
 // kernels are short and latency-bound (about 14 elements per thread at 128^3), so one element per
 // round left a thread waiting on one memory round trip per element.
-template <typename X> constexpr int ew_unroll() { return sizeof(X) == 8 ? 4 : 8; }
+template <typename X> __host__ __device__ constexpr int ew_unroll() { return sizeof(X) == 8 ? 4 : 8; }
 
 // <p, Ap>: the SpMV's per-CTA parts summed in one order in every CTA (pap_n > 0), or the value
 // its grid reduction stored (pap_n == 0: the transposed product)
