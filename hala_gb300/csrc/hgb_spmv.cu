@@ -48,10 +48,10 @@ __device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
     return spmv_acc<false>(mul_rn(beta, *yp), alpha, acc);
 }
 
-// CTAs per SM the register budget is held to: the FP64 staging (50 KB per CTA) allows 4, and
-// without the bound the FP64 kernel took 78 registers and ran 3 CTAs per SM (a variant with 4
-// measured 45 against 56 us per 128^3 product); FP32 / BF16 keep 48 registers, 5 CTAs, no spills
-template <typename V> constexpr int spmv_min_ctas() { return sizeof(V) == 8 ? 4 : 5; }
+// CTAs per SM the register budget is held to (FP32 / BF16: 48 registers, 5 CTAs, no spills).  The
+// FP64 kernel keeps its 78 registers and 3 CTAs per SM: held to 64 registers and 4 CTAs it measured
+// slower on the 128^3 product (62.5 against 56 us)
+template <typename V> constexpr int spmv_min_ctas() { return sizeof(V) == 8 ? 3 : 5; }
 
 // The fused <x, y>: with a counter, the grid reduction into *dot_out (the last CTA adds the
 // parts); without one, each CTA's part goes to partials[blockIdx.x] and the consuming kernel sums
