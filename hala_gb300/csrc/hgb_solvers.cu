@@ -23,7 +23,12 @@ constexpr int kItersPerGraph = 16;
 // Elements a thread takes per round in the CG vector kernels, their loads issued together: the
 // kernels are short and latency-bound (about 14 elements per thread at 128^3), so one element per
 // round left a thread waiting on one memory round trip per element.
-template <typename X> __host__ __device__ constexpr int ew_unroll() { return sizeof(X) == 8 ? 4 : 8; }
+template <typename X, int NARR = 2> __host__ __device__ constexpr int ew_unroll() {
+    return (sizeof(X) == 8 ? 4 : 8) / (NARR > 2 ? 2 : 1);   // NARR: vectors read per element
+}
+// their grids are num_sms x 4 CTAs of 256 threads: the register budget keeps all four resident
+// (unbounded, the batched loads took up to 86 registers and the grid ran in two waves)
+constexpr int kEwThreads = 256, kEwCtasPerSm = 4;
 
 // <p, Ap>: the SpMV's per-CTA parts summed in one order in every CTA (pap_n > 0), or the value
 // its grid reduction stored (pap_n == 0: the transposed product)
@@ -39,7 +44,7 @@ __device__ __forceinline__ double parts_sum(const double *part, int np, double s
 }
 
 template <typename X>
-__global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in, SolverScalars *s,
+__global__ void __launch_bounds__(kEwThreads, kEwCtasPerSm) cg_update_kernel(long n, const SolverScalars *__restrict__ s_in, SolverScalars *s,
                                  const X *__restrict__ p, const X *__restrict__ Ap, X *__restrict__ x,
                                  X *__restrict__ r, double *partials, unsigned *counter, const double *pap_part,
                                  int pap_n) {
@@ -49,7 +54,7 @@ __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in,
     const X a = (X)(s_in->zr / pap);
     const X ma = -a;
     DotAcc<X> rr;
-    constexpr int U = ew_unroll<X>();
+    constexpr int U = ew_unroll<X, 4>();
     const long T = (long)gridDim.x * blockDim.x;
     for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
         X pv[U], av[U], xv[U], rv[U];
@@ -84,7 +89,7 @@ __global__ void cg_update_kernel(long n, const SolverScalars *__restrict__ s_in,
 }
 
 template <typename X>
-__global__ void cg_rz_kernel(long n, SolverScalars *s, const X *__restrict__ r, const X *__restrict__ z,
+__global__ void __launch_bounds__(kEwThreads, kEwCtasPerSm) cg_rz_kernel(long n, SolverScalars *s, const X *__restrict__ r, const X *__restrict__ z,
                              double *partials, unsigned *counter, int init) {
     if (!init && s->done) return;
     DotAcc<X> rz, rr;
@@ -125,7 +130,7 @@ __global__ void cg_rz_kernel(long n, SolverScalars *s, const X *__restrict__ r, 
 
 // p = (zr_new / zr_old) p + z   (scal(a, p); axpy(1, z, p))
 template <typename X>
-__global__ void cg_p_kernel(long n, const SolverScalars *__restrict__ s, X *__restrict__ p, const X *__restrict__ z) {
+__global__ void __launch_bounds__(kEwThreads, kEwCtasPerSm) cg_p_kernel(long n, const SolverScalars *__restrict__ s, X *__restrict__ p, const X *__restrict__ z) {
     if (s->done) return;
     const X bta = (X)(s->zr / s->nzr);
     constexpr int U = ew_unroll<X>();
@@ -758,7 +763,7 @@ __global__ void ru_init_kernel(SolverScalars *s, double tol2, double delta2, dou
 }
 
 // a = <r,z>/<p,Ap>; d += a p; r -= a Ap; ||r||^2; decide whether this iteration updates
-__global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict__ p, const float *__restrict__ Ap,
+__global__ void __launch_bounds__(kEwThreads, kEwCtasPerSm) ru_step_kernel(long n, SolverScalars *s, const float *__restrict__ p, const float *__restrict__ Ap,
                                float *__restrict__ d, float *__restrict__ r, double *partials, unsigned *counter,
                                const double *pap_part, int pap_n) {
     if (s->done) return;
@@ -766,7 +771,7 @@ __global__ void ru_step_kernel(long n, SolverScalars *s, const float *__restrict
     const float a = (float)(s->zr / pap);
     const float ma = -a;
     DotAcc<float> rr;
-    constexpr int U = ew_unroll<float>();
+    constexpr int U = ew_unroll<float, 4>();
     const long T = (long)gridDim.x * blockDim.x;
     for (long base = blockIdx.x * (long)blockDim.x + threadIdx.x; base < n; base += T * U) {
         float pv[U], av[U], dv[U], rv[U];
@@ -840,7 +845,7 @@ __global__ void ru_replace_kernel(long n, SolverScalars *s, const double *__rest
 }
 
 // p = beta p + z with beta = <r,z> / <r,z>_old, or p = z after a restart
-__global__ void ru_p_kernel(long n, const SolverScalars *__restrict__ s, float *__restrict__ p,
+__global__ void __launch_bounds__(kEwThreads, kEwCtasPerSm) ru_p_kernel(long n, const SolverScalars *__restrict__ s, float *__restrict__ p,
                             const float *__restrict__ z) {
     if (s->done) return;
     const float bta = s->restart ? 0.0f : (float)(s->zr / s->nzr);

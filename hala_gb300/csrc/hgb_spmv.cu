@@ -48,11 +48,6 @@ __device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
     return spmv_acc<false>(mul_rn(beta, *yp), alpha, acc);
 }
 
-// CTAs per SM the register budget is held to (FP32 / BF16: 48 registers, 5 CTAs, no spills).  The
-// FP64 kernel keeps its 78 registers and 3 CTAs per SM: held to 64 registers and 4 CTAs it measured
-// slower on the 128^3 product (62.5 against 56 us)
-template <typename V> constexpr int spmv_min_ctas() { return sizeof(V) == 8 ? 3 : 5; }
-
 // The fused <x, y>: with a counter, the grid reduction into *dot_out (the last CTA adds the
 // parts); without one, each CTA's part goes to partials[blockIdx.x] and the consuming kernel sums
 // them (in one order in every CTA), which keeps the serial last-CTA step out of the product.
@@ -68,7 +63,7 @@ __device__ __forceinline__ void spmv_dot_epilogue(double d, double *partials, un
 
 // y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A)
 template <typename V, bool FUSE_DOT, bool EXACT>
-__global__ void __launch_bounds__(kWarpBlock, spmv_min_ctas<V>())
+__global__ void __launch_bounds__(kWarpBlock)
 spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
                  typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, typename Val<V>::X beta,
                  typename Val<V>::X *__restrict__ y, double *partials, unsigned *counter, double *dot_out,
