@@ -320,7 +320,7 @@ __device__ __forceinline__ void cgp_partial(double v, double *part) {
     if (threadIdx.x == 0) part[blockIdx.x] = a[0];
 }
 
-// RPT > 0: thread t owns rows t, t + stride, ... (RPT of them, 2 or 4) for the whole launch and keeps their
+// RPT > 0: thread t owns rows t, t + stride, ... (RPT of them: 1, 2 or 4) for the whole launch and keeps their
 // x, r, p and (rows of at most kCgpMaxE entries) their matrix entries in registers: an iteration
 // then reads only the neighbours' p from L2.  RPT = 0: the rows are walked with grid-stride loops
 // and every vector lives in memory (systems too large for one register-resident row set).
@@ -462,25 +462,29 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
 }
 
 // Launch shape of the persistent CG: {grid, rows per thread (0: grid-stride)}; grid 0 when no
-// co-resident grid exists.  Four rows per thread while that needs at most one CTA per SM (every
-// CTA costs each barrier one more arrival on the counter and each reduction one more part), else
-// two rows per thread up to two CTAs per SM, else grid-stride loops.
+// co-resident grid exists.  Every CTA costs each barrier one more arrival on the counter and each
+// reduction one more part, every row of a thread one more serial stretch of its phase: one row per
+// thread up to one CTA per SM, two up to two CTAs per SM, four up to two, else grid-stride loops.
+// (256^2 Poisson: 11.1 us per iteration with two rows per thread on 128 CTAs, 13.2 with four on 64.)
 struct CgpShape {
     int grid = 0, rpt = 0;
 };
 template <typename V, typename X, bool EXACT>
 static CgpShape cgp_shape(hgb_ctx *c, long n) {
     CgpShape sh;
-    int nb[3] = {0, 0, 0};
+    int nb[4] = {0, 0, 0, 0};
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], cg_persistent_kernel<V, X, EXACT, 0>, kCgpThreads, 0) ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], cg_persistent_kernel<V, X, EXACT, 2>, kCgpThreads, 0) ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], cg_persistent_kernel<V, X, EXACT, 4>, kCgpThreads, 0)) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], cg_persistent_kernel<V, X, EXACT, 1>, kCgpThreads, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], cg_persistent_kernel<V, X, EXACT, 2>, kCgpThreads, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[3], cg_persistent_kernel<V, X, EXACT, 4>, kCgpThreads, 0)) {
         cudaGetLastError();
         return sh;
     }
-    const long g4 = (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads), g2 = (n + 2L * kCgpThreads - 1) / (2L * kCgpThreads);
-    if (g4 <= std::min<long>((long)nb[2] * c->num_sms, (long)c->num_sms)) return CgpShape{(int)g4, 4};
-    if (g2 <= std::min<long>((long)nb[1] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g2, 2};
+    const long g1 = (n + kCgpThreads - 1) / kCgpThreads;
+    const long g2 = (n + 2L * kCgpThreads - 1) / (2L * kCgpThreads), g4 = (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads);
+    if (g1 <= std::min<long>((long)nb[1] * c->num_sms, (long)c->num_sms)) return CgpShape{(int)g1, 1};
+    if (g2 <= std::min<long>((long)nb[2] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g2, 2};
+    if (g4 <= std::min<long>((long)nb[3] * c->num_sms, 2L * c->num_sms)) return CgpShape{(int)g4, 4};
     // about four rows per thread: fewer CTAs make cheaper barriers, the data are in L2 anyway
     const long want = std::max<long>(1, (n + 4L * kCgpThreads - 1) / (4L * kCgpThreads));
     sh.grid = (int)std::min<long>(want, (long)nb[0] * c->num_sms);
@@ -497,9 +501,10 @@ static bool cgp_eligible(hgb_csr *A, hgb_ilu *M, bool trans) {
 
 template <typename V, typename X, bool EXACT>
 static const void *cgp_kernel(int rpt) {
-    return rpt == 4 ? (const void *)cg_persistent_kernel<V, X, EXACT, 4>
-                    : rpt == 2 ? (const void *)cg_persistent_kernel<V, X, EXACT, 2>
-                               : (const void *)cg_persistent_kernel<V, X, EXACT, 0>;
+    return rpt == 1   ? (const void *)cg_persistent_kernel<V, X, EXACT, 1>
+           : rpt == 2 ? (const void *)cg_persistent_kernel<V, X, EXACT, 2>
+           : rpt == 4 ? (const void *)cg_persistent_kernel<V, X, EXACT, 4>
+                      : (const void *)cg_persistent_kernel<V, X, EXACT, 0>;
 }
 
 // Runs the loop of an initialised CgWork (r, p, the scalars' zr / it / tol2) to the end.
