@@ -329,8 +329,18 @@ def other_workloads(E, eng, dev, stream, flush, peak, steps=3, warm=2):
         return fi, ai
     msfa, (fi, ai) = _events_ms(stream, forward_adjoint, 2, 1)
     launches += 3 * (int(fi.kernel_launches) + int(ai.kernel_launches))
+    # the same forward solve in plain FP64 (ILU(0)-PCG, FP64 factor), for the mixed-vs-FP64 comparison
+    M64 = E.make_ilu(eng, gp, gi, gv)
+
+    def forward64():
+        u.zero_()
+        return E.solve_cg_info(eng, A64, M64, f, u, tol, max_iter=20000)
+    ms64f, fi64 = _events_ms(stream, forward64, 2, 1)
+    launches += 3 * int(fi64.kernel_launches)
+    del M64
     res = float(np.linalg.norm(1.0 - P.csr_matvec(p, i, v, u.cpu().numpy())) / np.sqrt(n))
-    out["adjoint_vardiff512"] = {"ms_forward_plus_adjoint": msfa, "ms_forward": statistics.median(fw["fwd"][1:]),
+    out["adjoint_vardiff512"] = {"ms_forward_fp64_pcg": ms64f, "forward_fp64_iterations": fi64.iterations,
+                                 "ms_forward_plus_adjoint": msfa, "ms_forward": statistics.median(fw["fwd"][1:]),
                                  "ms_adjoint": statistics.median(fw["adj"][1:]), "forward_iterations": fi.iterations,
                                  "adjoint_iterations": ai.iterations, "forward_rel_residual": res, "n": n,
                                  "loss": float(torch.sum((u - ut) ** 2))}
