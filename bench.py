@@ -439,9 +439,10 @@ def main():
     torch.cuda.synchronize()
     setup64 = time.perf_counter() - t0
     t0 = time.perf_counter()
-    M32 = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
+    M16 = E.make_ilu(eng, gp, gi, gv, store=torch.bfloat16)
     torch.cuda.synchronize()
-    setup32 = time.perf_counter() - t0
+    setup16 = time.perf_counter() - t0
+    M32 = E.make_ilu(eng, gp, gi, gv, store=torch.float32)
     flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
     if args.kernels_only:
@@ -460,6 +461,8 @@ def main():
             M64.apply(gb, y64)
             flush_l2(flush)
             M32.apply(xs32, y32)
+            flush_l2(flush)
+            M16.apply(xs32, y32)
         torch.cuda.synchronize()
         print(json.dumps({"kernels_only": True, "n": n, "nnz": nnz}))
         return
@@ -485,19 +488,19 @@ def main():
         x.zero_()
         return E.solve_cg_info(eng, A64, M64, gb, x, tol)
 
+    # the headline mixed form: FP32 operator and vectors, the ILU(0) factor stored in BF16 (FP64
+    # pivots), FP64 reliable updates; the same with an FP32-stored factor beside it
     def solve_mixed():
         x.zero_()
-        return E.solve_ru_pcg(eng, A64, A32, M32, gb, x, tol, delta=RU_DELTA)
+        return E.solve_ru_pcg(eng, A64, A32, M16, gb, x, tol, delta=RU_DELTA)
 
     def solve_ir():
         x.zero_()
         return E.solve_ir_pcg(eng, A64, A32, M32, gb, x, tol, inner_rtol=IR_INNER_RTOL)
 
-    M16 = E.make_ilu(eng, gp, gi, gv, store=torch.bfloat16)
-
-    def solve_mixed_bf16_store():
+    def solve_mixed_f32_store():
         x.zero_()
-        return E.solve_ru_pcg(eng, A64, A32, M16, gb, x, tol, delta=RU_DELTA)
+        return E.solve_ru_pcg(eng, A64, A32, M32, gb, x, tol, delta=RU_DELTA)
 
     clocks = ClockSampler(torch.cuda.current_device())
     if world > 1:
@@ -509,7 +512,7 @@ def main():
     msmx, infmx = timed(solve_mixed, args.steps, args.warmup)
     xmx = x.clone()
     msir, infir = timed(solve_ir, args.steps, args.warmup)
-    msbs, infbs = timed(solve_mixed_bf16_store, args.steps, args.warmup)
+    msbs, infbs = timed(solve_mixed_f32_store, args.steps, args.warmup)
     torch.cuda.synchronize()
 
     # ---- kernel timing for the roofline (same stream, CUDA events, L2 flushed per launch)
@@ -556,6 +559,7 @@ def main():
     eng.set_spmv_mode("fused")
     t_ilu64 = kernel_ms(lambda: M64.apply(gb, y64))
     t_ilu32 = kernel_ms(lambda: M32.apply(xs32, y32))
+    t_ilu16 = kernel_ms(lambda: M16.apply(xs32, y32))
     clk = clocks.stop()
 
     # ---- end to end through the host-buffer entry points (pinned host memory)
@@ -567,7 +571,7 @@ def main():
         hx[:] = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E.solve_ru_pcg_mixed(eng, tol, hp, hi, hv, M32, hb_, hx, delta=RU_DELTA)
+        E.solve_ru_pcg_mixed(eng, tol, hp, hi, hv, M16, hb_, hx, delta=RU_DELTA)
         if k >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     h2d = 4 * (n + 1) + 4 * nnz + 8 * nnz + 8 * n + 8 * n
@@ -580,7 +584,7 @@ def main():
         hx[:] = 0.0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Mh = E.make_ilu_host(eng, hp, hi, hv, store=torch.float32)
+        Mh = E.make_ilu_host(eng, hp, hi, hv, store=torch.bfloat16)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         E.solve_ru_pcg_mixed(eng, tol, hp, hi, hv, Mh, hb_, hx, delta=RU_DELTA)
@@ -623,6 +627,7 @@ def main():
     vb64 = spmv_bytes(n, nnz, 8, 8)
     ib64 = ilu_apply_bytes(n, nnz, 8, 8)
     ib32 = ilu_apply_bytes(n, nnz, 4, 4) + 8 * n    # + FP64 pivots
+    ib16 = ilu_apply_bytes(n, nnz, 2, 4) + 8 * n
     xs = x64.cpu().numpy()
     xm = xmx.cpu().numpy()
     from hala_gb300 import problems as P
@@ -631,20 +636,20 @@ def main():
     it64 = inf64[-1].iterations
     launches = (sum(int(q.kernel_launches) for q in inf64) + sum(int(q.kernel_launches) for q in infmx)
                 + sum(int(q.kernel_launches) for q in infir) + sum(int(q.kernel_launches) for q in infbs))
-    launches += 5 * 20 * 5 + 4 * 10   # kernel timing: 5 x 100 SpMV, 2 x 10 ILU applies (2 launches each)
-    # dominant kernel of the headline (mixed) solve: the FP32-store triangular sweeps (ILU apply)
-    ach_ilu = ib32 / (t_ilu32 * 1e-3) / 1e9
+    launches += 5 * 20 * 5 + 6 * 10   # kernel timing: 5 x 100 SpMV, 3 x 10 ILU applies (2 launches each)
+    # dominant kernel of the headline (mixed) solve: the BF16-store triangular sweeps (ILU apply)
+    ach_ilu = ib16 / (t_ilu16 * 1e-3) / 1e9
     prof = {}
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             prof = json.load(f)
     except Exception:
         pass
-    roof = {"bound": "hbm", "kernel": "bsolve_kernel x2 (ILU(0) apply of the FP32 store: forward + backward "
+    roof = {"bound": "hbm", "kernel": "bsolve_kernel x2 (ILU(0) apply of the BF16 store: forward + backward "
                                       "sweep; latency-bound wavefront, see ilu_apply)",
             "achieved": ach_ilu, "peak": peak, "unit": "GB/s", "frac": ach_ilu / peak,
-            "traffic": prof.get("ilu_apply_f32_bytes"), "peak_source": peak_src,
-            "algorithmic_bytes": ib32, "ms_per_launch": t_ilu32 / 2, "ms_per_apply": t_ilu32}
+            "traffic": prof.get("ilu_apply_bf16_bytes"), "peak_source": peak_src,
+            "algorithmic_bytes": ib16, "ms_per_launch": t_ilu16 / 2, "ms_per_apply": t_ilu16}
     spmv = {"kernel": "spmv_warp_kernel", "f64": {"ms": t_spmv64, "gbs": vb64 / (t_spmv64 * 1e-3) / 1e9,
                                                "frac": vb64 / (t_spmv64 * 1e-3) / 1e9 / peak, "bytes": vb64,
                                                "traffic": prof.get("spmv_f64_bytes")},
@@ -672,10 +677,12 @@ def main():
     out = {
         "metric": METRIC, "value": aggregate_rate(world, t_mx), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mx, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner (bf16 ILU factor) / f64 refinement",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD.format(grid=GRID),
-                   "n": n, "nnz": nnz, "form": "mixed: FP32 values/vectors/ILU (FP64 pivots) PCG, FP64 "
-                                               f"refinement by reliable updates (delta {RU_DELTA})",
+                   "n": n, "nnz": nnz, "form": "mixed: PCG with FP32 matrix values and vectors and the "
+                                               "ILU(0) factor stored in BF16 (FP64 pivots), FP64 refinement "
+                                               f"by reliable updates (delta {RU_DELTA})",
                    "l2": "flushed between timed solves (256 MB write); matrix 217 MB > 129 MB L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"solves_per_s": aggregate_rate(world, t_64), "ms_per_solve": t_64, "iterations": it64,
@@ -683,11 +690,11 @@ def main():
         "mixed": {"solves_per_s": aggregate_rate(world, t_mx), "ms_per_solve": t_mx, "inner_iterations": infmx[-1].iterations,
                   "reliable_updates": infmx[-1].outer, "rel_residual": resmx,
                   "err_vs_fp64": float(np.linalg.norm(xm - xs) / np.linalg.norm(xs)),
-                  "err_vs_xtrue": float(np.linalg.norm(xm - xt) / np.linalg.norm(xt)), "setup_ms": setup32 * 1e3},
+                  "err_vs_xtrue": float(np.linalg.norm(xm - xt) / np.linalg.norm(xt)), "setup_ms": setup16 * 1e3},
         "mixed_over_fp64": t_64 / t_mx,
-        "mixed_bf16_store": {"solves_per_s": 1e3 / statistics.mean(msbs), "ms_per_solve": statistics.mean(msbs),
-                             "inner_iterations": infbs[-1].iterations, "reliable_updates": infbs[-1].outer,
-                             "form": "as mixed, the ILU(0) factor stored in BF16 (FP64 pivots), FP32 operator"},
+        "mixed_f32_store": {"solves_per_s": 1e3 / statistics.mean(msbs), "ms_per_solve": statistics.mean(msbs),
+                            "inner_iterations": infbs[-1].iterations, "reliable_updates": infbs[-1].outer,
+                            "form": "as mixed, the ILU(0) factor stored in FP32 (FP64 pivots)"},
         "mixed_restarted_ir": {"solves_per_s": aggregate_rate(world, t_ir),
                                "ms_per_solve": t_ir, "inner_iterations": infir[-1].iterations,
                                "sweeps": infir[-1].outer, "inner_rtol": IR_INNER_RTOL},
@@ -695,13 +702,15 @@ def main():
         "ilu_apply": {"f64": {"ms": t_ilu64, "gbs": ib64 / (t_ilu64 * 1e-3) / 1e9, "bytes": ib64,
                               "traffic": prof.get("ilu_apply_f64_bytes")},
                       "f32": {"ms": t_ilu32, "gbs": ib32 / (t_ilu32 * 1e-3) / 1e9, "bytes": ib32,
-                              "traffic": prof.get("ilu_apply_f32_bytes")}},
+                              "traffic": prof.get("ilu_apply_f32_bytes")},
+                      "bf16": {"ms": t_ilu16, "gbs": ib16 / (t_ilu16 * 1e-3) / 1e9, "bytes": ib16,
+                               "traffic": prof.get("ilu_apply_bf16_bytes")}},
         "e2e": {"value": aggregate_rate(world, t_e2e), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "entry": "hgb_mixed_ru_pcg_solve (host pntr/indx/vals/b/x)",
                 "rel_residual": e2e_err,
                 "with_setup": {"solves_per_s": 1e3 / statistics.mean(e2es_ms), "ms_per_step": statistics.mean(e2es_ms),
                                "ilu_setup_ms": statistics.mean(setup_ms),
-                               "entries": "hgb_ilu0_create_host (FP32 store) + hgb_mixed_ru_pcg_solve, host buffers"}},
+                               "entries": "hgb_ilu0_create_host (BF16 store) + hgb_mixed_ru_pcg_solve, host buffers"}},
         "gpu_launches": launches,
         "other_workloads": others,
         "gpu_launches_other_workloads": other_launches,
