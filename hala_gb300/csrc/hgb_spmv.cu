@@ -48,21 +48,22 @@ __device__ __forceinline__ X spmv_out(X alpha, X acc, X beta, const X *yp) {
     return spmv_acc<false>(mul_rn(beta, *yp), alpha, acc);
 }
 
-// The fused <x, y>: with a counter, the grid reduction into *dot_out (the last CTA adds the
-// parts); without one, each CTA's part goes to partials[blockIdx.x] and the consuming kernel sums
-// them (in one order in every CTA), which keeps the serial last-CTA step out of the product.
+// The fused <x, y> (DOT): 0 none; 1 the grid reduction into *dot_out (the last CTA adds the
+// parts); 2 each CTA's part to partials[blockIdx.x], summed by the consuming kernel (in one order
+// in every CTA), which keeps the serial last-CTA step out of the product.
+template <int DOT>
 __device__ __forceinline__ void spmv_dot_epilogue(double d, double *partials, unsigned *counter, double *dot_out) {
     double dsum[1] = {d};
-    if (counter) {
+    if (DOT == 1) {
         grid_sum<1>(dsum, partials, counter, [&](double (&v)[1]) { *dot_out = v[0]; });
-    } else {
+    } else if (DOT == 2) {
         block_sum<1>(dsum);
         if (threadIdx.x == 0) partials[blockIdx.x] = dsum[0];
     }
 }
 
-// y = alpha * A x + beta * y ; optionally dot_out = <x, y> (square A)
-template <typename V, bool FUSE_DOT, bool EXACT>
+// y = alpha * A x + beta * y ; optionally <x, y> (square A; DOT as spmv_dot_epilogue)
+template <typename V, int DOT, bool EXACT>
 __global__ void __launch_bounds__(kWarpBlock)
 spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
                  typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, typename Val<V>::X beta,
@@ -160,7 +161,7 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
                 }
                 const X out = spmv_out<EXACT>(alpha, acc, beta, y + row);
                 y[row] = out;
-                if (FUSE_DOT) dacc.add(__ldg(x + row), out);
+                if (DOT) dacc.add(__ldg(x + row), out);
             }
             __syncwarp();   // buffer buf is refilled by tile k+2
             ps0 = ps1;
@@ -172,13 +173,13 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
         }
     }
     cp_async_wait<0>();
-    if (FUSE_DOT) spmv_dot_epilogue(dacc.get(), partials, counter, dot_out);
+    if (DOT) spmv_dot_epilogue<DOT>(dacc.get(), partials, counter, dot_out);
 }
 
 // Arrays that are not 16-byte aligned cannot be staged with cp.async: one row per thread,
 // grid-stride, the row's vals/indx and x gathers (8 at a time) straight from global memory
 // through L1.  Same arithmetic as spmv_warp_kernel.
-template <typename V, bool FUSE_DOT, bool EXACT>
+template <typename V, int DOT, bool EXACT>
 __global__ void __launch_bounds__(256)
 spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx,
                    const V *__restrict__ vals, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x,
@@ -204,9 +205,9 @@ spmv_direct_kernel(int n_rows, const int *__restrict__ pntr, const int *__restri
         }
         const X out = spmv_out<EXACT>(alpha, acc, beta, y + r);
         y[r] = out;
-        if (FUSE_DOT) dacc.add(__ldg(x + r), out);
+        if (DOT) dacc.add(__ldg(x + r), out);
     }
-    if (FUSE_DOT) spmv_dot_epilogue(dacc.get(), partials, counter, dot_out);
+    if (DOT) spmv_dot_epilogue<DOT>(dacc.get(), partials, counter, dot_out);
 }
 
 
@@ -397,30 +398,30 @@ void Transpose::release() {
     pntr = row = map = nullptr;
 }
 
-template <typename V, bool FUSE_DOT, bool EXACT>
+template <typename V, int DOT, bool EXACT>
 static int spmv_n_launch_mode(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                               typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
                               typename Val<V>::X *y, double *dot_out, const int *skip, int *nparts) {
-    // nparts: the per-CTA parts of <x, y> stay in the context's parts slots (their count returned)
-    double *partials = FUSE_DOT ? (nparts ? c->partials + kSpmvPartsOffset : c->partials) : nullptr;
-    unsigned *counter = (FUSE_DOT && !nparts) ? c->counter : nullptr;
+    // DOT 2: the per-CTA parts of <x, y> stay in the context's parts slots (their count to *nparts)
+    double *partials = DOT == 2 ? c->partials + kSpmvPartsOffset : (DOT == 1 ? c->partials : nullptr);
+    unsigned *counter = DOT == 1 ? c->counter : nullptr;
     if (aligned16(vals) && aligned16(indx)) {
         // persistent grid: the resident CTAs of every SM (occupancy queried once per kernel)
         static int occ = 0;
         if (!occ) {
-            HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmv_warp_kernel<V, FUSE_DOT, EXACT>, kWarpBlock, 0));
+            HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, spmv_warp_kernel<V, DOT, EXACT>, kWarpBlock, 0));
             occ = std::max(occ, 1);
         }
         const long tiles = ((long)n_rows + 31) / 32;
         const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, std::min(c->num_sms * occ, kMaxReduceBlocks)));
         if (nparts) *nparts = g;
-        spmv_warp_kernel<V, FUSE_DOT, EXACT><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
+        spmv_warp_kernel<V, DOT, EXACT><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y,
                                                                             partials, counter, dot_out, skip);
         return launch_check("spmv_warp_kernel");
     }
     const int g = std::min((n_rows + 255) / 256, std::min(c->num_sms * 8, kMaxReduceBlocks));
     if (nparts) *nparts = g;
-    spmv_direct_kernel<V, FUSE_DOT, EXACT><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, partials,
+    spmv_direct_kernel<V, DOT, EXACT><<<g, 256, 0, c->stream>>>(n_rows, pntr, indx, vals, alpha, x, beta, y, partials,
                                                                    counter, dot_out, skip);
     return launch_check("spmv_direct_kernel");
 }
@@ -432,11 +433,14 @@ int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, cons
     if (nparts) *nparts = 0;
     if (n_rows <= 0) return HGB_OK;
     const bool exact = c->spmv_mode == HGB_SPMV_EXACT;
-    if (dot_out || nparts)
-        return exact ? spmv_n_launch_mode<V, true, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nparts)
-                     : spmv_n_launch_mode<V, true, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nparts);
-    return exact ? spmv_n_launch_mode<V, false, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr)
-                 : spmv_n_launch_mode<V, false, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr);
+    if (nparts)
+        return exact ? spmv_n_launch_mode<V, 2, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nparts)
+                     : spmv_n_launch_mode<V, 2, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nparts);
+    if (dot_out)
+        return exact ? spmv_n_launch_mode<V, 1, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nullptr)
+                     : spmv_n_launch_mode<V, 1, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, dot_out, skip, nullptr);
+    return exact ? spmv_n_launch_mode<V, 0, true>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr)
+                 : spmv_n_launch_mode<V, 0, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr);
 }
 
 template int spmv_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, double,
