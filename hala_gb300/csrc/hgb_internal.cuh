@@ -37,10 +37,12 @@ int dev_error_to_status(int word);
 // Maximum number of CTAs a reduction kernel launches; bounds the partial-sum scratch.
 constexpr int kMaxReduceBlocks = 2048;
 constexpr int kReduceSlots = 4;   // values reduced together in one pass
-// the context's partials: kMaxReduceBlocks x 64 slots for the grid reductions (up to 64 values per
-// pass), then kMaxReduceBlocks per-CTA <x, y> parts of a fused SpMV whose consumer sums them
-constexpr long kSpmvPartsOffset = (long)kMaxReduceBlocks * 64;
-constexpr long kPartialsDoubles = kSpmvPartsOffset + kMaxReduceBlocks;
+// the context's partials (1 MB, a size that measured faster than one just above it: the mixed
+// 128^3 solve took 5 ms longer with 1 MB + 16 KB): the grid reductions' slots below
+// kSpmvPartsOffset (a pass of up to 64 values runs on at most kSpmvPartsOffset / 64 CTAs), then
+// kMaxReduceBlocks per-CTA <x, y> parts of a fused SpMV whose consumer sums them
+constexpr long kSpmvPartsOffset = (long)kMaxReduceBlocks * 48;
+constexpr long kPartialsDoubles = (long)kMaxReduceBlocks * 64;
 
 // Scalars kept on the device by the fused solvers (one set per context).
 struct SolverScalars {

@@ -1221,7 +1221,8 @@ __global__ void gm_xupdate_kernel(long n, const GmresState *__restrict__ st, con
 
 template <typename X>
 static int gm_dots_launch(hgb_ctx *c, long n, int k1, const GmresState *st, const X *W, const X *r, double *cf) {
-    const int grid = reduce_grid(c, n, 256 * 8);
+    // up to 64 partial sums per CTA: the grid stays below the SpMV parts of the context's partials
+    const int grid = std::min(reduce_grid(c, n, 256 * 8), (int)(kSpmvPartsOffset / 64));
     for (int j0 = 0; j0 < k1; j0 += 64) {   // groups of up to 64 columns, one grid reduction each
         const int kk = std::min(64, k1 - j0);
         const X *Wj = W + (long)j0 * n;
