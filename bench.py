@@ -658,7 +658,7 @@ def main():
                     "bytes": spmv_bytes(n, nnz, 4, 4), "traffic": prof.get("spmv_f32_bytes")},
             "bf16f32": {"ms": t_spmvbf, "gbs": spmv_bytes(n, nnz, 2, 4) / (t_spmvbf * 1e-3) / 1e9,
                         "frac": spmv_bytes(n, nnz, 2, 4) / (t_spmvbf * 1e-3) / 1e9 / peak,
-                        "bytes": spmv_bytes(n, nnz, 2, 4)},
+                        "bytes": spmv_bytes(n, nnz, 2, 4), "traffic": prof.get("spmv_bf16_bytes")},
             "f64_exact": {"ms": t_spmv64x, "gbs": vb64 / (t_spmv64x * 1e-3) / 1e9,
                           "frac": vb64 / (t_spmv64x * 1e-3) / 1e9 / peak},
             "f32_exact": {"ms": t_spmv32x, "gbs": spmv_bytes(n, nnz, 4, 4) / (t_spmv32x * 1e-3) / 1e9,
