@@ -255,13 +255,16 @@ static int cg_iteration(hgb_ctx *c, hgb_csr *A, hgb_ilu *M, CgWork<X> &w, X *x, 
 // Unpreconditioned CG on a system whose matrix and vectors stay in L2 (the 256^2 Poisson class):
 // there the graph-replayed iteration is bound by its launches and their reductions' tails
 // (about 27 us per iteration for six launches), not by bytes.  One cooperative launch runs up to
-// kCgpChunk iterations with three grid barriers each: after the SpMV (<p, Ap> complete), after
-// the x / r update (||r||^2 complete) and after the direction update (p complete before the next
-// product).  Every CTA keeps its rows for the whole launch, writes one partial per reduction and,
-// after the barrier, sums all CTAs' partials in the same order, so every CTA takes the same
-// decision with the same bits and no CTA waits on a single finisher.  The arithmetic is the
-// graph path's (DotAcc partials per thread, the same separately rounded updates, the product in
-// the context's SpMV mode), with z = r, so <r, z> is ||r||^2.  Barriers are bounded: a barrier
+// kCgpChunk iterations with two grid barriers each: after the x / r update (||r||^2 complete, and
+// r in memory for the next product) and after the direction update (<p, Ap> complete).  The
+// product is taken of r, s = A r, and the new direction's product follows by the recurrence
+// Ap = beta Ap + s beside p = beta p + r, so no barrier waits for the new p (a launch starts
+// with Ap = A p).  Every CTA keeps its rows for the whole launch, writes one partial per reduction
+// and, after the barrier, sums all CTAs' partials in the same order, so every CTA takes the same
+// decision with the same bits and no CTA waits on a single finisher.  The updates are the graph
+// path's (DotAcc partials per thread, separately rounded, the product in the context's SpMV
+// mode), with z = r, so <r, z> is ||r||^2; the Ap recurrence rounds differently from A p, so the
+// iteration count can differ from the graph path's by a few.  Barriers are bounded: a barrier
 // that runs out of polls sets DEV_ERR_TIMEOUT and every CTA returns.
 constexpr int kCgpThreads = 256;
 constexpr int kCgpChunk = 4096;                 // iterations per launch (the barrier counter stays small)
@@ -280,44 +283,48 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     return v;
 }
 
-// All CTAs of the cooperative launch arrive; false when the wait ran out (DEV_ERR_TIMEOUT set).
-__device__ __forceinline__ bool cgp_barrier(unsigned *count, unsigned target, int *err) {
+// One reduction of the persistent CG: the CTA's partial of v (warp sums, then warp 0), the
+// arrival of every CTA (a grid barrier, bounded), then the sum of all G partials in one fixed
+// order (lane b takes partials b, b + 32, ..., then the warp's butterfly), the same bits in every
+// CTA.  Two CTA barriers: the first orders every thread's earlier global writes before warp 0's
+// release, the second publishes the sum.  False when the wait ran out (DEV_ERR_TIMEOUT set).
+__device__ __forceinline__ bool cgp_reduce(double v, double *part, unsigned *count, unsigned target, int *err,
+                                           double &sum) {
+    __shared__ double wsh[32], res;
     __shared__ int ok;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) wsh[wid] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        // release at GPU scope, cumulative over the CTA's writes that the bar.sync ordered before it
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+    if (wid == 0) {
+        const double t = warp_sum(lane < (int)(blockDim.x >> 5) ? wsh[lane] : 0.0);
+        if (lane == 0) {
+            part[blockIdx.x] = t;
+            // release at GPU scope, cumulative over the CTA's writes that the bar.sync ordered before it
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+        }
+        // every lane polls (one coalesced load), so each lane's own acquire orders its loads below
         int spins = 0, good = 1;
-        while (ld_acquire_u32(count) < target) {
+        while (!__all_sync(0xFFFFFFFFu, ld_acquire_u32(count) >= target)) {
             if (++spins > kSpinLimit || ((spins & 1023) == 0 && (*(volatile int *)err & DEV_ERR_TIMEOUT))) {
-                atomicOr(err, DEV_ERR_TIMEOUT);
                 good = 0;
                 break;
             }
         }
-        ok = good;
+        good = __all_sync(0xFFFFFFFFu, good);
+        double acc = 0.0;
+        if (good)
+            for (int b = lane; b < (int)gridDim.x; b += 32) acc += __ldcg(part + b);
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            if (!good) atomicOr(err, DEV_ERR_TIMEOUT);
+            res = acc;
+            ok = good;
+        }
     }
     __syncthreads();
+    sum = res;
     return ok != 0;
-}
-
-// the sum of the G partials, in one fixed order: the same bits in every CTA
-__device__ __forceinline__ double cgp_sum(const double *part, int G) {
-    __shared__ double res;
-    double v[1] = {0.0};
-    for (int b = threadIdx.x; b < G; b += blockDim.x) v[0] += __ldcg(part + b);
-    block_sum<1>(v);
-    if (threadIdx.x == 0) res = v[0];
-    __syncthreads();
-    const double r = res;
-    __syncthreads();
-    return r;
-}
-
-__device__ __forceinline__ void cgp_partial(double v, double *part) {
-    double a[1] = {v};
-    block_sum<1>(a);
-    if (threadIdx.x == 0) part[blockIdx.x] = a[0];
 }
 
 // RPT > 0: thread t owns rows t, t + stride, ... (RPT of them: 1, 2 or 4) for the whole launch and keeps their
@@ -365,44 +372,48 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
             }
         }
     }
-    for (int c = 0; c < kCgpChunk; c++) {
-        // Ap = A p and <p, Ap>; the neighbours' p come from L2 (__ldcg: other CTAs wrote them)
-        DotAcc<X> pap;
-        X ap[K];
+    // row k of this thread (RPT > 0) or row i (RPT = 0) times the vector v, whose entries other
+    // CTAs wrote during this launch (__ldcg: from L2)
+    auto row_product = [&](int k, long i, const X *v) -> X {
+        X acc = X(0);
+        if (RPT > 0 && len[k] <= kCgpMaxE) {
+            X xv[kCgpMaxE];
+#pragma unroll
+            for (int e = 0; e < kCgpMaxE; e++)
+                if (e < len[k]) xv[e] = __ldcg(v + ci[k][e]);
+#pragma unroll
+            for (int e = 0; e < kCgpMaxE; e++)
+                if (e < len[k]) acc = cgp_acc<EXACT, X>(acc, cv[k][e], xv[e]);
+        } else {
+            const int jb = RPT > 0 ? beg[k] : pntr[i], je = RPT > 0 ? beg[k] + len[k] : pntr[i + 1];
+            for (int j = jb; j < je; j++) acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(v + indx[j]));
+        }
+        return acc;
+    };
+    // q = A p for the direction the launch starts from, and <p, q>
+    X qr[K];
+    double pAp;
+    {
+        DotAcc<X> pq;
         if (RPT > 0) {
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                if (row[k] >= n) continue;
-                X acc = X(0);
-                if (len[k] <= kCgpMaxE) {
-                    X pv[kCgpMaxE];
-#pragma unroll
-                    for (int e = 0; e < kCgpMaxE; e++)
-                        if (e < len[k]) pv[e] = __ldcg(p + ci[k][e]);
-#pragma unroll
-                    for (int e = 0; e < kCgpMaxE; e++)
-                        if (e < len[k]) acc = cgp_acc<EXACT, X>(acc, cv[k][e], pv[e]);
-                } else {
-                    for (int j = beg[k]; j < beg[k] + len[k]; j++)
-                        acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
+            for (int k = 0; k < K; k++)
+                if (row[k] < n) {
+                    qr[k] = row_product(k, row[k], p);
+                    pq.add(pr[k], qr[k]);
                 }
-                ap[k] = acc;
-                pap.add(pr[k], acc);
-            }
         } else {
             for (long i = t0; i < n; i += stride) {
-                X acc = X(0);
-                for (int j = pntr[i]; j < pntr[i + 1]; j++)
-                    acc = cgp_acc<EXACT, X>(acc, Val<V>::get(vals[j]), __ldcg(p + indx[j]));
-                Ap[i] = acc;
-                pap.add(p[i], acc);
+                const X q = row_product(0, i, p);
+                Ap[i] = q;
+                pq.add(p[i], q);
             }
         }
-        cgp_partial(pap.get(), partA);
         target += G;
-        if (!cgp_barrier(count, target, err)) return;
-        const double pAp = cgp_sum(partA, G);
-        // a = <r,z> / <p,Ap>; x += a p; r -= a Ap; ||r||^2
+        if (!cgp_reduce(pq.get(), partA, count, target, err, pAp)) return;
+    }
+    for (int c = 0; c < kCgpChunk; c++) {
+        // a = <r,z> / <p,Ap>; x += a p; r -= a Ap; ||r||^2 (r to memory: the next product reads it)
         const X a = (X)(zr / pAp), ma = -a;
         DotAcc<X> rrd;
         if (RPT > 0) {
@@ -410,7 +421,8 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
             for (int k = 0; k < K; k++) {
                 if (row[k] >= n) continue;
                 xr[k] = add_rn(xr[k], mul_rn(a, pr[k]));
-                rr[k] = add_rn(rr[k], mul_rn(ma, ap[k]));
+                rr[k] = add_rn(rr[k], mul_rn(ma, qr[k]));
+                r[row[k]] = rr[k];
                 rrd.add(rr[k], rr[k]);
             }
         } else {
@@ -421,28 +433,38 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
                 rrd.add(ri, ri);
             }
         }
-        cgp_partial(rrd.get(), partB);
         target += G;
-        if (!cgp_barrier(count, target, err)) return;
-        rrv = cgp_sum(partB, G);
+        if (!cgp_reduce(rrd.get(), partB, count, target, err, rrv)) return;
         it++;
         done = (it >= max_iter) || (rrv < tol2) || !(rrv == rrv);
         if (done) break;
-        // z = r: <r, z> = ||r||^2 (the same partials); p = (zr_new / zr_old) p + z
+        // z = r: <r, z> = ||r||^2; p = (zr_new / zr_old) p + z and, with s = A r, the product of the
+        // new direction by the same recurrence: Ap = (zr_new / zr_old) Ap + s.  So the product reads
+        // r, complete at the barrier above, and no barrier waits for the new p.
         const X bta = (X)(rrv / zr);
+        DotAcc<X> pq;
         if (RPT > 0) {
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 if (row[k] >= n) continue;
+                const X sk = row_product(k, row[k], r);
                 pr[k] = add_rn(mul_rn(bta, pr[k]), rr[k]);
-                p[row[k]] = pr[k];
+                qr[k] = add_rn(mul_rn(bta, qr[k]), sk);
+                pq.add(pr[k], qr[k]);
             }
         } else {
-            for (long i = t0; i < n; i += stride) p[i] = add_rn(mul_rn(bta, p[i]), r[i]);
+            for (long i = t0; i < n; i += stride) {
+                const X si = row_product(0, i, r);
+                const X pi = add_rn(mul_rn(bta, p[i]), r[i]);
+                const X qi = add_rn(mul_rn(bta, Ap[i]), si);
+                p[i] = pi;
+                Ap[i] = qi;
+                pq.add(pi, qi);
+            }
         }
         zr = rrv;
         target += G;
-        if (!cgp_barrier(count, target, err)) return;
+        if (!cgp_reduce(pq.get(), partA, count, target, err, pAp)) return;
     }
     if (RPT > 0) {
 #pragma unroll
@@ -450,6 +472,7 @@ cg_persistent_kernel(long n, const int *__restrict__ pntr, const int *__restrict
             if (row[k] < n) {
                 x[row[k]] = xr[k];
                 r[row[k]] = rr[k];
+                p[row[k]] = pr[k];
             }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
