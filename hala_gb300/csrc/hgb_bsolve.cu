@@ -386,19 +386,28 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // ---- solver threads
         X *outb = out + row_lo;
         X *pendb = pend ? pend + row_lo : nullptr;
-        // thread t's packet of step s into its ring slot s % D (an empty group past the last step);
-        // without a row in step s it writes an idle packet (zero-slot codes, the barrier flag)
-        auto issue = [&](int s) {
-            if (s < ns) {
-                const int4 d = sdesc[s];
-                int4 *slot = myring + (s & (D - 1)) * (NP * NT);
-                if (t < d.y) {
-                    bs_copy16(slot, A.pk0 + d.x + t);
+        // thread t's packets of steps s0 .. s0 + D/2 - 1 into their ring slots s % D, one commit
+        // group per half ring (its descriptors read together); without a row in a step the thread
+        // writes an idle packet (zero-slot codes, the barrier flag)
+        constexpr int HB = D / 2;
+        auto issue = [&](int s0) {
+            int4 dd[HB];
 #pragma unroll
-                    for (int p = 0; p < NV; p++)
-                        bs_copy16(slot + (1 + p) * NT, A.pkv + (long)p * A.npk + d.x + t);
-                } else {
-                    *slot = make_int4(A.R, A.R, A.R, bs_word(0, kBsIdle, (d.w >> 16) & 1));
+            for (int h = 0; h < HB; h++) dd[h] = (s0 + h < ns) ? sdesc[s0 + h] : make_int4(0, 0, 0, 0);
+#pragma unroll
+            for (int h = 0; h < HB; h++) {
+                const int s = s0 + h;
+                if (s < ns) {
+                    const int4 d = dd[h];
+                    int4 *slot = myring + (s & (D - 1)) * (NP * NT);
+                    if (t < d.y) {
+                        bs_copy16(slot, A.pk0 + d.x + t);
+#pragma unroll
+                        for (int p = 0; p < NV; p++)
+                            bs_copy16(slot + (1 + p) * NT, A.pkv + (long)p * A.npk + d.x + t);
+                    } else {
+                        *slot = make_int4(A.R, A.R, A.R, bs_word(0, kBsIdle, (d.w >> 16) & 1));
+                    }
                 }
             }
             bs_commit();
@@ -420,10 +429,13 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // the next block's CTA (the next rank of this cluster): its remote ring
         const bool has_next = rank + 1 < ncl && b + 1 < A.nblk;
         const uint32_t next_rbuf = has_next ? bs_peer(rbuf, rank + 1) : 0u;
-        for (int s = 0; s < D - 1; s++) issue(s);
+        issue(0);
+        issue(HB);
         for (int s = 0; s < ns; s++) {
-            issue(s + D - 1);
-            cp_async_wait<D - 1>();   // step s has landed
+            if (s % HB == 0) {   // the half ring of steps s .. s + HB - 1 has landed; refill the other half
+                if (s > 0) issue(s + HB);
+                cp_async_wait<1>();
+            }
             const int4 *slot = myring + (s & (D - 1)) * (NP * NT);
             const int4 p0 = slot[0];
             const int w = p0.w, nd = (w >> 15) & 0xFFFF, sl = w & 0x7FFF;
