@@ -316,6 +316,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 }
             };
             load_rj(w, jq);
+            // The buffer passed as pend (the next launch's output, or this launch's input once its
+            // slice is in shared memory; nothing in this launch reads it) goes back to the pending
+            // pattern in the fetcher warps, off the solver threads' steps (a store per row in each
+            // step cost the FP32 sweeps 8 %).  FP64 spreads it over the fetchers' steps, FP32 writes
+            // it after them: each measured faster for its type (the FP64 slice in one burst beside the
+            // solver threads' last steps cost 2 %).
+            constexpr bool kPendSpread = sizeof(X) == 8;
+            const int pchunk = ns > 0 ? (cnt + ns - 1) / ns : 0;   // rows per step (kPendSpread)
             for (int s = w; s < ns; s += kBsFetchWarps) {
                 load_rj(s + kBsFetchWarps, jn);
                 // the ring slot of step s was last used by step s - kBsF (the solver threads reset
@@ -379,13 +387,35 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                 }
 #pragma unroll
                 for (int q = 0; q < RPL; q++) jq[q] = jn[q];
+                // FP64: the other buffer's share of this step back to the pending pattern (below)
+                if (kPendSpread && pend) {
+                    const int r0 = s * pchunk, r1 = min(cnt, r0 + pchunk);
+                    for (int i = r0 + l; i < r1; i += 32) pend[row_lo + i] = Pending<X>::value();
+                }
+            }
+            // FP32: the other buffer's whole slice back to the pending pattern at the end of the
+            // fetchers' steps, in 16-byte stores
+            if (!kPendSpread && pend) {
+                X *pb = pend + row_lo;
+                const int ft = t - NT, FT = 32 * kBsFetchWarps;
+                const int pmis = (int)(((size_t)pb & 15) / sizeof(X));
+                const int phead = min(cnt, (E - pmis) % E), pbody = (cnt - phead) / E;
+                const X pv = Pending<X>::value();
+                for (int i = ft; i < phead; i += FT) pb[i] = pv;
+                for (int i = ft; i < pbody; i += FT) {
+                    X *q = pb + phead + i * E;   // 16-byte aligned
+                    if constexpr (sizeof(X) == 4)
+                        *(float4 *)q = make_float4(pv, pv, pv, pv);
+                    else
+                        *(double2 *)q = make_double2(pv, pv);
+                }
+                for (int i = phead + pbody * E + ft; i < cnt; i += FT) pb[i] = pv;
             }
             continue;   // to the block-end barrier
         }
 
         // ---- solver threads
         X *outb = out + row_lo;
-        X *pendb = pend ? pend + row_lo : nullptr;
         // thread t's packets of steps s0 .. s0 + D/2 - 1 into their ring slots s % D, one commit
         // group per half ring (its descriptors read together); without a row in a step the thread
         // writes an idle packet (zero-slot codes, the barrier flag)
@@ -488,7 +518,6 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             if (nd != kBsIdle) {
                 xs[sl] = acc;
                 st_relaxed(outb + sl, acc);
-                if (pendb) pendb[sl] = Pending<X>::value();
                 if (rw.push >= 0 && has_next) {
                     // the next block reads this value first: offer it to that CTA's ring (taken only
                     // if the entry awaits exactly that step; the result is not read, which measured
@@ -938,9 +967,8 @@ template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
 static int bs_launch_nt(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
     constexpr int CTA = bs_cta<NT>();
     const size_t smem = bs_smem_bytes<V, X, NT>(S.R);
-    // the attribute allows the largest block (16384 FP64 / 32768 FP32 rows), so solves with smaller
-    // blocks launch too
-    const size_t smem_max = bs_smem_bytes<V, X, NT>(sizeof(X) == 8 ? 16384 : 32768);
+    // the attribute allows the largest block (16384 rows), so solves with smaller blocks launch too
+    const size_t smem_max = bs_smem_bytes<V, X, NT>(16384);
     static int attr_dev = -1;   // device on which the kernel's shared-memory attribute was set
     if (attr_dev != c->device) {
         int mx = 0;
@@ -1004,7 +1032,7 @@ template <typename V, typename X>
 int bsolve_launch(hgb_ctx *c, const BlockSolve &S, int mode, int unit, X alpha, const X *in, X *out, X *pend,
                   const int *skip) {
     if (S.n == 0) return HGB_OK;
-    if (S.R > 32768) return fail(HGB_ERR_ARG, "bsolve: %d rows per block exceed the 15-bit slot", S.R);
+    if (S.R > 16384) return fail(HGB_ERR_ARG, "bsolve: %d rows per block exceed the shared-memory slice", S.R);
     if (S.vsize != (int)sizeof(V) || !S.pkv) return fail(HGB_ERR_ARG, "bsolve: values not loaded for this store");
     BsArgs A;
     A.nblk = S.nblk;

@@ -24,7 +24,7 @@ struct BlockSolve {
 };
 
 // Rows per block for a solve over n rows with an xsize-byte solution (the block's slice lives in
-// shared memory: at most 16384 FP64 or 32768 FP32 rows).
+// shared memory: at most 16384 rows).
 int bsolve_rows(hgb_ctx *c, int xsize, int n);
 
 int bsolve_analyse(hgb_ctx *c, int n, int nnz, const int *pntr_d, const int *indx_d, const int *diag_d, int lower,
