@@ -20,11 +20,11 @@
 // when it needs a value from the block before.  The
 // launch groups the CTAs into thread-block clusters that take consecutive blocks: inside a
 // cluster, the CTA of block b also offers each value that block b+1 needs first straight to the
-// ring of block b+1's CTA (a compare-and-swap in distributed shared memory), so most hops between
-// blocks skip the L2 round trip.  Ring entries hold a NaN pattern tagged with the step they wait
-// for; a deposit (offered value or fetched one) replaces exactly that pattern, so an offer that
-// comes too early or too late is dropped and the fetchers deliver the value instead: the offers
-// never wait and never decide correctness.  Entries
+// ring of block b+1's CTA (a store in distributed shared memory), so most hops between blocks
+// skip the L2 round trip.  A ring entry is taken only by the step it was deposited for (FP64: a
+// NaN pattern tagged with the awaited step, replaced by compare-and-swap; FP32: the value with its
+// step beside it), so an offer that comes too early or too late is dropped or ignored and the
+// fetchers deliver the value instead: the offers never wait and never decide correctness.  Entries
 // keep the reference's accumulation order within each row, so results are bit-identical to the
 // sequential loops of apply_ilu_array / sparse_trsv_array (sparse/hala_sparse_utils.hpp).
 #include "hgb_internal.cuh"
@@ -49,6 +49,7 @@ constexpr int kBsThreads = 128;
 constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
 template <int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * kBsFetchWarps; }
 constexpr int kBsF = 32;          // steps in the remote-value ring
+using RingE = unsigned long long; // remote-ring entry (see Ring)
 constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on its ring entry before
                                              // reading the value from L2 itself
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
@@ -76,11 +77,11 @@ inline int bs_nv(int vsize) { return vsize == 8 ? 3 : (vsize == 4 ? 2 : 1); }
 constexpr int kBsMaxCluster = 16;  // largest thread-block cluster (above 8: non-portable sizes)
 
 // shared memory: [packet ring D x (1 + NV) x NT pieces | step descriptors |
-//                 remote-value ring kBsF x NT | solution slice + zero slot]
+//                 remote-value ring kBsF x NT entries | solution slice + zero slot]
 template <typename V, typename X, int NT>
 constexpr size_t bs_smem_bytes(int R) {
     return (size_t)bs_depth<V, NT>() * (1 + BsCfg<V>::NV) * NT * 16 + (size_t)kBsStepCap * 16 +
-           (size_t)kBsF * NT * sizeof(X) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
+           (size_t)kBsF * NT * sizeof(RingE) + ((size_t)R + 16 / sizeof(X) + 1) * sizeof(X);
 }
 
 // One row's values, unpacked from its value pieces (pieces are NT int4 apart in the ring):
@@ -211,33 +212,53 @@ __device__ __forceinline__ bool bs_give_up(int spins, int *err) {
 }
 constexpr int kBsSpinLimitSleeping = 1 << 22;   // polls with a 128 ns sleep: about half a second
 
-// Remote-ring entries: a signalling-NaN pattern tagged with the step whose value the entry awaits
-// (arithmetic never produces signalling NaNs, and solver outputs are canonicalised).
-template <typename X> struct RingTag;
-template <> struct RingTag<double> {
-    using U = unsigned long long;
-    __device__ static U tag(int s) { return 0x7FF4BEEF00000000ull | (unsigned)s; }
-    __device__ static bool is(double v) { return ((U)__double_as_longlong(v) >> 32) == 0x7FF4BEEFull; }
-    __device__ static U bits(double v) { return (U)__double_as_longlong(v); }
-    __device__ static double val(U b) { return __longlong_as_double((long long)b); }
-};
-template <> struct RingTag<float> {
-    using U = unsigned;
-    __device__ static U tag(int s) { return 0x7FA00000u | ((unsigned)s & 0x1FFFFFu); }
-    __device__ static bool is(float v) { return (__float_as_uint(v) & 0xFFE00000u) == 0x7FA00000u; }
-    __device__ static U bits(float v) { return __float_as_uint(v); }
-    __device__ static float val(U b) { return __uint_as_float(b); }
-};
 __device__ __forceinline__ unsigned long long bs_peer_cas(uint32_t a, unsigned long long expect, unsigned long long v) {
     unsigned long long old;
     asm volatile("atom.shared::cluster.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "r"(a), "l"(expect), "l"(v) : "memory");
     return old;
 }
-__device__ __forceinline__ unsigned bs_peer_cas(uint32_t a, unsigned expect, unsigned v) {
-    unsigned old;
-    asm volatile("atom.shared::cluster.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(a), "r"(expect), "r"(v) : "memory");
-    return old;
+// a strong (relaxed, cluster-scope) 64-bit store into a peer's shared memory: the peer polls the
+// entry with volatile loads
+__device__ __forceinline__ void bs_peer_store64(uint32_t a, unsigned long long v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.b64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
 }
+
+// Remote-ring entries (64 bits), one per (step mod kBsF, solver thread).  A deposit (a fetched
+// value or an offer from the cluster peer) may only be taken by the step it was made for.
+//  - FP64: a signalling-NaN pattern tagged with the step the entry awaits (arithmetic never
+//    produces signalling NaNs, and solver outputs are canonicalised); a deposit replaces exactly
+//    that pattern (compare-and-swap), and the consumer puts the tag of the entry's next use back
+//    after reading it.
+//  - FP32: the value in the low half and the step it belongs to in the high half, written with one
+//    64-bit store; the consumer takes it only when the step matches, so nothing is reset after a
+//    read and a deposit needs no compare-and-swap.  A deposit that overwrites an unread older step
+//    (an offer more than kBsF steps early) only sends that older step's consumer to read the value
+//    from L2 itself.
+template <typename X> struct Ring;
+template <> struct Ring<double> {
+    __device__ static RingE tag(int s) { return 0x7FF4BEEF00000000ull | (unsigned)s; }
+    __device__ static RingE init(int q) { return tag(q); }
+    __device__ static bool awaits(RingE e, int s) { return e == tag(s); }
+    __device__ static bool ready(RingE e, int) { return (e >> 32) != 0x7FF4BEEFull; }
+    __device__ static double value(RingE e) { return __longlong_as_double((long long)e); }
+    __device__ static void deposit(RingE *slot, int s, double v) {
+        atomicCAS(slot, tag(s), (RingE)__double_as_longlong(v));
+    }
+    __device__ static void consumed(volatile RingE *e, int s) { *e = tag(s + kBsF); }
+    __device__ static void offer(uint32_t peer, int ps, double v) {
+        bs_peer_cas(peer, tag(ps), (RingE)__double_as_longlong(v));
+    }
+};
+template <> struct Ring<float> {
+    __device__ static RingE stamp(int s, float v) { return ((RingE)(unsigned)s << 32) | __float_as_uint(v); }
+    __device__ static RingE init(int) { return ~0ull; }
+    __device__ static bool awaits(RingE e, int s) { return (unsigned)(e >> 32) != (unsigned)s; }
+    __device__ static bool ready(RingE e, int s) { return (unsigned)(e >> 32) == (unsigned)s; }
+    __device__ static float value(RingE e) { return __uint_as_float((unsigned)e); }
+    __device__ static void deposit(RingE *slot, int s, float v) { *(volatile RingE *)slot = stamp(s, v); }
+    __device__ static void consumed(volatile RingE *, int) {}
+    __device__ static void offer(uint32_t peer, int ps, float v) { bs_peer_store64(peer, stamp(ps, v)); }
+};
 
 // MODE 0: x_i = (b_i - sum_k v_k x_k) [/ d_i]  (apply_ilu_array's order);
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
@@ -254,8 +275,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][NT]
     int4 *sdesc = ring + D * NP * NT;                   // [kBsStepCap]
-    X *rbuf = (X *)(sdesc + kBsStepCap);                // [kBsF][NT] remote values
-    X *xsbuf = rbuf + kBsF * NT;                        // [R + 16 / sizeof(X) + 1]
+    RingE *rbuf = (RingE *)(sdesc + kBsStepCap);        // [kBsF][NT] remote values
+    X *xsbuf = (X *)(rbuf + kBsF * NT);                 // [R + 16 / sizeof(X) + 1]
     __shared__ int blk_sh, done_step;                   // done_step: solver threads finished steps <= it
     const int t = threadIdx.x;
     const unsigned rank = bs_cluster_rank(), ncl = bs_cluster_size();
@@ -265,7 +286,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     }
     const bool solver = t < NT;
     int4 *myring = ring + t;                            // solver thread's piece 0 of ring slot 0
-    volatile X *vrbuf = rbuf;
+    volatile RingE *vrbuf = rbuf;
     for (;;) {
         // clusters take tickets; rank r of the cluster with ticket q solves block q * ncl + r.  The
         // cluster barriers: every CTA of the cluster is done with the previous round (including its
@@ -276,7 +297,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             for (unsigned r = 0; r < ncl; r++) bs_peer_store(bs_peer(&blk_sh, r), q);
         }
         if (t == 0) done_step = -1;
-        for (int i = t; i < kBsF * NT; i += CTA) rbuf[i] = RingTag<X>::val(RingTag<X>::tag(i / NT));
+        for (int i = t; i < kBsF * NT; i += CTA) rbuf[i] = Ring<X>::init(i / NT);
         bs_cluster_sync();
         const int q = blk_sh;
         if (q * (int)ncl >= A.nblk) break;   // the same for the whole cluster
@@ -336,14 +357,12 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     }
                     __nanosleep(128);
                 }
-                X *slot = rbuf + (s & (kBsF - 1)) * NT + l;
-                volatile X *vslot = slot;
-                using U = typename RingTag<X>::U;
-                const U want = RingTag<X>::tag(s);
+                RingE *slot = rbuf + (s & (kBsF - 1)) * NT + l;
+                volatile RingE *vslot = slot;
                 unsigned todo = 0;
 #pragma unroll
                 for (int q = 0; q < RPL; q++)   // rows whose value the block before has not offered yet
-                    if (jq[q] >= 0 && RingTag<X>::bits(vslot[32 * q]) == want) todo |= 1u << q;
+                    if (jq[q] >= 0 && Ring<X>::awaits(vslot[32 * q], s)) todo |= 1u << q;
                 spins = 0;
                 // one lane polls a single value of the step until it is produced, then the warp
                 // loads them all: one L2 load per round instead of one per row keeps the memory
@@ -370,7 +389,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 #pragma unroll
                     for (int q = 0; q < RPL; q++)
                         if ((todo & (1u << q)) && !Pending<X>::is(v[q])) {
-                            atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(v[q]));
+                            Ring<X>::deposit(slot + 32 * q, s, v[q]);
                             todo &= ~(1u << q);
                         }
                     if (!todo) break;
@@ -381,7 +400,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
 #pragma unroll
                         for (int q = 0; q < RPL; q++)
                             if (todo & (1u << q))
-                                atomicCAS((U *)(slot + 32 * q), want, RingTag<X>::bits(Pending<X>::canon(Pending<X>::value())));
+                                Ring<X>::deposit(slot + 32 * q, s, Pending<X>::canon(Pending<X>::value()));
                         todo = 0;
                     }
                 }
@@ -446,14 +465,14 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         // entry e showed the pending pattern: wait for the deposit (bounded, then read directly)
         // (an offer that was dropped, or a slow fetcher, costs at most kBsDirectAfter cycles: then
         // the thread reads the value from L2 itself)
-        auto remote_wait = [&](volatile X *e, int cd) -> X {
+        auto remote_wait = [&](volatile RingE *e, int s, int cd) -> X {
             const long long t0 = clock64();
-            X v = *e;
-            while (RingTag<X>::is(v)) {
+            RingE v = *e;
+            while (!Ring<X>::ready(v, s)) {
                 if (clock64() - t0 > kBsDirectAfter) return wait_value(out + (-cd - 1), A.err);
                 v = *e;
             }
-            return v;
+            return Ring<X>::value(v);
         };
         int last_pub = -1;   // thread 0: the last step published to the fetchers
         // the next block's CTA (the next rank of this cluster): its remote ring
@@ -477,18 +496,19 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             X xv[kBsInline];
 #pragma unroll
             for (int k = 0; k < kBsInline; k++) xv[k] = xs[max(code[k], 0)];
-            // dependencies on earlier blocks: the first one comes from the fetchers' ring (the entry
-            // goes back to the pending pattern for its next use, kBsF steps later); any further one
-            // is polled directly
+            // dependencies on earlier blocks: the first one comes from the fetchers' ring (an FP64
+            // entry goes back to the pending pattern for its next use, kBsF steps later); any
+            // further one is polled directly
             {
                 const int k0 = code[0] < 0 ? 0 : (code[1] < 0 ? 1 : (code[2] < 0 ? 2 : -1));
-                volatile X *e = vrbuf + (s & (kBsF - 1)) * NT + t;
-                X rv = *e;
+                volatile RingE *e = vrbuf + (s & (kBsF - 1)) * NT + t;
+                const RingE ev = *e;
+                X rv = Ring<X>::value(ev);
                 if (k0 >= 0) {
                     const int c0 = (k0 == 0) ? code[0] : (k0 == 1 ? code[1] : code[2]);
-                    if (RingTag<X>::is(rv)) rv = remote_wait(e, c0);
+                    if (!Ring<X>::ready(ev, s)) rv = remote_wait(e, s, c0);
                 }
-                *e = RingTag<X>::val(RingTag<X>::tag(s + kBsF));   // the entry's next use
+                Ring<X>::consumed(e, s);   // FP64: the entry's next use
 #pragma unroll
                 for (int k = 0; k < kBsInline; k++)
                     if (k == k0) xv[k] = rv;
@@ -523,8 +543,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
                     // if the entry awaits exactly that step; the result is not read, which measured
                     // faster than reading it a step later)
                     const int ps = rw.push >> 8, pt = rw.push & 255;
-                    bs_peer_cas(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * NT + pt) * sizeof(X)),
-                                RingTag<X>::tag(ps), RingTag<X>::bits(acc));
+                    Ring<X>::offer(next_rbuf + (uint32_t)(((ps & (kBsF - 1)) * NT + pt) * sizeof(RingE)), ps, acc);
                 }
             }
             if (w < 0) {   // end of a level (or of 16 steps of one): publish it to the solver threads, and
