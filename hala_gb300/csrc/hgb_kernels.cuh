@@ -139,6 +139,12 @@ template <typename V>
 int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,
                   typename Val<V>::X *y, double *dot_out, const int *skip = nullptr, int *nparts = nullptr);
+// Y = alpha A X + beta Y over nrhs column-major columns, the matrix read once (each column
+// bit-identical to spmv_n_launch's product)
+template <typename V>
+int spmm_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals, int nrhs,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, long ldx, typename Val<V>::X beta,
+                  typename Val<V>::X *y, long ldy);
 template <typename V>
 int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,
                   typename Val<V>::X alpha, const typename Val<V>::X *x, typename Val<V>::X beta,

@@ -2,7 +2,8 @@
 // solve_batch_cg / solve_batch_cg_ilu (hex/solvers/hala_solvers_cg_batch.hpp:68-248).
 //
 // Vectors are n x nrhs column-major, as in the reference.  The SpMM is the reference's
-// sparse_gemm_array (sparse/hala_sparse_utils.hpp:127-133): one sparse_gemv_array per column, so
+// sparse_gemm_array (sparse/hala_sparse_utils.hpp:127-133), one sparse_gemv_array per column: here
+// one kernel reads the matrix once and sums every column in the single-column product's order, so
 // each column is bit-identical to hgb_csr_gemv.  The ILU apply runs the single-column sweeps per
 // column.  The PCG follows solve_cg_core (hex/solvers/hala_solvers_cg.hpp:92-156) with one scalar
 // per column (batch_dot, vdivide, batch_axpy, batch_scal of wax/hala_blas_extensions.hpp) and
@@ -98,11 +99,8 @@ static int mr_grid(hgb_ctx *c, long total) {
 template <typename V>
 static int mr_gemm(hgb_csr *A, int nrhs, typename Val<V>::X alpha, const typename Val<V>::X *x, long ldx,
                    typename Val<V>::X beta, typename Val<V>::X *y, long ldy) {
-    hgb_ctx *c = csr_ctx(A);
-    for (int k = 0; k < nrhs; k++)
-        HGB_TRY(spmv_n_launch<V>(c, csr_rows(A), csr_pntr(A), csr_indx(A), (const V *)csr_vals(A), alpha,
-                                 x + (long)k * ldx, beta, y + (long)k * ldy, nullptr));
-    return HGB_OK;
+    return spmm_n_launch<V>(csr_ctx(A), csr_rows(A), csr_pntr(A), csr_indx(A), (const V *)csr_vals(A), nrhs, alpha, x,
+                            ldx, beta, y, ldy);
 }
 
 template <typename X>

@@ -176,6 +176,109 @@ spmv_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict
     if (DOT) spmv_dot_epilogue<DOT>(dacc.get(), partials, counter, dot_out);
 }
 
+// Y = alpha * A X + beta * Y for nrhs column-major columns (x column c at x + c * ldx): the tiles
+// of spmv_warp_kernel, each staged in shared memory once and summed for kMmCols columns at a time
+// (the matrix is read once, not once per column).  Every column is summed in column order in
+// the mode's rounding, so each column equals the single-column product bit for bit.
+constexpr int kMmCols = 4;   // columns summed per pass over a tile (gathers in flight per lane)
+template <typename V, bool EXACT>
+__global__ void __launch_bounds__(kWarpBlock)
+spmm_warp_kernel(int n_rows, const int *__restrict__ pntr, const int *__restrict__ indx, const V *__restrict__ vals,
+                 int nrhs, typename Val<V>::X alpha, const typename Val<V>::X *__restrict__ x, long ldx,
+                 typename Val<V>::X beta, typename Val<V>::X *__restrict__ y, long ldy) {
+    using X = typename Val<V>::X;
+    constexpr int EV = 16 / (int)sizeof(V);
+    constexpr int SV = kWarpCap + 2 * EV, SI = kWarpCap + 8;
+    __shared__ __align__(16) V s_vals[kWarpBlock / 32][2][SV];
+    __shared__ __align__(16) int s_idx[kWarpBlock / 32][2][SI];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nnz = __ldg(pntr + n_rows);
+    const long ntiles = ((long)n_rows + 31) / 32;
+    const long nwarps = (long)gridDim.x * (kWarpBlock / 32);
+    const long per = (ntiles + nwarps - 1) / nwarps;
+    const long tb = ((long)blockIdx.x * (kWarpBlock / 32) + wib) * per;
+    const long te = min(ntiles, tb + per);
+    auto load_ptrs = [&](long k, int &ps, int &pe) {
+        const int row = (int)(k * 32) + lane;
+        ps = __ldg(pntr + min(row, n_rows));
+        pe = __ldg(pntr + min(row + 1, n_rows));
+    };
+    auto start_tile = [&](long k, int ps, int pe, int buf, int &base, int &end) {
+        const int nr = min(32, n_rows - (int)(k * 32));
+        base = __shfl_sync(0xffffffffu, ps, 0);
+        end = __shfl_sync(0xffffffffu, pe, nr - 1);
+        if (end - base <= kWarpCap) {
+            V *sv = s_vals[wib][buf];
+            int *si = s_idx[wib][buf];
+            const int av = base & ~(EV - 1), ai = base & ~3;
+            for (int g = av + lane * EV; g < end; g += 32 * EV) {
+                if (g + EV <= nnz) cp_async16(sv + (g - av), vals + g);
+                else
+                    for (int q = 0; q < EV && g + q < end; q++) sv[g - av + q] = vals[g + q];
+            }
+            for (int g = ai + lane * 4; g < end; g += 32 * 4) {
+                if (g + 4 <= nnz) cp_async16(si + (g - ai), indx + g);
+                else
+                    for (int q = 0; q < 4 && g + q < end; q++) si[g - ai + q] = indx[g + q];
+            }
+        }
+        cp_async_commit();
+    };
+    if (tb >= te) return;
+    int ps0, pe0, ps1 = 0, pe1 = 0, base0, end0;
+    load_ptrs(tb, ps0, pe0);
+    start_tile(tb, ps0, pe0, 0, base0, end0);
+    if (tb + 1 < te) load_ptrs(tb + 1, ps1, pe1);
+    for (long k = tb; k < te; k++) {
+        const int buf = (int)((k - tb) & 1);
+        int base1 = 0, end1 = 0, ps2 = 0, pe2 = 0;
+        if (k + 1 < te) start_tile(k + 1, ps1, pe1, buf ^ 1, base1, end1);
+        else cp_async_commit();
+        if (k + 2 < te) load_ptrs(k + 2, ps2, pe2);
+        cp_async_wait<1>();   // tile k has landed
+        __syncwarp();
+        const int row = (int)(k * 32) + lane;
+        if (row < n_rows) {
+            const bool staged = end0 - base0 <= kWarpCap;
+            const V *sv = s_vals[wib][buf];
+            const int *si = s_idx[wib][buf];
+            const int ov = base0 & ~(EV - 1), oi = base0 & ~3;
+            for (int c0 = 0; c0 < nrhs; c0 += kMmCols) {
+                const int nc = min(kMmCols, nrhs - c0);
+                const X *xc = x + (long)c0 * ldx;
+                X acc[kMmCols];
+#pragma unroll
+                for (int q = 0; q < kMmCols; q++) acc[q] = X(0);
+                for (int j = ps0; j < pe0; j++) {
+                    const X v = staged ? Val<V>::get(sv[j - ov]) : Val<V>::get(__ldg(vals + j));
+                    const int col = staged ? si[j - oi] : __ldg(indx + j);
+                    X xv[kMmCols];
+#pragma unroll
+                    for (int q = 0; q < kMmCols; q++)
+                        if (q < nc) xv[q] = __ldg(xc + (long)q * ldx + col);
+#pragma unroll
+                    for (int q = 0; q < kMmCols; q++)
+                        if (q < nc) acc[q] = spmv_acc<EXACT>(acc[q], v, xv[q]);
+                }
+#pragma unroll
+                for (int q = 0; q < kMmCols; q++)
+                    if (q < nc) {
+                        X *yp = y + (long)(c0 + q) * ldy + row;
+                        *yp = spmv_out<EXACT>(alpha, acc[q], beta, yp);
+                    }
+            }
+        }
+        __syncwarp();   // buffer buf is refilled by tile k+2
+        ps0 = ps1;
+        pe0 = pe1;
+        base0 = base1;
+        end0 = end1;
+        ps1 = ps2;
+        pe1 = pe2;
+    }
+    cp_async_wait<0>();
+}
+
 // Arrays that are not 16-byte aligned cannot be staged with cp.async: one row per thread,
 // grid-stride, the row's vals/indx and x gathers (8 at a time) straight from global memory
 // through L1.  Same arithmetic as spmv_warp_kernel.
@@ -443,12 +546,50 @@ int spmv_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, cons
                  : spmv_n_launch_mode<V, 0, false>(c, n_rows, pntr, indx, vals, alpha, x, beta, y, nullptr, skip, nullptr);
 }
 
+template <typename V>
+int spmm_n_launch(hgb_ctx *c, int n_rows, const int *pntr, const int *indx, const V *vals, int nrhs,
+                  typename Val<V>::X alpha, const typename Val<V>::X *x, long ldx, typename Val<V>::X beta,
+                  typename Val<V>::X *y, long ldy) {
+    if (n_rows <= 0 || nrhs <= 0) return HGB_OK;
+    if (!aligned16(vals) || !aligned16(indx)) {   // no staging: the single-column products
+        for (int k = 0; k < nrhs; k++)
+            HGB_TRY(spmv_n_launch<V>(c, n_rows, pntr, indx, vals, alpha, x + (long)k * ldx, beta, y + (long)k * ldy,
+                                     nullptr));
+        return HGB_OK;
+    }
+    const bool exact = c->spmv_mode == HGB_SPMV_EXACT;
+    static int occ_dev[2][64] = {};
+    if (c->device < 0 || c->device >= 64) return fail(HGB_ERR_UNSUPPORTED, "spmm: device ordinal %d", c->device);
+    int &occ = occ_dev[exact ? 1 : 0][c->device];
+    if (!occ) {
+        HGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ, exact ? (const void *)spmm_warp_kernel<V, true> : (const void *)spmm_warp_kernel<V, false>,
+            kWarpBlock, 0));
+        occ = std::max(occ, 1);
+    }
+    const long tiles = ((long)n_rows + 31) / 32;
+    const int g = (int)std::max<long>(1, std::min<long>((tiles + 7) / 8, (long)c->num_sms * occ));
+    if (exact)
+        spmm_warp_kernel<V, true><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, nrhs, alpha, x, ldx,
+                                                                    beta, y, ldy);
+    else
+        spmm_warp_kernel<V, false><<<g, kWarpBlock, 0, c->stream>>>(n_rows, pntr, indx, vals, nrhs, alpha, x, ldx,
+                                                                     beta, y, ldy);
+    return launch_check("spmm_warp_kernel");
+}
+
 template int spmv_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, double,
                                    const double *, double, double *, double *, const int *, int *);
 template int spmv_n_launch<float>(hgb_ctx *, int, const int *, const int *, const float *, float,
                                   const float *, float, float *, double *, const int *, int *);
 template int spmv_n_launch<uint16_t>(hgb_ctx *, int, const int *, const int *, const uint16_t *, float,
                                      const float *, float, float *, double *, const int *, int *);
+template int spmm_n_launch<double>(hgb_ctx *, int, const int *, const int *, const double *, int, double,
+                                   const double *, long, double, double *, long);
+template int spmm_n_launch<float>(hgb_ctx *, int, const int *, const int *, const float *, int, float,
+                                  const float *, long, float, float *, long);
+template int spmm_n_launch<uint16_t>(hgb_ctx *, int, const int *, const int *, const uint16_t *, int, float,
+                                     const float *, long, float, float *, long);
 
 template <typename V>
 int spmv_t_launch(hgb_ctx *c, int n_rows, int n_cols, const int *pntr, const int *indx, const V *vals,

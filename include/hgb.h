@@ -262,9 +262,10 @@ int hgb_cg_solve_op(hgb_ctx *ctx, hgb_csr *A, hgb_ilu *M, char trans, const void
 
 /* ---- several right-hand sides with one matrix (n x nrhs column-major blocks) ---- */
 
-/* Y = alpha A X + beta Y, one column at a time: sparse_gemm_array 'N','N'
- * (sparse/hala_sparse_utils.hpp:127-133) through sparse_gemm (wax); each column is bit-identical to
- * hgb_csr_gemv.  ldx >= columns of A, ldy >= rows of A. */
+/* Y = alpha A X + beta Y: sparse_gemm_array 'N','N' (sparse/hala_sparse_utils.hpp:127-133) through
+ * sparse_gemm (wax).  One kernel reads the matrix once and sums every column in the single-column
+ * product's order, so each column is bit-identical to hgb_csr_gemv (in the context's SpMV mode).
+ * ldx >= columns of A, ldy >= rows of A. */
 int hgb_csr_gemm(hgb_csr *A, int nrhs, double alpha, const void *x, int ldx, double beta, void *y, int ldy);
 
 /* R = M^-1 X (trans 'N') or M^-T X, column by column: gpu_ilu::apply with num_rhs

@@ -32,6 +32,34 @@ def test_gemm_columns_bit_exact(eng, rng):
         assert np.array_equal(y[c * n:(c + 1) * n], O.spmv("N", n, n, 1.0, p, i, v, X[c * n:(c + 1) * n], 0.0))
 
 
+@pytest.mark.parametrize("vdt", [torch.float64, torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("mode", ["exact", "fused"])
+def test_gemm_one_pass_equals_columns(eng, rng, vdt, mode):
+    """The SpMM reads the matrix once for all columns; every column must equal the single-column
+    product bit for bit, in both arithmetic modes, for column counts around the kernel's group of
+    four, beta != 0 and leading dimensions larger than n."""
+    from hala_gb300 import hgb as H
+    p, i, v = P.aniso3d(23, 21, 17)
+    n = len(p) - 1
+    xdt = torch.float64 if vdt == torch.float64 else torch.float32
+    A = E.make_sparse_matrix(eng, n, T(p), T(i), T(v).to(vdt))
+    eng.set_spmv_mode(mode)
+    try:
+        for k, ld, beta in ((1, n, 0.0), (4, n, 0.5), (7, n + 5, -1.25), (9, n + 1, 0.0)):
+            X = torch.from_numpy(rng.standard_normal(ld * k)).to(dev, xdt)
+            Y0 = torch.from_numpy(rng.standard_normal(ld * k)).to(dev, xdt)
+            Y = Y0.clone()
+            H.check(H.lib().hgb_csr_gemm(A.h, k, 0.75, E._p(X), ld, beta, E._p(Y), ld), "gemm")
+            for c in range(k):
+                yc = Y0[c * ld:c * ld + n].clone()
+                A.gemv("N", 0.75, X[c * ld:c * ld + n].contiguous(), beta, yc)
+                assert torch.equal(Y[c * ld:c * ld + n], yc), (k, c)
+                # rows between n and ld are not touched
+                assert torch.equal(Y[c * ld + n:(c + 1) * ld], Y0[c * ld + n:(c + 1) * ld])
+    finally:
+        eng.set_spmv_mode("exact")
+
+
 def test_ilu_apply_nrhs_bit_exact(eng, rng):
     p, i, v = P.aniso3d(24)
     n, k = len(p) - 1, 3
