@@ -11,9 +11,9 @@
 //
 // The CTA has two roles.  128 solver threads take one row each per step.  Every solver thread
 // streams its own row packets (three dependency codes and the row's slot, then the values and
-// diagonal terms, 16-byte pieces) D steps ahead into a private shared-memory ring with cp.async,
-// one commit group per step, so no handshake between warps sits on that path; a named barrier
-// ends each level.  Four fetcher warps take the coming steps in turn: a warp polls one value of
+// diagonal terms, 16-byte pieces) up to D steps ahead into a private shared-memory ring with
+// cp.async, half a ring per commit group, so no handshake between warps sits on that path; a
+// named barrier ends each level.  Four fetcher warps take the coming steps in turn: a warp polls one value of
 // its step in L2 until it is produced, then loads the first dependency on an earlier block of
 // every row of the step (re-polling the few not yet produced) and deposits each value in a
 // shared-memory ring.  A solver thread therefore waits on shared memory, not on an L2 round trip,

@@ -90,7 +90,8 @@ def test_cg_iteration_limit(eng, rng):
 @pytest.mark.parametrize("vdt", [torch.float64, torch.float32, torch.bfloat16])
 def test_cg_persistent_small_systems(eng, eng_fused, rng, vdt):
     """unpreconditioned CG on an L2-resident system runs as one persistent cooperative launch
-    (three grid barriers per iteration): against the oracle's loop in both SpMV modes"""
+    (two grid barriers per iteration, Ap by recurrence): against the oracle's loop in both SpMV
+    modes"""
     p, i, v = P.poisson2d(100)
     n = len(p) - 1
     b = rng.uniform(-1, 1, n)
