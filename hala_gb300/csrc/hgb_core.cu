@@ -48,7 +48,6 @@ int h2d_chunked(hgb_ctx *c, cudaStream_t s, void *dst, const void *src, size_t b
 int dev_error_to_status(int w) {
     if (w & DEV_ERR_TIMEOUT) return HGB_ERR_TIMEOUT;
     if (w & DEV_ERR_CSR) return HGB_ERR_CSR;
-    if (w & DEV_ERR_TMA) return HGB_ERR_TIMEOUT;
     if (w & DEV_ERR_ZERO_PIVOT) return HGB_ERR_ZERO_PIVOT;
     return HGB_OK;
 }

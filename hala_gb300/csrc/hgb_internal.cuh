@@ -30,7 +30,7 @@ int cuda_fail(cudaError_t e, const char *what);
     } while (0)
 
 // Device error word bits (written by kernels, read by the host after a launch sequence).
-enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_CSR = 2, DEV_ERR_ZERO_PIVOT = 4, DEV_ERR_TMA = 8 };
+enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_CSR = 2, DEV_ERR_ZERO_PIVOT = 4 };
 
 int dev_error_to_status(int word);
 

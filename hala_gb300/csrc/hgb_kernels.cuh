@@ -7,54 +7,9 @@ struct hgb_zilu;
 
 namespace hgb {
 
-// ------------------------------------------------------------ TMA / mbarrier helpers ----
+// ------------------------------------------------------------ shared-memory addressing ----
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// 1D bulk copy global -> shared, completion signalled on bar.  dst, src 16B aligned, bytes % 16 == 0.
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-
-// Bounded wait on a bulk-copy barrier.  A copy that never lands (it cannot, for in-bounds
-// aligned copies) would otherwise hang; on the limit the error word is set and the caller
-// proceeds with whatever the buffer holds, so the launch terminates.
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
-    long spins = 0;
-    while (!mbar_try_wait(bar, parity)) {
-        if (++spins > (1L << 22)) {
-            atomicOr(err, DEV_ERR_TMA);
-            return;
-        }
-    }
 }
 
 // Per-thread asynchronous copies global -> shared (cp.async), completion tracked per thread in
