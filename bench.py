@@ -344,6 +344,30 @@ def other_workloads(E, eng, dev, stream, flush, peak, steps=3, warm=2):
                                  "ms_adjoint": statistics.median(fw["adj"][1:]), "forward_iterations": fi.iterations,
                                  "adjoint_iterations": ai.iterations, "forward_rel_residual": res, "n": n,
                                  "loss": float(torch.sum((u - ut) ** 2))}
+
+    # 128^3 SpMM over 4 right-hand sides (sparse_gemm): one pass over the matrix against the four
+    # single-column products; algorithmic bytes = the matrix once + the columns of X and Y
+    p, i, v = P.aniso3d(GRID, coef=COEF)
+    n, k = len(p) - 1, 4
+    gp, gi, gv = T(p), T(i), T(v)
+    mm = {"nrhs": k, "n": n, "nnz": len(i), "l2": "flushed before each product"}
+    for name, vdt in (("f64", torch.float64), ("f32", torch.float32)):
+        A = E.make_sparse_matrix(eng, n, gp, gi, gv.to(vdt))
+        X = torch.randn(n * k, dtype=vdt, device=dev)
+        Y = torch.empty_like(X)
+        t1, _ = _events_ms(stream, lambda: A.gemm(k, 1.0, X, 0.0, Y), 5, 2, flush)
+
+        def cols():
+            for c in range(k):
+                A.gemv("N", 1.0, X[c * n:(c + 1) * n], 0.0, Y[c * n:(c + 1) * n])
+        t2, _ = _events_ms(stream, cols, 5, 2, flush)
+        launches += 7 * (1 + k)
+        vb = 8 if vdt == torch.float64 else 4
+        byts = (vb + 4) * len(i) + 4 * (n + 1) + 2 * k * vb * n
+        mm[name] = {"ms_one_pass": t1, "ms_column_by_column": t2, "gbs": byts / (t1 * 1e-3) / 1e9,
+                    "frac": byts / (t1 * 1e-3) / 1e9 / peak, "algorithmic_bytes": byts}
+        del A
+    out["spmm_aniso128_4rhs"] = mm
     return out, launches
 
 
@@ -398,7 +422,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=None, help="grid edge (default 128: the headline workload)")
     ap.add_argument("--kernels-only", action="store_true",
-                    help="only the SpMV and ILU-apply launches (for profiling captures)")
+                    help="only the SpMV, ILU-apply and SpMM launches (for profiling captures)")
     ap.add_argument("--no-other-workloads", action="store_true",
                     help="skip the other workloads and the library baseline (reported beside the headline)")
     args = ap.parse_args()
@@ -450,6 +474,8 @@ def main():
         y32 = torch.empty(n, dtype=torch.float32, device=dev)
         xs32 = gb.float()
         Ab = E.make_sparse_matrix(eng, n, gp, gi, gv.to(torch.bfloat16))
+        X4 = torch.randn(4 * n, dtype=torch.float64, device=dev)
+        Y4 = torch.empty_like(X4)
         for _ in range(3):
             flush_l2(flush)
             A64.gemv("N", 1.0, gb, 0.0, y64)
@@ -463,6 +489,8 @@ def main():
             M32.apply(xs32, y32)
             flush_l2(flush)
             M16.apply(xs32, y32)
+            flush_l2(flush)
+            A64.gemm(4, 1.0, X4, 0.0, Y4)   # one-pass SpMM over 4 columns
         torch.cuda.synchronize()
         print(json.dumps({"kernels_only": True, "n": n, "nnz": nnz}))
         return
