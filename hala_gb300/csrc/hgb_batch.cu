@@ -22,6 +22,7 @@
 namespace hgb {
 
 constexpr int kBatchSmem = 64 * 1024;    // per CTA: 4 float vectors of up to 4096 rows
+constexpr int kBatchUnroll = 4;          // matrix entries whose loads are issued together
 
 struct BatchArgs {
     int nitems;
@@ -85,8 +86,20 @@ __device__ void solve_system(const G &g, const BatchArgs &A, int s, float *sm) {
         for (int i = t0; i < n; i += ts) {
             const int row = r0 + i;
             double acc = A.b[row];
-            for (int k = __ldg(A.pntr + row); k < __ldg(A.pntr + row + 1); k++)
-                acc -= (double)__ldg(A.vals + k) * A.x[__ldg(A.indx + k)];
+            const int kb = __ldg(A.pntr + row), ke = __ldg(A.pntr + row + 1);
+            for (int k = kb; k < ke; k += kBatchUnroll) {
+                float vv[kBatchUnroll];
+                double xv[kBatchUnroll];
+#pragma unroll
+                for (int u = 0; u < kBatchUnroll; u++)
+                    if (k + u < ke) {
+                        vv[u] = __ldg(A.vals + k + u);
+                        xv[u] = A.x[__ldg(A.indx + k + u)];
+                    }
+#pragma unroll
+                for (int u = 0; u < kBatchUnroll; u++)
+                    if (k + u < ke) acc -= (double)vv[u] * xv[u];
+            }
             r[i] = (float)acc;
             d[i] = 0.0f;
             rr += acc * acc;
@@ -106,9 +119,23 @@ __device__ void solve_system(const G &g, const BatchArgs &A, int s, float *sm) {
             double pq = 0.0;
             for (int i = t0; i < n; i += ts) {
                 const int row = r0 + i;
+                const int kb = __ldg(A.pntr + row), ke = __ldg(A.pntr + row + 1);
                 float acc = 0.0f;
-                for (int k = __ldg(A.pntr + row); k < __ldg(A.pntr + row + 1); k++)
-                    acc += __ldg(A.vals + k) * p[__ldg(A.indx + k) - r0];
+                // entries kBatchUnroll at a time, their loads issued together (the row's matrix
+                // comes from L2: one round trip per group, not per entry); the sum keeps the order
+                for (int k = kb; k < ke; k += kBatchUnroll) {
+                    float vv[kBatchUnroll];
+                    int cc[kBatchUnroll];
+#pragma unroll
+                    for (int u = 0; u < kBatchUnroll; u++)
+                        if (k + u < ke) {
+                            vv[u] = __ldg(A.vals + k + u);
+                            cc[u] = __ldg(A.indx + k + u);
+                        }
+#pragma unroll
+                    for (int u = 0; u < kBatchUnroll; u++)
+                        if (k + u < ke) acc += vv[u] * p[cc[u] - r0];
+                }
                 q[i] = acc;
                 pq += (double)p[i] * acc;
             }
