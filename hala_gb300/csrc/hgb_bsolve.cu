@@ -13,8 +13,9 @@
 // streams its own row packets (three dependency codes and the row's slot, then the values and
 // diagonal terms, 16-byte pieces) up to D steps ahead into a private shared-memory ring with
 // cp.async, half a ring per commit group, so no handshake between warps sits on that path; a
-// named barrier ends each level.  Four fetcher warps take the coming steps in turn: a warp polls one value of
-// its step in L2 until it is produced, then loads the first dependency on an earlier block of
+// named barrier ends each level.  Three (FP64) or four (FP32) fetcher warps take the coming steps
+// in turn: a warp polls one value of its step in L2 until it is produced, then loads the first
+// dependency on an earlier block of
 // every row of the step (re-polling the few not yet produced) and deposits each value in a
 // shared-memory ring.  A solver thread therefore waits on shared memory, not on an L2 round trip,
 // when it needs a value from the block before.  The
@@ -46,8 +47,11 @@ namespace hgb {
 // per ILU(0) application at 128^3 and 0.40 against 0.27 ms at 96^3, the longer steps of the wider
 // CTA costing more than the hops saved.
 constexpr int kBsThreads = 128;
-constexpr int kBsFetchWarps = 4;  // fetcher warps: remote dependencies of the coming steps
-template <int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * kBsFetchWarps; }
+// Fetcher warps (the remote dependencies of the coming steps): four for FP32 solutions, three for
+// FP64 (measured at 128^3: FP32 mixed solve 71.0 ms with four, 75.7 with three, 90.2 with two,
+// slower again with eight; FP64 solve 122.6 ms with three against 125.3 with four).
+template <typename X> __host__ __device__ constexpr int bs_fetch_warps() { return sizeof(X) == 8 ? 3 : 4; }
+template <typename X, int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * bs_fetch_warps<X>(); }
 constexpr int kBsF = 32;          // steps in the remote-value ring
 using RingE = unsigned long long; // remote-ring entry (see Ring)
 constexpr long long kBsDirectAfter = 3000;   // cycles a solver thread waits on its ring entry before
@@ -264,13 +268,14 @@ template <> struct Ring<float> {
 // MODE 1: x_i = (alpha b_i - (sum_k v_k x_k)) [/ d_i]  (sparse_trsv_array's order).
 // UNIT: no division; RECIP: multiply by the stored FP32 reciprocal instead of dividing.
 template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
-__global__ void __launch_bounds__(bs_cta<NT>(), 1)
+__global__ void __launch_bounds__(bs_cta<X, NT>(), 1)
 bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
     constexpr int NV = BsCfg<V>::NV, D = bs_depth<V, NT>(), NP = 1 + NV;
-    constexpr int CTA = bs_cta<NT>(), RPL = NT / 32;   // fetcher rows per lane
+    constexpr int CTA = bs_cta<X, NT>(), RPL = NT / 32;   // fetcher rows per lane
+    constexpr int FW = bs_fetch_warps<X>();
     static_assert(NT % 32 == 0 && NT <= 256, "solver threads");
     static_assert((D & (D - 1)) == 0 && D >= 2, "ring shape");
-    static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * kBsFetchWarps, "remote ring shape");
+    static_assert((kBsF & (kBsF - 1)) == 0 && kBsF >= 2 * FW, "remote ring shape");
     if (A.skip && *A.skip) return;
     extern __shared__ __align__(128) unsigned char smem[];
     int4 *ring = (int4 *)smem;                          // [D][NP][NT]
@@ -323,7 +328,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
         __syncthreads();
 
         if (!solver) {
-            // ---- fetcher warps: warp w takes steps w, w+4, w+8, ... one at a time, polling the
+            // ---- fetcher warps: warp w takes steps w, w+FW, w+2FW, ... one at a time, polling the
             // step's remote values (RPL rows per lane) until all are deposited; the remote rows of
             // its next step are loaded meanwhile
             const int w = (t - NT) >> 5, l = t & 31;
@@ -345,8 +350,8 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             // solver threads' last steps cost 2 %).
             constexpr bool kPendSpread = sizeof(X) == 8;
             const int pchunk = ns > 0 ? (cnt + ns - 1) / ns : 0;   // rows per step (kPendSpread)
-            for (int s = w; s < ns; s += kBsFetchWarps) {
-                load_rj(s + kBsFetchWarps, jn);
+            for (int s = w; s < ns; s += FW) {
+                load_rj(s + FW, jn);
                 // the ring slot of step s was last used by step s - kBsF (the solver threads reset
                 // each entry to the pending pattern after reading it)
                 int spins = 0;
@@ -416,7 +421,7 @@ bsolve_kernel(BsArgs A, X alpha, const X *in, X *out, X *pend) {
             // fetchers' steps, in 16-byte stores
             if (!kPendSpread && pend) {
                 X *pb = pend + row_lo;
-                const int ft = t - NT, FT = 32 * kBsFetchWarps;
+                const int ft = t - NT, FT = 32 * FW;
                 const int pmis = (int)(((size_t)pb & 15) / sizeof(X));
                 const int phead = min(cnt, (E - pmis) % E), pbody = (cnt - phead) / E;
                 const X pv = Pending<X>::value();
@@ -671,7 +676,7 @@ static int bs_clusters_fit(hgb_ctx *c, int cl) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cl * 16);
-        cfg.blockDim = dim3(bs_cta<kBsThreads>());
+        cfg.blockDim = dim3(bs_cta<double, kBsThreads>());
         cfg.dynamicSmemBytes = smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -984,7 +989,7 @@ int bsolve_load_values(hgb_ctx *c, BlockSolve &S, const void *svals, int vsize, 
 
 template <typename V, typename X, int MODE, bool UNIT, bool RECIP, int NT>
 static int bs_launch_nt(hgb_ctx *c, const BlockSolve &S, const BsArgs &A, X alpha, const X *in, X *out, X *pend) {
-    constexpr int CTA = bs_cta<NT>();
+    constexpr int CTA = bs_cta<X, NT>();
     const size_t smem = bs_smem_bytes<V, X, NT>(S.R);
     // the attribute allows the largest block (16384 rows), so solves with smaller blocks launch too
     const size_t smem_max = bs_smem_bytes<V, X, NT>(16384);
