@@ -54,10 +54,11 @@ template <typename X> __host__ __device__ constexpr int bs_fetch_warps() { retur
 template <typename X, int NT> __host__ __device__ constexpr int bs_cta() { return NT + 32 * bs_fetch_warps<X>(); }
 constexpr int kBsF = 32;          // steps in the remote-value ring
 using RingE = unsigned long long; // remote-ring entry (see Ring)
-constexpr long long kBsDirectAfter = 6000;   // cycles a solver thread waits on its ring entry before
-                                             // reading the value from L2 itself (128^3: 3000 cycles
-                                             // cost the mixed solve 3 % and the FP64 solve 6 %, 1500
-                                             // cycles 15 %: the direct reads compete with the fetchers)
+// Cycles a solver thread waits on its ring entry before reading the value from L2 itself.  The
+// fetchers deliver every value anyway; a direct read only competes with them.  128^3 (mixed /
+// FP64 solve, ms): 1500 cycles 81.5 / 133.6, 3000 70.9 / 122.5, 6000 68.6 / 115.1-116.1,
+// 12000 68.1 / 114.7, 30000 67.8 / 114.7.
+constexpr long long kBsDirectAfter = 30000;
 constexpr int kBsStepCap = 1024;  // steps per block: the block's descriptors sit in shared memory
 constexpr int kBsInline = 3;      // dependencies carried in a row packet; more go to the overflow arrays
 
